@@ -1,0 +1,234 @@
+/* ugpu.h -- C ABI of the GB300 (sm_103a) backend for utopia's sparse-solver hot path.
+ *
+ * Every entry point returns an int status: UGPU_OK (0) on success, a negative
+ * UGPU_ERR_* code otherwise; ugpu_last_error(ctx) gives the message.  No C++
+ * exception crosses this boundary.  Handles own their device memory unless they
+ * were created by a *_wrap_* call (borrowed memory is never freed).  All work is
+ * issued on the context's stream; calls that return host scalars synchronise.
+ * One context per host thread (the reference's solvers are single-threaded host
+ * code; MPI ranks map to separate processes).
+ *
+ * Each declaration names the reference interface it replaces (paths relative to
+ * the utopia repository).
+ */
+#ifndef UGPU_H
+#define UGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(__GNUC__)
+#define UGPU_API __attribute__((visibility("default")))
+#else
+#define UGPU_API
+#endif
+
+/* status codes */
+#define UGPU_OK 0
+#define UGPU_ERR_CUDA (-1)
+#define UGPU_ERR_ARG (-2)
+#define UGPU_ERR_ALLOC (-3)
+#define UGPU_ERR_NOT_SPD (-4)
+#define UGPU_ERR_STATE (-5)
+#define UGPU_ERR_UNSUPPORTED (-6)
+#define UGPU_ERR_INTERNAL (-7)
+
+/* element types */
+#define UGPU_F64 0
+#define UGPU_F32 1
+#define UGPU_BF16 2
+
+/* matrix layouts used by the SpMV family */
+#define UGPU_FORMAT_CSR 0
+#define UGPU_FORMAT_SELL 1
+
+/* pointwise ops */
+#define UGPU_EMUL 0 /* out = a .* b */
+#define UGPU_EDIV 1 /* out = a ./ b */
+#define UGPU_EMIN 2
+#define UGPU_EMAX 3
+
+/* solver kinds */
+#define UGPU_SOLVER_CG 1          /* utopia::ConjugateGradient */
+#define UGPU_SOLVER_MULTIGRID 2   /* utopia::Multigrid */
+#define UGPU_SOLVER_INVDIAG 3     /* utopia::InvDiagPreconditioner */
+#define UGPU_SOLVER_MPRGP 4       /* utopia::MPRGP */
+#define UGPU_SOLVER_PGS 5         /* utopia::ProjectedGaussSeidel */
+#define UGPU_SOLVER_CHOLESKY 6    /* dense coarse-level direct solver (utopia::Factorization) */
+
+/* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
+#define UGPU_CONVERGED_FNORM_ABS 2
+#define UGPU_CONVERGED_FNORM_RELATIVE 3
+#define UGPU_CONVERGED_SNORM_RELATIVE 4
+#define UGPU_DIVERGED_MAX_IT (-5)
+#define UGPU_DIVERGED_NAN (-6)
+#define UGPU_DIVERGED_INDEFINITE (-8)
+
+typedef struct ugpu_ctx ugpu_ctx;
+typedef struct ugpu_vec ugpu_vec;
+typedef struct ugpu_mat ugpu_mat;
+typedef struct ugpu_solver ugpu_solver;
+
+/* SolutionStatus (utopia/solvers/utopia_SolutionStatus.hpp) plus GPU counters */
+typedef struct ugpu_solution_status {
+    int64_t iterates;
+    double gradient_norm;
+    double relative_gradient_norm;
+    double step_norm;
+    int32_t reason;
+    int32_t converged;
+    int64_t spmv_count;     /* operator applications of the outer solver */
+    double execution_time;  /* seconds, host wall clock of apply() */
+    int64_t kernel_launches;
+} ugpu_solution_status;
+
+/* ---------------------------------------------------------------- context ---- */
+/* Replaces the PETSc/MPI initialisation of utopia::Utopia::Init (utopia/utopia_Instance.cpp). */
+UGPU_API int ugpu_create(int device, ugpu_ctx **out);
+UGPU_API int ugpu_destroy(ugpu_ctx *ctx);
+UGPU_API const char *ugpu_last_error(const ugpu_ctx *ctx);
+UGPU_API int ugpu_synchronize(ugpu_ctx *ctx);
+/* kernels launched through this context so far (instrumentation) */
+UGPU_API int ugpu_launch_count(const ugpu_ctx *ctx, int64_t *out);
+/* the context's CUDA stream (cudaStream_t) for callers that interleave their own work */
+UGPU_API int ugpu_stream(const ugpu_ctx *ctx, void **out);
+
+/* ---------------------------------------------------------------- vectors ---- */
+/* Replaces PetscVector construction/zeros/values/wrap
+ * (utopia/backend/petsc/utopia_petsc_Vector.hpp:39-52; utopia/utopia_core/interfaces/utopia_Vector.hpp:21-94). */
+UGPU_API int ugpu_vec_create(ugpu_ctx *ctx, int64_t n, int dtype, ugpu_vec **out);
+/* borrowed device memory (cf. PetscVector::wrap with a no-op deleter,
+ * utopia/plug_in_and_out/isolver/utopia_isolver_lsolve.cpp:155-161) */
+UGPU_API int ugpu_vec_wrap_device(ugpu_ctx *ctx, void *device_ptr, int64_t n, int dtype, ugpu_vec **out);
+UGPU_API int ugpu_vec_destroy(ugpu_vec *v);
+UGPU_API int ugpu_vec_size(const ugpu_vec *v, int64_t *n, int *dtype);
+UGPU_API int ugpu_vec_device_ptr(const ugpu_vec *v, void **out);
+/* host array of the vector's dtype (synchronous) */
+UGPU_API int ugpu_vec_upload(ugpu_vec *v, const void *host);
+UGPU_API int ugpu_vec_download(const ugpu_vec *v, void *host);
+/* Vector::set(value) (utopia/utopia_core/interfaces/utopia_Vector.hpp) */
+UGPU_API int ugpu_vec_set(ugpu_vec *v, double value);
+/* y = x with dtype conversion (assignment `y = x`) */
+UGPU_API int ugpu_vec_copy(const ugpu_vec *x, ugpu_vec *y);
+
+/* ---------------------------------------------------------------- BLAS 1 ---- */
+/* BLAS1Tensor axpy / scale (utopia/utopia_core/interfaces/utopia_BLAS_Operands.hpp:10-54; PETSc VecAXPY
+ * utopia/backend/petsc/utopia_petsc_Vector.cpp:671): y = alpha*x + beta*y */
+UGPU_API int ugpu_axpby(double alpha, const ugpu_vec *x, double beta, ugpu_vec *y);
+/* dot (VecDot, utopia_petsc_Vector.cpp:59): FP64 accumulation, deterministic order */
+UGPU_API int ugpu_dot(const ugpu_vec *a, const ugpu_vec *b, double *out);
+/* fused dots (utopia::dots, utopia/utopia_core/expressions/utopia_DotVecVecs.hpp:86-130; VecMDot) */
+UGPU_API int ugpu_dots(int k, const ugpu_vec *const *a, const ugpu_vec *const *b, double *out);
+/* norm2 (VecNorm, utopia/backend/petsc/utopia_petsc_Vector.hpp:303) */
+UGPU_API int ugpu_norm2(const ugpu_vec *a, double *out);
+/* e_mul/e_div/e_min/e_max (utopia/utopia_core/interfaces/utopia_ElementWiseOperand.hpp:6-12) */
+UGPU_API int ugpu_pointwise(int op, const ugpu_vec *a, const ugpu_vec *b, ugpu_vec *out);
+/* e_pseudo_inv (utopia/utopia_core/utopia_ElementWisePseudoInverse.hpp:20-65) */
+UGPU_API int ugpu_pseudo_inverse(const ugpu_vec *in, ugpu_vec *out, double tol);
+/* multi_min (utopia/utopia_core/eval/utopia_MultiReduce.hpp:14-24), FP64 vectors */
+UGPU_API int ugpu_multi_min(const ugpu_vec *a, const ugpu_vec *b, double *out);
+
+/* ---------------------------------------------------------------- matrices ---- */
+/* CSR from host arrays (copied): PetscMatrix from CRS (utopia_isolver_lsolve.cpp:75-89 wraps
+ * rowptr/colidx/values).  int32 indices, FP64 values. */
+UGPU_API int ugpu_csr_create(ugpu_ctx *ctx, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t *rowptr,
+                             const int32_t *colidx, const double *values, ugpu_mat **out);
+/* CSR from device arrays of the same layout (copied) */
+UGPU_API int ugpu_csr_create_device(ugpu_ctx *ctx, int64_t nrows, int64_t ncols, int64_t nnz,
+                                    const int32_t *rowptr, const int32_t *colidx, const double *values,
+                                    ugpu_mat **out);
+UGPU_API int ugpu_mat_destroy(ugpu_mat *A);
+UGPU_API int ugpu_mat_info(const ugpu_mat *A, int64_t *nrows, int64_t *ncols, int64_t *nnz, int *value_dtype);
+/* structure and values back to host (values converted to FP64) */
+UGPU_API int ugpu_csr_download(const ugpu_mat *A, int32_t *rowptr, int32_t *colidx, double *values);
+/* overwrite the values of an existing pattern (host FP64 array, length nnz) */
+UGPU_API int ugpu_mat_update_values(ugpu_mat *A, const double *values);
+/* value-precision copy (FP64 -> FP32 / BF16 storage) for the mixed-precision hierarchy */
+UGPU_API int ugpu_mat_cast(const ugpu_mat *A, int value_dtype, ugpu_mat **out);
+/* choose the SpMV layout: UGPU_FORMAT_CSR or UGPU_FORMAT_SELL (sliced ELL, the default) */
+UGPU_API int ugpu_mat_set_format(ugpu_mat *A, int format);
+/* sliced-ELL statistics: slices, stored slots (incl. padding), diagonal-keyed slices */
+UGPU_API int ugpu_mat_sell_info(const ugpu_mat *A, int64_t *nslices, int64_t *nstored, int64_t *ndiag_slices,
+                                int *rows_per_slice);
+/* diag(A) (MatGetDiagonal, utopia/backend/petsc/utopia_petsc_Matrix.cpp:756) */
+UGPU_API int ugpu_diag(const ugpu_mat *A, ugpu_vec *d);
+/* explicit transpose (BLAS3Matrix::transpose, utopia_BLAS_Operands.hpp:135-171; used by IPRTransfer
+ * utopia/solvers/multilevel/transfer/utopia_IPRTransfer.hpp:28-39) */
+UGPU_API int ugpu_transpose(const ugpu_mat *A, ugpu_mat **out);
+/* C = A*B, full symbolic structure (MatMatMult; utopia/utopia_core/eval/utopia_Eval_Multiply.hpp:10-102) */
+UGPU_API int ugpu_spgemm(const ugpu_mat *A, const ugpu_mat *B, ugpu_mat **out);
+/* Galerkin product Ac = P^T A P (utopia::ptap -> MatPtAP,
+ * utopia/backend/petsc/eval/utopia_petsc_Eval_Multiply.cpp:12-61) */
+UGPU_API int ugpu_ptap(const ugpu_mat *A, const ugpu_mat *P, ugpu_mat **out);
+
+/* ---------------------------------------------------------------- SpMV family ---- */
+/* y = A x (MatMult, utopia/backend/petsc/utopia_petsc_Matrix.cpp:1358; Operator::apply
+ * utopia/utopia_core/interfaces/utopia_Operator.hpp:47).  x, y: FP64 or FP32 (both the same). */
+UGPU_API int ugpu_spmv(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y);
+/* y = A x + v (MatMultAdd, utopia_petsc_Matrix.cpp:1400-1404); y may alias v */
+UGPU_API int ugpu_spmv_add(const ugpu_mat *A, const ugpu_vec *x, const ugpu_vec *v, ugpu_vec *y);
+/* r = b - A x (Eval_Residual, utopia/utopia_core/eval/utopia_Eval_Residual.hpp:19-38), one pass */
+UGPU_API int ugpu_residual(const ugpu_mat *A, const ugpu_vec *b, const ugpu_vec *x, ugpu_vec *r);
+/* fused Jacobi sweep x_out = x + omega * d^+ (b - A x) (utopia/solvers/smoothers/utopia_Jacobi.hpp:131-141
+ * with the relaxation omega; omega = 1 is the reference); x_out must not alias x */
+UGPU_API int ugpu_jacobi_sweep(const ugpu_mat *A, const ugpu_vec *b, const ugpu_vec *x, double omega,
+                               ugpu_vec *x_out);
+
+/* ---------------------------------------------------------------- solvers ---- */
+/* Solvers mirror the reference classes.  Parameters use the reference's Configurable::read key
+ * names (utopia/solvers/linear/utopia_IterativeSolver.hpp:34-43 atol, rtol, stol, max_it, verbose;
+ * utopia/solvers/multilevel/utopia_MultiLevelBase.hpp:46-54 pre_smoothing_steps,
+ * post_smoothing_steps; utopia/solvers/multilevel/utopia_LinearMultiLevel.hpp:37-44
+ * must_generate_masks; utopia/solvers/smoothers/utopia_Chebyshev3level.hpp:39-56 scale_max_eig,
+ * scale_min_eig, power_method_tol, power_method_max_it; utopia/solvers/nonlinear/constrained/
+ * quadratic_programming/utopia_MPRGP.hpp:29-35 eig_comp_tol, power_method_max_it;
+ * utopia_ProjectedGaussSeidel.hpp:34-41 use_symmetric_sweep, n_local_sweeps) plus the
+ * backend's own keys: "smoother" (0 Jacobi, 1 Chebyshev3level, 2 PointJacobi), "omega",
+ * "precision" (UGPU_F64 / UGPU_F32 / UGPU_BF16 level storage of the multigrid), "flexible"
+ * (flexible CG outer iteration), "fix_semidefinite_operators", "graph_batch" (iterations per
+ * captured CUDA graph), "use_graphs", "multicolour" (PGS colouring), "format". */
+UGPU_API int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out);
+UGPU_API int ugpu_solver_destroy(ugpu_solver *s);
+UGPU_API int ugpu_solver_set(ugpu_solver *s, const char *key, double value);
+UGPU_API int ugpu_solver_get(const ugpu_solver *s, const char *key, double *value);
+/* PreconditionedSolver::set_preconditioner (utopia/solvers/linear/utopia_PreconditionedSolver.hpp:13-92);
+ * the preconditioner handle is borrowed and must outlive the solver */
+UGPU_API int ugpu_solver_set_preconditioner(ugpu_solver *s, ugpu_solver *prec);
+/* LinearMultiLevel::set_transfer_operators, interpolation operators ordered coarse -> fine
+ * (utopia_LinearMultiLevel.hpp:58-79); the matrices are copied */
+UGPU_API int ugpu_mg_set_transfer_operators(ugpu_solver *mg, int n, const ugpu_mat *const *interpolations);
+/* Galerkin operator of level l (0 = coarsest, after the std::reverse of
+ * utopia_LinearMultiLevel.hpp:224), returned as a new FP64 CSR copy */
+UGPU_API int ugpu_mg_level_matrix(const ugpu_solver *mg, int l, ugpu_mat **out);
+UGPU_API int ugpu_mg_n_levels(const ugpu_solver *mg, int *out);
+/* Chebyshev eigen-bounds of level l (Chebyshev3level::init_eigs, utopia_Chebyshev3level.hpp:118-121) */
+UGPU_API int ugpu_mg_eigs(const ugpu_solver *mg, int l, double *eig_max, double *eig_min);
+/* one V-cycle z = M^{-1} r from a zero initial guess (Multigrid::apply with max_it 1) */
+UGPU_API int ugpu_mg_vcycle(ugpu_solver *mg, const ugpu_vec *r, ugpu_vec *z);
+/* update(op): LinearSolver::update (utopia/solvers/linear/utopia_LinearSolver.hpp:70-73).  The
+ * matrix is borrowed and must stay alive while the solver uses it. */
+UGPU_API int ugpu_solver_update(ugpu_solver *s, const ugpu_mat *A);
+/* apply(rhs, x): LinearSolver::apply / Multigrid::apply / ConjugateGradient::solve(op, b, x) with the
+ * stored operator; x holds the initial guess on entry */
+UGPU_API int ugpu_solver_apply(ugpu_solver *s, const ugpu_vec *rhs, ugpu_vec *x);
+/* solve(A, b, x) = update(A) + apply(b, x) (OperatorBasedLinearSolver::solve,
+ * utopia/solvers/linear/utopia_MatrixFreeLinearSolver.hpp:54-57) */
+UGPU_API int ugpu_solver_solve(ugpu_solver *s, const ugpu_mat *A, const ugpu_vec *b, ugpu_vec *x);
+/* QPSolver::set_box_constraints (utopia/solvers/nonlinear/constrained/quadratic_programming/
+ * utopia_QPSolver.hpp:14-139); NULL bound = unbounded (fill_empty_bounds,
+ * utopia/solvers/nonlinear/constrained/utopia_BoxConstraints.hpp:281) */
+UGPU_API int ugpu_qp_set_box_constraints(ugpu_solver *s, const ugpu_vec *lb, const ugpu_vec *ub);
+UGPU_API int ugpu_solver_status(const ugpu_solver *s, ugpu_solution_status *out);
+
+/* ---------------------------------------------------------------- box constraints ---- */
+/* project(lb, ub, x) (utopia/solvers/nonlinear/constrained/utopia_VariableBoundSolverInterface.hpp:134-155) */
+UGPU_API int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* UGPU_H */

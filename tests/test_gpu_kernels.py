@@ -1,0 +1,191 @@
+"""GPU parity of the BLAS-1, SpMV-family, transpose and SpGEMM kernels against the oracle,
+called through the C ABI."""
+import hashlib
+
+import numpy as np
+import pytest
+
+import utopia_gb300 as U
+from utopia_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def bf16_round(a):
+    """Round float64 -> bf16 (nearest even) -> float64, as the storage conversion does."""
+    f = np.asarray(a, dtype=np.float32).view(np.uint32).astype(np.uint64)
+    lsb = (f >> 16) & 1
+    f = ((f + 0x7FFF + lsb) >> 16) << 16
+    return f.astype(np.uint32).view(np.float32).astype(np.float64)
+
+
+def random_csr(n, m, density, seed, long_rows=0):
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(seed)
+    M = sp.random(n, m, density=density, random_state=rng, format="csr")
+    if long_rows:
+        M = M.tolil()
+        for r in rng.choice(n, long_rows, replace=False):
+            cols = rng.choice(m, min(m, 700), replace=False)
+            M[r, cols] = rng.standard_normal(cols.size)
+        M = M.tocsr()
+    M.sort_indices()
+    return P.CSR.from_scipy(M)
+
+
+MATRICES = {
+    "lap2d": lambda: P.laplacian_2d(70, 33),
+    "lap3d": lambda: P.laplacian_3d(20, 19, 18),
+    "lognormal": lambda: P.lognormal_diffusion_3d(24, 5)[0],
+    "interp": lambda: P.interpolation_3d(16),
+    "random": lambda: random_csr(3001, 2777, 0.003, 11),
+    "random_long_rows": lambda: random_csr(1500, 1600, 0.004, 12, long_rows=5),
+    "empty_rows": lambda: P.CSR(5, 4, np.array([0, 0, 2, 2, 3, 3]), np.array([1, 3, 0]), np.array([1.0, -2.0, 3.0])),
+}
+
+
+def test_vector_roundtrip_and_blas1(ctx):
+    rng = np.random.default_rng(0)
+    a, b = rng.standard_normal(100_003), rng.standard_normal(100_003)
+    va, vb = U.Vector(ctx, a), U.Vector(ctx, b)
+    np.testing.assert_array_equal(va.numpy(), a)
+    d1, d2 = va.dot(vb), va.dot(vb)
+    assert d1 == d2  # deterministic reduction order
+    assert abs(d1 - a @ b) <= 1e-12 * np.abs(a * b).sum()
+    assert abs(va.norm2() - np.linalg.norm(a)) <= 1e-13 * np.linalg.norm(a)
+    vb.axpby(2.0, va, -0.5)
+    np.testing.assert_allclose(vb.numpy(), 2 * a - 0.5 * b, rtol=1e-15, atol=1e-15)
+    out = U.dots([(va, va), (va, vb)])
+    assert abs(out[0] - a @ a) <= 1e-12 * (a @ a)
+    v32 = U.Vector(ctx, n=a.size, dtype=U.F32)
+    va.copy_to(v32)
+    np.testing.assert_array_equal(v32.numpy(), a.astype(np.float32))
+
+
+def test_empty_vector_dot(ctx):
+    v = U.Vector(ctx, n=0)
+    assert v.dot(v) == 0.0
+
+
+@pytest.mark.parametrize("name", list(MATRICES))
+def test_spmv_fp64_matches_oracle(ctx, oracle, name):
+    A = MATRICES[name]()
+    x = np.random.default_rng(1).standard_normal(A.ncols)
+    yref = oracle.Matrix(A).matvec(x)
+    M = U.SparseMatrix(ctx, A)
+    vx, vy = U.Vector(ctx, x), U.Vector(ctx, n=A.nrows)
+    scale = np.abs(A.values) @ np.ones(1) if False else None
+    bound = 1e-14 * (np.abs(A.to_scipy()) @ np.abs(x)) + 1e-300
+    for fmt in (U.FORMAT_SELL, U.FORMAT_CSR):
+        M.set_format(fmt)
+        M.apply(vx, vy)
+        y = vy.numpy()
+        assert np.all(np.abs(y - yref) <= 4 * bound), (name, fmt)
+
+
+def test_stencil_operators_use_diagonal_slices(ctx):
+    for A in (P.laplacian_3d(32), P.lognormal_diffusion_3d(16, 1)[0]):
+        info = U.SparseMatrix(ctx, A).sell_info()
+        assert info["ndiag_slices"] == info["nslices"]
+        # padding below 2% of the nonzeros
+        assert info["nstored"] <= 1.02 * A.nnz + info["rows_per_slice"] * 7
+    info = U.SparseMatrix(ctx, P.interpolation_3d(16)).sell_info()
+    assert info["ndiag_slices"] < info["nslices"]
+
+
+@pytest.mark.parametrize("dtype", [U.F32, U.BF16])
+def test_spmv_low_precision_storage(ctx, dtype):
+    A = P.lognormal_diffusion_3d(20, 3)[0]
+    x = np.random.default_rng(2).standard_normal(A.ncols).astype(np.float32)
+    M = U.SparseMatrix(ctx, A).cast(dtype)
+    vals = A.values.astype(np.float32).astype(np.float64) if dtype == U.F32 else bf16_round(A.values)
+    ref = P.CSR(A.nrows, A.ncols, A.rowptr, A.colidx, vals).matvec(x.astype(np.float64))
+    vx, vy = U.Vector(ctx, x, dtype=U.F32), U.Vector(ctx, n=A.nrows, dtype=U.F32)
+    M.apply(vx, vy)
+    bound = 1e-6 * (np.abs(P.CSR(A.nrows, A.ncols, A.rowptr, A.colidx, vals).to_scipy()) @ np.abs(x))
+    assert np.all(np.abs(vy.numpy() - ref) <= 4 * bound + 1e-30)
+
+
+def test_residual_add_and_jacobi(ctx):
+    A = P.lognormal_diffusion_3d(16, 4)[0]
+    rng = np.random.default_rng(3)
+    x, b = rng.standard_normal(A.nrows), rng.standard_normal(A.nrows)
+    M = U.SparseMatrix(ctx, A)
+    vx, vb, vr = U.Vector(ctx, x), U.Vector(ctx, b), U.Vector(ctx, n=A.nrows)
+    Ax = A.matvec(x)
+    M.residual(vb, vx, vr)
+    np.testing.assert_allclose(vr.numpy(), b - Ax, rtol=1e-12, atol=1e-12 * np.abs(Ax).max())
+    M.apply_add(vx, vb, vr)
+    np.testing.assert_allclose(vr.numpy(), Ax + b, rtol=1e-12, atol=1e-12 * np.abs(Ax).max())
+    d = A.to_scipy().diagonal()
+    vo = U.Vector(ctx, n=A.nrows)
+    M.jacobi_sweep(vb, vx, 0.8, vo)
+    np.testing.assert_allclose(vo.numpy(), x + 0.8 / d * (b - Ax), rtol=1e-12, atol=1e-12)
+    vd = U.Vector(ctx, n=A.nrows)
+    M.diag(vd)
+    np.testing.assert_array_equal(vd.numpy(), d)
+
+
+def test_bad_csr_is_rejected(ctx):
+    bad_col = P.CSR(2, 2, np.array([0, 1, 2]), np.array([0, 5]), np.array([1.0, 1.0]))
+    with pytest.raises(U.UgpuError):
+        U.SparseMatrix(ctx, bad_col)
+    unsorted = P.CSR(1, 3, np.array([0, 2]), np.array([2, 0]), np.array([1.0, 1.0]))
+    with pytest.raises(U.UgpuError):
+        U.SparseMatrix(ctx, unsorted)
+    bad_ptr = P.CSR(2, 2, np.array([0, 3, 2]), np.array([0, 1]), np.array([1.0, 1.0]))
+    with pytest.raises(U.UgpuError):
+        U.SparseMatrix(ctx, bad_ptr)
+
+
+def _same_csr(gpu_mat, ora_mat, values="exact"):
+    rp, ci, v = gpu_mat.csr()
+    orp, oci, ov = ora_mat.arrays()
+    assert (rp == orp).all() and (ci == oci).all()
+    if values == "exact":
+        np.testing.assert_array_equal(v, ov)
+    else:
+        np.testing.assert_allclose(v, ov, rtol=1e-12, atol=1e-12 * np.abs(ov).max())
+
+
+@pytest.mark.parametrize("name", ["interp", "random", "random_long_rows", "empty_rows"])
+def test_transpose_bit_exact(ctx, oracle, name):
+    A = MATRICES[name]()
+    _same_csr(U.SparseMatrix(ctx, A).transpose(), oracle.Matrix(A).transpose(), "exact")
+
+
+def test_spgemm_structure_bit_exact(ctx, oracle):
+    A = random_csr(800, 900, 0.01, 5)
+    B = random_csr(900, 700, 0.01, 6)
+    _same_csr(U.SparseMatrix(ctx, A).matmul(U.SparseMatrix(ctx, B)), oracle.Matrix(A).matmul(oracle.Matrix(B)),
+              "close")
+
+
+def test_spgemm_long_rows_use_the_cta_path(ctx, oracle):
+    A = random_csr(300, 400, 0.02, 8, long_rows=3)
+    B = random_csr(400, 500, 0.02, 9)
+    _same_csr(U.SparseMatrix(ctx, A).matmul(U.SparseMatrix(ctx, B)), oracle.Matrix(A).matmul(oracle.Matrix(B)),
+              "close")
+
+
+def test_ptap_structure_bit_exact_fixture(ctx, oracle, laplace_hierarchy):
+    A, Is, _ = laplace_hierarchy
+    _same_csr(U.SparseMatrix(ctx, A).ptap(U.SparseMatrix(ctx, Is[2])), oracle.Matrix(A).ptap(oracle.Matrix(Is[2])),
+              "close")
+
+
+def test_ptap_full_size_128(ctx):
+    """Galerkin product at the 128^3 configuration: 64^3 coarse operator with the
+    27-point structure (nnz = 190^3 = 6,859,000), symmetric, and row sums of
+    P^T A P equal to P^T (A (P 1))."""
+    A = P.laplacian_3d(128)
+    Pm = P.interpolation_3d(128)
+    Ac = U.SparseMatrix(ctx, A).ptap(U.SparseMatrix(ctx, Pm))
+    assert Ac.nrows == 64 ** 3 and Ac.nnz == 190 ** 3
+    rp, ci, v = Ac.csr()
+    S = P.CSR(Ac.nrows, Ac.ncols, rp, ci, v).to_scipy()
+    assert abs(S - S.T).max() <= 1e-12
+    one = np.ones(Pm.ncols)
+    ref = Pm.to_scipy().T @ (A.to_scipy() @ (Pm.to_scipy() @ one))
+    np.testing.assert_allclose(S @ one, ref, rtol=1e-12, atol=1e-12)

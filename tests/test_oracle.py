@@ -1,0 +1,120 @@
+"""CPU tests of the oracle: pinned against the reference's own fixtures and tolerances,
+against scipy for the sparse kernels, and against the committed regression pins."""
+import ctypes
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from utopia_gb300 import problems as P
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def test_glibc_rand_matches_libc(oracle):
+    libc = ctypes.CDLL("libc.so.6")
+    libc.srand(1)
+    ref = np.array([libc.rand() for _ in range(2000)], dtype=np.int32)
+    assert (oracle.glibc_rand(2000) == ref).all()
+
+
+def test_spmv_matches_scipy(oracle):
+    A = P.laplacian_3d(10, 9, 8)
+    x = np.random.default_rng(7).standard_normal(A.ncols)
+    y = oracle.Matrix(A).matvec(x)
+    np.testing.assert_allclose(y, A.to_scipy() @ x, rtol=1e-14, atol=1e-13)
+
+
+def test_transpose_and_ptap_structure_match_scipy(oracle):
+    A = P.laplacian_3d(8)
+    Pm = P.interpolation_3d(8)
+    Ao, Po = oracle.Matrix(A), oracle.Matrix(Pm)
+    rp, ci, v = Po.transpose().arrays()
+    T = Pm.to_scipy().T.tocsr()
+    T.sort_indices()
+    assert (rp == T.indptr).all() and (ci == T.indices).all()
+    np.testing.assert_array_equal(v, T.data)
+    rp, ci, v = Ao.ptap(Po).arrays()
+    S = (Pm.to_scipy().T @ A.to_scipy() @ Pm.to_scipy()).tocsr()
+    S.sort_indices()
+    assert (rp == S.indptr).all() and (ci == S.indices).all()
+    np.testing.assert_allclose(v, S.data, rtol=1e-13, atol=1e-14)
+
+
+def test_galerkin_operators_are_27_point(oracle):
+    # P^T A P of the 7-point Laplacian with trilinear transfers is a 27-point stencil:
+    # nnz = (3n - 2)^3 on an n^3 grid (64^3: 6,859,000; 32^3: 830,584; 16^3: 97,336)
+    A, Ps, b = P.poisson3d_mg(32, 3)
+    mg = oracle.Multigrid(oracle.Matrix(A), Ps)
+    assert [mg.level_matrix(l).nnz for l in range(mg.n_levels)] == [22 ** 3, 46 ** 3, A.nnz]
+
+
+def test_reference_petsc_cg_mg_fixture(oracle, laplace_hierarchy):
+    """petsc_cg_mg (utopia/tests/petsc/utopia_PetscLinearSolverTest.cpp:400-477): CG with the
+    InvDiag preconditioner, then CG + multigrid (masks on, fix_semidefinite, max_it 1 per
+    preconditioner call) on the 4-level 2D fixture; the reference checks A x ~= rhs to 1e-6."""
+    A, Is, rhs = laplace_hierarchy
+    Am = oracle.Matrix(A)
+    x, st = oracle.cg_solve(Am, rhs, x0=rhs, precond="invdiag")
+    assert st["converged"]
+    mg = oracle.Multigrid(Am, Is, smoother="jacobi", pre=3, post=3, fix_semidefinite=True, masks=True)
+    x, st = oracle.cg_solve(Am, rhs, x0=rhs, precond="mg", mg=mg, atol=1e-10, rtol=1e-18, stol=1e-18)
+    assert np.allclose(A.matvec(x), rhs, atol=1e-6)
+
+
+def test_reference_petsc_mg_jacobi_fixture(oracle, laplace_hierarchy):
+    """petsc_mg_jacobi (utopia_PetscLinearSolverTest.cpp:479-508): multigrid with the
+    PointJacobi smoother as a solver; asserts approxeq(A x, rhs, 1e-6)."""
+    A, Is, rhs = laplace_hierarchy
+    mg = oracle.Multigrid(oracle.Matrix(A), Is, smoother="point_jacobi", pre=3, post=3)
+    x, st = mg.solve(rhs, atol=1e-9, rtol=1e-9, max_it=1000)
+    assert np.allclose(A.matvec(x), rhs, atol=1e-6)
+
+
+def test_mask_zero_on_dirichlet_rows(oracle, laplace_hierarchy):
+    A, Is, rhs = laplace_hierarchy
+    mg = oracle.Multigrid(oracle.Matrix(A), Is)
+    m = mg.mask(mg.n_levels - 1)
+    sA = A.to_scipy().tolil()
+    offdiag = np.array([any(j != i and abs(v) > 2.2e-10 for j, v in zip(sA.rows[i], sA.data[i]))
+                        for i in range(A.nrows)])
+    np.testing.assert_array_equal(m, offdiag.astype(float))
+
+
+def test_regression_pins(oracle):
+    pins = json.load(open(os.path.join(GOLDEN, "pins.json")))
+    A, b = P.poisson2d_cg(64, seed=0)
+    x, st = oracle.cg_solve(oracle.Matrix(A), b, atol=1e-8 * np.linalg.norm(b))
+    assert st["iterates"] == pins["cg_jacobi_poisson2d_64"]["iterates"]
+    A, Ps, b = P.poisson3d_mg(32, 3, seed=1)
+    Am = oracle.Matrix(A)
+    mg = oracle.Multigrid(Am, Ps, smoother="chebyshev", pre=3, post=3)
+    for l in range(mg.n_levels):
+        rp, ci, _ = mg.level_matrix(l).arrays()
+        h = hashlib.sha256(rp.tobytes() + ci.tobytes()).hexdigest()
+        assert h == pins["galerkin_poisson3d_32"][f"level{l}"]
+    for l in range(1, mg.n_levels):
+        np.testing.assert_allclose(mg.eigs(l), pins["galerkin_poisson3d_32"]["eigs"][l - 1], rtol=1e-12)
+    x, st = oracle.cg_solve(Am, b, precond="mg", mg=mg, atol=1e-10 * np.linalg.norm(b))
+    assert st["iterates"] == pins["mgpcg_chebyshev_poisson3d_32"]["iterates"]
+
+
+def test_unpreconditioned_cg_and_max_it(oracle):
+    A, b = P.poisson2d_cg(32, seed=3)
+    Am = oracle.Matrix(A)
+    x, st = oracle.cg_solve(Am, b, precond="none", atol=1e-10)
+    assert st["converged"] and np.linalg.norm(b - A.matvec(x)) < 1e-9
+    x, st = oracle.cg_solve(Am, b, precond="invdiag", atol=1e-30, max_it=5)
+    assert st["reason"] == -5 and st["iterates"] == 5
+
+
+def test_mixed_precision_restatement_reaches_tolerance(oracle):
+    A, Ps, b = P.lognormal_mg(24, 3, seed=2)
+    Am = oracle.Matrix(A)
+    for prec in ("fp32", "bf16"):
+        mg = oracle.Multigrid(Am, Ps, precision=prec, smoother="jacobi", pre=2, post=2, omega=0.8)
+        x, st = oracle.cg_solve(Am, b, precond="mg", mg=mg, atol=1e-8 * np.linalg.norm(b), flexible=True)
+        assert st["converged"]
+        assert np.linalg.norm(b - A.matvec(x)) <= 1e-8 * np.linalg.norm(b) * 1.0001

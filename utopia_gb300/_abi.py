@@ -1,0 +1,137 @@
+"""ctypes binding of libugpu (include/ugpu.h).
+
+The shared library is built in-tree by ``utopia_gb300.build``; this module never
+falls back to anything else: if the library or a GPU is missing, calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import re
+import threading
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "libugpu.so")
+HEADER = os.path.join(ROOT, "include", "ugpu.h")
+
+F64, F32, BF16 = 0, 1, 2
+FORMAT_CSR, FORMAT_SELL = 0, 1
+SOLVER_CG, SOLVER_MULTIGRID, SOLVER_INVDIAG, SOLVER_MPRGP, SOLVER_PGS, SOLVER_CHOLESKY = 1, 2, 3, 4, 5, 6
+
+_lock = threading.Lock()
+_lib = None
+
+
+class UgpuError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"ugpu error {code}: {msg}")
+        self.code = code
+
+
+class SolutionStatus(C.Structure):
+    _fields_ = [
+        ("iterates", C.c_int64),
+        ("gradient_norm", C.c_double),
+        ("relative_gradient_norm", C.c_double),
+        ("step_norm", C.c_double),
+        ("reason", C.c_int32),
+        ("converged", C.c_int32),
+        ("spmv_count", C.c_int64),
+        ("execution_time", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_vp, _d, _i64, _i32, _int = C.c_void_p, C.c_double, C.c_int64, C.c_int32, C.c_int
+_pp = C.POINTER(C.c_void_p)
+
+SIGNATURES = {
+    "ugpu_create": [_int, _pp],
+    "ugpu_destroy": [_vp],
+    "ugpu_last_error": [_vp],
+    "ugpu_synchronize": [_vp],
+    "ugpu_launch_count": [_vp, C.POINTER(_i64)],
+    "ugpu_stream": [_vp, _pp],
+    "ugpu_vec_create": [_vp, _i64, _int, _pp],
+    "ugpu_vec_wrap_device": [_vp, _vp, _i64, _int, _pp],
+    "ugpu_vec_destroy": [_vp],
+    "ugpu_vec_size": [_vp, C.POINTER(_i64), C.POINTER(_int)],
+    "ugpu_vec_device_ptr": [_vp, _pp],
+    "ugpu_vec_upload": [_vp, _vp],
+    "ugpu_vec_download": [_vp, _vp],
+    "ugpu_vec_set": [_vp, _d],
+    "ugpu_vec_copy": [_vp, _vp],
+    "ugpu_axpby": [_d, _vp, _d, _vp],
+    "ugpu_dot": [_vp, _vp, C.POINTER(_d)],
+    "ugpu_dots": [_int, _pp, _pp, C.POINTER(_d)],
+    "ugpu_norm2": [_vp, C.POINTER(_d)],
+    "ugpu_pointwise": [_int, _vp, _vp, _vp],
+    "ugpu_pseudo_inverse": [_vp, _vp, _d],
+    "ugpu_multi_min": [_vp, _vp, C.POINTER(_d)],
+    "ugpu_csr_create": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _pp],
+    "ugpu_csr_create_device": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _pp],
+    "ugpu_mat_destroy": [_vp],
+    "ugpu_mat_info": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_int)],
+    "ugpu_csr_download": [_vp, _vp, _vp, _vp],
+    "ugpu_mat_update_values": [_vp, _vp],
+    "ugpu_mat_cast": [_vp, _int, _pp],
+    "ugpu_mat_set_format": [_vp, _int],
+    "ugpu_mat_sell_info": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_int)],
+    "ugpu_diag": [_vp, _vp],
+    "ugpu_transpose": [_vp, _pp],
+    "ugpu_spgemm": [_vp, _vp, _pp],
+    "ugpu_ptap": [_vp, _vp, _pp],
+    "ugpu_spmv": [_vp, _vp, _vp],
+    "ugpu_spmv_add": [_vp, _vp, _vp, _vp],
+    "ugpu_residual": [_vp, _vp, _vp, _vp],
+    "ugpu_jacobi_sweep": [_vp, _vp, _vp, _d, _vp],
+    "ugpu_solver_create": [_vp, _int, _pp],
+    "ugpu_solver_destroy": [_vp],
+    "ugpu_solver_set": [_vp, C.c_char_p, _d],
+    "ugpu_solver_get": [_vp, C.c_char_p, C.POINTER(_d)],
+    "ugpu_solver_set_preconditioner": [_vp, _vp],
+    "ugpu_mg_set_transfer_operators": [_vp, _int, _pp],
+    "ugpu_mg_level_matrix": [_vp, _int, _pp],
+    "ugpu_mg_n_levels": [_vp, C.POINTER(_int)],
+    "ugpu_mg_eigs": [_vp, _int, C.POINTER(_d), C.POINTER(_d)],
+    "ugpu_mg_vcycle": [_vp, _vp, _vp],
+    "ugpu_solver_update": [_vp, _vp],
+    "ugpu_solver_apply": [_vp, _vp, _vp],
+    "ugpu_solver_solve": [_vp, _vp, _vp, _vp],
+    "ugpu_qp_set_box_constraints": [_vp, _vp, _vp],
+    "ugpu_solver_status": [_vp, C.POINTER(SolutionStatus)],
+    "ugpu_project": [_vp, _vp, _vp],
+}
+
+
+def header_symbols(path: str = HEADER):
+    """Function names declared with UGPU_API in include/ugpu.h."""
+    txt = open(path).read()
+    return sorted(set(re.findall(r"UGPU_API\s+[\w\s\*]+?\b(ugpu_\w+)\s*\(", txt)))
+
+
+def load(path: str = LIB_PATH):
+    """Load libugpu.so (raises if it has not been built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(path):
+                raise RuntimeError(f"libugpu.so is not built ({path}); run __graft_entry__.build()")
+            L = C.CDLL(path)
+            for name, args in SIGNATURES.items():
+                f = getattr(L, name)
+                f.argtypes = args
+                f.restype = C.c_char_p if name == "ugpu_last_error" else C.c_int
+            _lib = L
+    return _lib
+
+
+def check(rc: int, ctx=None):
+    if rc != 0:
+        msg = load().ugpu_last_error(ctx)
+        raise UgpuError(rc, msg.decode() if msg else "")

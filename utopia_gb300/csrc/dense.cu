@@ -1,0 +1,292 @@
+// Dense FP64 coarse-level direct solver.
+//
+// Reference: the coarse solver of utopia::Multigrid (Multigrid::coarse_solve,
+// utopia/solvers/multilevel/utopia_Multigrid.hpp:440-444), a PETSc Factorization
+// (utopia/backend/petsc/solvers/linear/utopia_petsc_Factorization.hpp).
+//
+// Set-up: the Galerkin operator of the coarsest level is densified, factored by a
+// blocked right-looking Cholesky (A = L L^T), L is inverted blockwise (Y = L^-1) and
+// the explicit inverse A^-1 = Y^T Y is formed.  Every coarse solve is then one
+// FP64 GEMV with A^-1, an L2-resident matrix for the coarse sizes of the hot path
+// (1728^2 and 4096^2 doubles), instead of two latency-bound triangular sweeps.
+// GB300's FP64 tensor rate is no higher than its FP64 FMA rate, so the set-up uses
+// FP64 FMA tiles.
+#include <cmath>
+
+#include "abi_util.cuh"
+#include "device_util.cuh"
+
+namespace ugpu {
+
+namespace {
+
+constexpr int NB = 64;  // Cholesky / inversion block size
+
+template <class V>
+__global__ void k_densify(const int32_t *rp, const int32_t *ci, const V *cv, int64_t n, double *D) {
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        for (int64_t c = threadIdx.x; c < n; c += blockDim.x) D[i * n + c] = 0.0;
+        __syncthreads();
+        for (int32_t k = rp[i] + threadIdx.x; k < rp[i + 1]; k += blockDim.x) D[i * n + ci[k]] = cvt<double>(cv[k]);
+        __syncthreads();
+    }
+}
+
+// unblocked Cholesky of the kb x kb diagonal block at (k0, k0) in shared memory
+__global__ void __launch_bounds__(256) k_potrf_diag(double *A, int64_t n, int64_t k0, int kb, int *bad) {
+    __shared__ double a[NB][NB + 1];
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        int i = e / kb, j = e % kb;
+        a[i][j] = A[(k0 + i) * n + k0 + j];
+    }
+    __syncthreads();
+    for (int j = 0; j < kb; ++j) {
+        __shared__ double d;
+        if (threadIdx.x == 0) {
+            double v = a[j][j];
+            if (!(v > 0.0)) {
+                atomicOr(bad, 1);
+                v = 1.0;
+            }
+            d = sqrt(v);
+            a[j][j] = d;
+        }
+        __syncthreads();
+        for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) a[i][j] /= d;
+        __syncthreads();
+        // trailing update of the lower triangle: a[i][c] -= a[i][j] * a[c][j], j < c <= i
+        const int m = kb - j - 1;
+        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+            int i = j + 1 + e / m, c = j + 1 + e % m;
+            if (c <= i) a[i][c] -= a[i][j] * a[c][j];
+        }
+        __syncthreads();
+    }
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        int i = e / kb, j = e % kb;
+        A[(k0 + i) * n + k0 + j] = (j <= i) ? a[i][j] : 0.0;
+    }
+}
+
+// rows below the diagonal block: x * L11^T = a  (one thread per row, in place)
+__global__ void __launch_bounds__(256) k_trsm_panel(double *A, int64_t n, int64_t k0, int kb) {
+    __shared__ double l[NB][NB + 1];
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        int i = e / kb, j = e % kb;
+        l[i][j] = A[(k0 + i) * n + k0 + j];
+    }
+    __syncthreads();
+    for (int64_t r = k0 + kb + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n;
+         r += int64_t(gridDim.x) * blockDim.x) {
+        double *row = A + r * n + k0;
+        for (int c = 0; c < kb; ++c) {
+            double s = row[c];
+            for (int q = 0; q < c; ++q) s -= row[q] * l[c][q];
+            row[c] = s / l[c][c];
+        }
+    }
+}
+
+// C[M x N] (ldc) += alpha * op(A) op(B); TA/TB: operand stored transposed.
+// lower_only: skip tiles strictly above the diagonal (SYRK-style update).
+template <bool TA, bool TB>
+__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double *A, int64_t lda,
+                                               const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                                               bool lower_only) {
+    constexpr int TM = 64, TN = 64, TK = 16;
+    __shared__ double As[TK][TM + 1];
+    __shared__ double Bs[TK][TN + 1];
+    const int bm = blockIdx.y * TM, bn = blockIdx.x * TN;
+    if (lower_only && bn > bm + TM - 1) return;
+    const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
+    double acc[4][4] = {};
+    for (int k0 = 0; k0 < K; k0 += TK) {
+        for (int e = threadIdx.x; e < TM * TK; e += 256) {
+            int mm = e / TK, kk = e % TK;
+            int gm = bm + mm, gk = k0 + kk;
+            double v = 0.0;
+            if (gm < M && gk < K) v = TA ? A[int64_t(gk) * lda + gm] : A[int64_t(gm) * lda + gk];
+            As[kk][mm] = v;
+        }
+        for (int e = threadIdx.x; e < TN * TK; e += 256) {
+            int nn = e / TK, kk = e % TK;
+            int gn = bn + nn, gk = k0 + kk;
+            double v = 0.0;
+            if (gn < N && gk < K) v = TB ? B[int64_t(gn) * ldb + gk] : B[int64_t(gk) * ldb + gn];
+            Bs[kk][nn] = v;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < TK; ++kk) {
+            double a[4], b[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                a[q] = As[kk][ty + 16 * q];
+                b[q] = Bs[kk][tx + 16 * q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; ++p)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int p = 0; p < 4; ++p)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            int gm = bm + ty + 16 * p, gn = bn + tx + 16 * q;
+            if (gm < M && gn < N) {
+                double *c = C + int64_t(gm) * ldc + gn;
+                *c = (beta == 0.0 ? 0.0 : beta * *c) + alpha * acc[p][q];
+            }
+        }
+}
+
+// L_bb X = B for ncols right-hand-side columns stored in rows r0..r0+kb of Y (ld n),
+// columns [0, ncols); X overwrites B, scaled by sign.  One thread per column.
+__global__ void __launch_bounds__(256) k_trsm_left_lower(const double *L, double *Y, int64_t n, int64_t r0, int kb,
+                                                         int ncols, double sign) {
+    __shared__ double l[NB][NB + 1];
+    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+        int i = e / kb, j = e % kb;
+        l[i][j] = L[(r0 + i) * n + r0 + j];
+    }
+    __syncthreads();
+    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncols; c += gridDim.x * blockDim.x) {
+        double x[NB];
+        for (int i = 0; i < kb; ++i) {
+            double s = Y[(r0 + i) * n + c];
+            for (int q = 0; q < i; ++q) s -= l[i][q] * x[q];
+            x[i] = s / l[i][i];
+        }
+        for (int i = 0; i < kb; ++i) Y[(r0 + i) * n + c] = sign * x[i];
+    }
+}
+
+__global__ void k_set_identity_block(double *Y, int64_t n, int64_t r0, int kb) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < kb * kb; e += gridDim.x * blockDim.x) {
+        int i = e / kb, j = e % kb;
+        Y[(r0 + i) * n + r0 + j] = (i == j) ? 1.0 : 0.0;
+    }
+}
+
+__global__ void k_zero(double *p, int64_t m) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m; i += int64_t(gridDim.x) * blockDim.x)
+        p[i] = 0.0;
+}
+
+// x = Ainv * r (one warp per row); input/output dtypes converted on the fly
+template <class TI, class TO>
+__global__ void __launch_bounds__(256) k_gemv(const double *M, int64_t n, const TI *r, TO *x, const int *done) {
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = w0; i < n; i += nw) {
+        const double *row = M + i * n;
+        double s = 0.0;
+        for (int64_t c = lane; c < n; c += 32) s = fma(__ldg(row + c), cvt<double>(__ldg(r + c)), s);
+        s = warp_sum(s);
+        if (lane == 0) x[i] = cvt<TO>(s);
+    }
+}
+
+}  // namespace
+
+bool DenseCholesky::factor(const Mat &A) {
+    UGPU_CHECK(A.nrows == A.ncols, UGPU_ERR_ARG, "coarse solver: square matrix required");
+    Context &c = *A.ctx;
+    ctx = &c;
+    n = A.nrows;
+    UGPU_CHECK(n <= 16384, UGPU_ERR_UNSUPPORTED, "coarse solver: dense size limited to 16384");
+    L.alloc(sizeof(double) * std::max<int64_t>(n * n, 1));
+    Ainv.alloc(sizeof(double) * std::max<int64_t>(n * n, 1));
+    if (n == 0) return true;
+    double *Lp = L.as<double>();
+    double *Y = Ainv.as<double>();  // holds L^-1 first
+    auto dens = [&](auto tag) {
+        using V = decltype(tag);
+        k_densify<V><<<int(std::min<int64_t>(n, 4096)), 256, 0, c.stream>>>(A.rowptr.as<int32_t>(),
+                                                                              A.colidx.as<int32_t>(), A.vals.as<V>(),
+                                                                              n, Lp);
+    };
+    if (A.vdtype == UGPU_F64) dens(double{});
+    else if (A.vdtype == UGPU_F32) dens(float{});
+    else dens(__nv_bfloat16{});
+    c.launches++;
+    UGPU_LAUNCH_CHECK();
+    Buffer bad;
+    bad.alloc(sizeof(int));
+    UGPU_CUDA(cudaMemsetAsync(bad.ptr, 0, sizeof(int), c.stream));
+    // blocked right-looking Cholesky
+    for (int64_t k0 = 0; k0 < n; k0 += NB) {
+        int kb = int(std::min<int64_t>(NB, n - k0));
+        k_potrf_diag<<<1, 256, 0, c.stream>>>(Lp, n, k0, kb, bad.as<int>());
+        int64_t rest = n - k0 - kb;
+        if (rest > 0) {
+            int g = int(std::min<int64_t>((rest + 255) / 256, 1024));
+            k_trsm_panel<<<g, 256, 0, c.stream>>>(Lp, n, k0, kb);
+            dim3 grid(unsigned((rest + 63) / 64), unsigned((rest + 63) / 64));
+            k_dgemm<false, true><<<grid, 256, 0, c.stream>>>(int(rest), int(rest), kb, -1.0, Lp + (k0 + kb) * n + k0,
+                                                             n, Lp + (k0 + kb) * n + k0, n, 1.0,
+                                                             Lp + (k0 + kb) * n + k0 + kb, n, true);
+            c.launches += 2;
+        }
+        c.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    int hbad = 0;
+    UGPU_CUDA(cudaMemcpyAsync(&hbad, bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    UGPU_CUDA(cudaStreamSynchronize(c.stream));
+    if (hbad) return false;
+    // Y = L^-1, block row by block row: Y[bi, 0:r0] = -L_ii^-1 (L[bi, 0:r0] Y[0:r0, 0:r0]); Y_ii = L_ii^-1
+    k_zero<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Y, n * n);
+    c.launches++;
+    for (int64_t r0 = 0; r0 < n; r0 += NB) {
+        int kb = int(std::min<int64_t>(NB, n - r0));
+        if (r0 > 0) {
+            dim3 grid(unsigned((r0 + 63) / 64), unsigned((kb + 63) / 64));
+            // T = L[r0:r0+kb, 0:r0] * Y[0:r0, 0:r0] written into Y[r0:r0+kb, 0:r0]
+            k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(kb, int(r0), int(r0), 1.0, Lp + r0 * n, n, Y, n, 0.0,
+                                                              Y + r0 * n, n, false);
+            int g = int(std::min<int64_t>((r0 + 255) / 256, 1024));
+            k_trsm_left_lower<<<g, 256, 0, c.stream>>>(Lp, Y, n, r0, kb, int(r0), -1.0);
+            c.launches += 2;
+        }
+        k_set_identity_block<<<16, 256, 0, c.stream>>>(Y, n, r0, kb);
+        // the identity block occupies columns r0..r0+kb; solve in place on those columns only
+        k_trsm_left_lower<<<1, 256, 0, c.stream>>>(Lp, Y + r0, n, r0, kb, kb, 1.0);
+        c.launches += 2;
+        UGPU_LAUNCH_CHECK();
+    }
+    // Ainv = Y^T Y  (stored in L's buffer, then swapped)
+    {
+        dim3 grid(unsigned((n + 63) / 64), unsigned((n + 63) / 64));
+        k_dgemm<true, false><<<grid, 256, 0, c.stream>>>(int(n), int(n), int(n), 1.0, Y, n, Y, n, 0.0, Lp, n, false);
+        c.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    std::swap(L, Ainv);  // Ainv now holds the inverse; L holds L^-1 (kept for diagnostics)
+    UGPU_CUDA(cudaStreamSynchronize(c.stream));
+    return true;
+}
+
+void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int *done) {
+    Context &c = *ctx;
+    if (n == 0) return;
+    int g = int(std::min<int64_t>((n * 32 + 255) / 256, int64_t(c.sms) * 8));
+    const double *M = Ainv.as<double>();
+    if (rdt == UGPU_F64 && xdt == UGPU_F64)
+        k_gemv<double, double><<<g, 256, 0, c.stream>>>(M, n, static_cast<const double *>(rhs),
+                                                         static_cast<double *>(x), done);
+    else if (rdt == UGPU_F32 && xdt == UGPU_F32)
+        k_gemv<float, float><<<g, 256, 0, c.stream>>>(M, n, static_cast<const float *>(rhs), static_cast<float *>(x),
+                                                      done);
+    else
+        throw Error(UGPU_ERR_UNSUPPORTED, "coarse solve: FP64 or FP32 vectors");
+    c.launches++;
+    UGPU_LAUNCH_CHECK();
+}
+
+}  // namespace ugpu

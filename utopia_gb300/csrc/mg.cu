@@ -1,0 +1,606 @@
+// Geometric/Galerkin multigrid on the GPU.
+//
+// Mirrors utopia::Multigrid (utopia/solvers/multilevel/utopia_Multigrid.hpp), its base
+// LinearMultiLevel (utopia/solvers/multilevel/utopia_LinearMultiLevel.hpp), the
+// IPRTransfer (utopia/solvers/multilevel/transfer/utopia_IPRTransfer.hpp), the masks
+// (utopia/solvers/multilevel/utopia_MultiLevelMask.hpp) and the smoothers Jacobi,
+// PointJacobi and Chebyshev3level (utopia/solvers/smoothers/).  Level 0 is the coarsest
+// level, as after the std::reverse of LinearMultiLevel::galerkin_assembly.
+//
+// Precision: "precision" = UGPU_F64 (plain form: everything FP64), UGPU_F32 or UGPU_BF16
+// (mixed form: level matrices and transfers stored in FP32 or BF16, vectors and
+// accumulation in FP32; the Galerkin products, the eigen-estimates and the coarse
+// Cholesky stay FP64).
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+#include "abi_util.cuh"
+#include "device_util.cuh"
+#include "solver.cuh"
+
+namespace ugpu {
+
+namespace {
+
+// glibc rand() (TYPE_3 additive feedback, degree 31, separation 3) for the PowerMethod
+// start vector v_i = rand()/RAND_MAX + 1 (utopia/solvers/eigensolvers/utopia_PowerMethod.hpp:99-106),
+// restated so the sequence does not depend on other rand() users in the process.
+struct GlibcRand {
+    uint32_t ring[31];
+    int f = 3, b = 0;
+    explicit GlibcRand(uint32_t seed) {
+        if (seed == 0) seed = 1;
+        int64_t word = seed;
+        ring[0] = seed;
+        for (int k = 1; k < 31; ++k) {
+            int64_t hi = word / 127773, lo = word % 127773;
+            word = 16807 * lo - 2836 * hi;
+            if (word < 0) word += 2147483647;
+            ring[k] = uint32_t(word);
+        }
+        for (int k = 0; k < 310; ++k) next();
+    }
+    int32_t next() {
+        ring[f] += ring[b];
+        int32_t out = int32_t(ring[f] >> 1);
+        f = (f + 1) % 31;
+        b = (b + 1) % 31;
+        return out;
+    }
+};
+
+// MultiLevelMask::generate_mask_from_matrix: m_i = 0 if row i has an off-diagonal |a| > tol, else 1
+template <class V>
+__global__ void k_mask_fine(const int32_t *rp, const int32_t *ci, const V *cv, int64_t n, double tol, double *m) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        double v = 1.0;
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] != i && fabs(cvt<double>(cv[k])) > tol) v = 0.0;
+        m[i] = v;
+    }
+}
+
+// IPRTransfer::boolean_restrict_or: m_c = min(1, R_bool m_f)
+__global__ void k_mask_restrict(const int32_t *rp, const int32_t *ci, const double *cv, int64_t n, double tol,
+                                const double *mf, double *mc) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        double s = 0.0;
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) s += (fabs(cv[k]) > tol ? 1.0 : 0.0) * mf[ci[k]];
+        mc[i] = s > 1.0 ? 1.0 : s;
+    }
+}
+
+// mask = |m - 1|, counts the zeros
+template <class T>
+__global__ void k_mask_final(const double *m, int64_t n, T *out, unsigned long long *zeros) {
+    unsigned long long z = 0;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        double v = fabs(m[i] - 1.0);
+        out[i] = T(v);
+        z += (v == 0.0);
+    }
+    atomicAdd(zeros, z);
+}
+
+// LinearMultiLevel::fix_semidefinite_operator: diagonal entries with |a_ii| < 1e-12 get +1
+__global__ void k_fix_semidefinite(const int32_t *rp, const int32_t *ci, double *cv, int64_t n) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] == i && fabs(cv[k]) < 1e-12) cv[k] += 1.0;
+}
+
+// PointJacobi::update: LU = A - diag(A) (diagonal entries set to 0, structure kept)
+__global__ void k_zero_diag(const int32_t *rp, const int32_t *ci, double *cv, int64_t n) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] == i) cv[k] = 0.0;
+}
+
+// smoother weights from the FP64 diagonal
+//   mode 0 (Jacobi):      w = omega * (|d| > 0 ? 1/d : 0)         (e_pseudo_inv with tol 0)
+//   mode 1 (PointJacobi): w = 1/d, with 0 replaced by 1            (check_indef)
+template <class T>
+__global__ void k_weights(const double *d, int64_t n, double omega, int mode, T *w) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        double v;
+        if (mode == 0) {
+            v = fabs(d[i]) > 0.0 ? 1.0 / d[i] : 0.0;
+            v = omega * v;
+        } else {
+            v = 1.0 / d[i];
+            if (v == 0.0) v = 1.0;
+        }
+        w[i] = T(v);
+    }
+}
+
+struct Level {
+    const Mat *A64 = nullptr;           // FP64 operator (the fine one is borrowed)
+    std::unique_ptr<Mat> A64own;
+    std::unique_ptr<Mat> Awork;         // storage-precision copy for the mixed form
+    std::unique_ptr<Mat> LU;            // PointJacobi off-diagonal part
+    const Mat *A() const { return Awork ? Awork.get() : A64; }
+    int64_t n = 0;
+    Buffer w;      // smoother weights (vector dtype)
+    Buffer mask;   // restriction mask (vector dtype); unused if all ones
+    bool has_mask = false;
+    double emax = 0, emin = 0;
+    std::vector<double> cheb_alpha, cheb_beta;
+    Buffer r, c, c2, rR, p0, p1, rr;  // work vectors (vector dtype)
+};
+
+struct Transfer {
+    std::unique_ptr<Mat> P64, R64;    // FP64 interpolation and explicit restriction R = P^T
+    std::unique_ptr<Mat> Pw, Rw;      // storage-precision copies
+    const Mat *P() const { return Pw ? Pw.get() : P64.get(); }
+    const Mat *R() const { return Rw ? Rw.get() : R64.get(); }
+};
+
+class Multigrid final : public Solver {
+public:
+    explicit Multigrid(Context *c) : Solver(c, UGPU_SOLVER_MULTIGRID) {
+        prm["pre_smoothing_steps"] = 3;   // utopia_MultiLevelBase.hpp:35-42
+        prm["post_smoothing_steps"] = 3;
+        prm["smoother"] = 1;              // 0 Jacobi, 1 Chebyshev3level, 2 PointJacobi
+        prm["omega"] = 1.0;
+        prm["precision"] = UGPU_F64;
+        prm["must_generate_masks"] = 1;   // Multigrid forces masks on, utopia_Multigrid.hpp:76
+        prm["fix_semidefinite_operators"] = 0;
+        prm["scale_max_eig"] = 1.2;       // utopia_Chebyshev3level.hpp:183
+        prm["scale_min_eig"] = 0.06;
+        prm["power_method_tol"] = 1e-2;   // utopia_PowerMethod.hpp:150-151
+        prm["power_method_max_it"] = 30;
+        prm["rand_seed"] = 1;
+        prm["mg_type"] = 1;               // V-cycle
+    }
+
+    void set_transfers(const std::vector<const Mat *> &P) {
+        transfers_.clear();
+        for (auto *p : P) {
+            UGPU_CHECK(p && p->vdtype == UGPU_F64, UGPU_ERR_ARG, "transfer operators must be FP64 matrices");
+            Transfer t;
+            t.P64 = cast_matrix(*p, UGPU_F64);  // deep copy
+            t.R64 = transpose(*t.P64);          // IPRTransfer: R = transpose(I)
+            transfers_.push_back(std::move(t));
+        }
+        ready_ = false;
+    }
+
+    int n_levels() const { return int(levels_.size()); }
+    const Level &level(int l) const { return levels_.at(l); }
+
+    // Multigrid::update(op): IterativeSolver::update + galerkin_assembly + smoothers + coarse solver
+    void update(const Mat *A) override {
+        UGPU_CHECK(A && A->nrows == A->ncols, UGPU_ERR_ARG, "multigrid: square operator required");
+        UGPU_CHECK(A->vdtype == UGPU_F64, UGPU_ERR_ARG, "multigrid: FP64 fine operator required");
+        UGPU_CHECK(!transfers_.empty(), UGPU_ERR_STATE, "Provide interpolation operators first");
+        op = A;
+        vdt_ = (int(get("precision")) == UGPU_F64) ? UGPU_F64 : UGPU_F32;
+        const int sdt = int(get("precision"));
+        const int L = int(transfers_.size()) + 1;
+        // galerkin_assembly (utopia_LinearMultiLevel.hpp:201-226): fine first, then reverse
+        std::vector<Level> lev(L);
+        lev[0].A64 = A;
+        for (int i = 1; i < L; ++i) {
+            const Transfer &t = transfers_[L - 1 - i];
+            UGPU_CHECK(t.P64->nrows == lev[i - 1].A64->nrows, UGPU_ERR_ARG,
+                       "interpolation operator rows do not match the finer level");
+            lev[i].A64own = ptap(*lev[i - 1].A64, *t.P64);
+            if (get("fix_semidefinite_operators") != 0) {
+                Mat &J = *lev[i].A64own;
+                k_fix_semidefinite<<<stream_grid(*ctx, J.nrows), kBlock, 0, ctx->stream>>>(
+                    J.rowptr.as<int32_t>(), J.colidx.as<int32_t>(), J.vals.as<double>(), J.nrows);
+                ctx->launches++;
+                finalize_matrix(J);
+            }
+            lev[i].A64 = lev[i].A64own.get();
+        }
+        std::reverse(lev.begin(), lev.end());
+        levels_ = std::move(lev);
+        for (auto &l : levels_) l.n = l.A64->nrows;
+        // storage-precision copies of operators and transfers
+        for (int l = 0; l < L; ++l) {
+            if (sdt != UGPU_F64) levels_[l].Awork = cast_matrix(*levels_[l].A64, sdt);
+        }
+        for (auto &t : transfers_) {
+            if (sdt != UGPU_F64) {
+                t.Pw = cast_matrix(*t.P64, sdt);
+                t.Rw = cast_matrix(*t.R64, sdt);
+            } else {
+                t.Pw.reset();
+                t.Rw.reset();
+            }
+        }
+        make_masks();
+        // Multigrid::update(): smoothers of levels 1..L-1 in order, then the coarse solver
+        GlibcRand rng(uint32_t(get("rand_seed")));
+        const int sm = int(get("smoother"));
+        for (int l = 1; l < L; ++l) setup_smoother(l, sm, rng);
+        UGPU_CHECK(coarse_.factor(*levels_[0].A64), UGPU_ERR_NOT_SPD,
+                   "coarse operator is not symmetric positive definite");
+        const size_t vs = dtype_size(vdt_);
+        for (auto &l : levels_) {
+            size_t b = vs * std::max<int64_t>(l.n, 1);
+            l.r.alloc(b);
+            l.c.alloc(b);
+            l.c2.alloc(b);
+            l.rR.alloc(b);
+            l.p0.alloc(b);
+            l.p1.alloc(b);
+            l.rr.alloc(b);
+        }
+        f64_r_.alloc(sizeof(double) * std::max<int64_t>(A->nrows, 1));
+        f64_z_.alloc(sizeof(double) * std::max<int64_t>(A->nrows, 1));
+        UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        ready_ = true;
+    }
+
+    int pc_dtype() const override { return vdt_; }
+
+    // one V-cycle from zero: z = M^{-1} r (vectors of pc_dtype(), fine-level size)
+    void pc_enqueue(const void *r, void *z, const int *done) override {
+        UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
+        cycle(n_levels() - 1, r, z, done);
+    }
+
+    // Multigrid::apply as a stand-alone solver (utopia_Multigrid.hpp:162-238)
+    void apply(const Vec &rhs, Vec &x) override {
+        UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
+        UGPU_CHECK(rhs.dtype == UGPU_F64 && x.dtype == UGPU_F64, UGPU_ERR_ARG, "multigrid: FP64 rhs and x");
+        const int64_t n = op->nrows;
+        UGPU_CHECK(rhs.n == n && x.n == n, UGPU_ERR_ARG, "multigrid: size mismatch");
+        double t0 = now_s();
+        int64_t l0 = ctx->launches;
+        st = ugpu_solution_status{};
+        double *res = f64_r_.as<double>();
+        auto residual = [&]() {
+            SpmvArgs a;
+            a.x = x.data();
+            a.v = rhs.data();
+            a.y = res;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_RESIDUAL;
+            launch_spmv(*ctx, *op, a);
+            DotArgs d{};
+            d.nd = 1;
+            d.a[0] = d.b[0] = res;
+            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
+            double v;
+            host_dots(*ctx, n, d, &v);
+            return std::sqrt(v);
+        };
+        double r_norm = residual(), r0 = r_norm;
+        int64_t it = 1;
+        bool conv = false;
+        Buffer r32, z32;
+        if (vdt_ == UGPU_F32) {
+            r32.alloc(sizeof(float) * std::max<int64_t>(n, 1));
+            z32.alloc(sizeof(float) * std::max<int64_t>(n, 1));
+        }
+        while (!conv) {
+            if (vdt_ == UGPU_F64) {
+                cycle(n_levels() - 1, res, f64_z_.ptr, nullptr);
+            } else {
+                enq_convert(*ctx, UGPU_F64, res, UGPU_F32, r32.ptr, n, nullptr);
+                cycle(n_levels() - 1, r32.ptr, z32.ptr, nullptr);
+                enq_convert(*ctx, UGPU_F32, z32.ptr, UGPU_F64, f64_z_.ptr, n, nullptr);
+            }
+            enq_axpy(*ctx, UGPU_F64, n, 1.0, f64_z_.ptr, x.data(), nullptr);
+            r_norm = residual();
+            conv = check_convergence(it, r_norm, r_norm / r0, 1);
+            it++;
+        }
+        st.converged = st.reason > 0;
+        st.spmv_count = it;
+        st.execution_time = now_s() - t0;
+        st.kernel_launches = ctx->launches - l0;
+    }
+
+    void eigs(int l, double *emax, double *emin) const {
+        *emax = levels_.at(l).emax;
+        *emin = levels_.at(l).emin;
+    }
+
+private:
+    std::vector<Transfer> transfers_;
+    std::vector<Level> levels_;
+    DenseCholesky coarse_;
+    int vdt_ = UGPU_F64;
+    bool ready_ = false;
+    Buffer f64_r_, f64_z_;
+
+    void make_masks() {
+        const int L = n_levels();
+        for (auto &l : levels_) l.has_mask = false;
+        if (get("must_generate_masks") == 0) return;
+        const double tol = std::numeric_limits<double>::epsilon() * 1e6;
+        std::vector<Buffer> m(L);
+        for (int l = 0; l < L; ++l) m[l].alloc(sizeof(double) * std::max<int64_t>(levels_[l].n, 1));
+        const Mat &Af = *levels_[L - 1].A64;
+        k_mask_fine<double><<<stream_grid(*ctx, Af.nrows), kBlock, 0, ctx->stream>>>(
+            Af.rowptr.as<int32_t>(), Af.colidx.as<int32_t>(), Af.vals.as<double>(), Af.nrows, tol,
+            m[L - 1].as<double>());
+        ctx->launches++;
+        for (int l = L - 1; l > 0; --l) {
+            const Mat &R = *transfers_[l - 1].R64;
+            k_mask_restrict<<<stream_grid(*ctx, R.nrows), kBlock, 0, ctx->stream>>>(
+                R.rowptr.as<int32_t>(), R.colidx.as<int32_t>(), R.vals.as<double>(), R.nrows, tol, m[l].as<double>(),
+                m[l - 1].as<double>());
+            ctx->launches++;
+        }
+        Buffer zeros;
+        zeros.alloc(sizeof(unsigned long long));
+        for (int l = 0; l < L; ++l) {
+            auto &lv = levels_[l];
+            lv.mask.alloc(dtype_size(vdt_) * std::max<int64_t>(lv.n, 1));
+            UGPU_CUDA(cudaMemsetAsync(zeros.ptr, 0, sizeof(unsigned long long), ctx->stream));
+            if (vdt_ == UGPU_F64)
+                k_mask_final<double><<<stream_grid(*ctx, lv.n), kBlock, 0, ctx->stream>>>(
+                    m[l].as<double>(), lv.n, lv.mask.as<double>(), zeros.as<unsigned long long>());
+            else
+                k_mask_final<float><<<stream_grid(*ctx, lv.n), kBlock, 0, ctx->stream>>>(
+                    m[l].as<double>(), lv.n, lv.mask.as<float>(), zeros.as<unsigned long long>());
+            ctx->launches++;
+            unsigned long long hz = 0;
+            UGPU_CUDA(cudaMemcpyAsync(&hz, zeros.ptr, sizeof(hz), cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+            lv.has_mask = hz > 0;  // an all-ones mask is skipped (multiplying by 1 is exact)
+        }
+        UGPU_LAUNCH_CHECK();
+    }
+
+    void setup_smoother(int l, int sm, GlibcRand &rng) {
+        Level &lv = levels_[l];
+        Mat &A64 = const_cast<Mat &>(*lv.A64);
+        ensure_diag(A64);
+        lv.w.alloc(dtype_size(vdt_) * std::max<int64_t>(lv.n, 1));
+        int g = stream_grid(*ctx, lv.n);
+        if (sm == 0 || sm == 2) {
+            int mode = (sm == 0) ? 0 : 1;
+            if (vdt_ == UGPU_F64)
+                k_weights<double><<<g, kBlock, 0, ctx->stream>>>(A64.diag.as<double>(), lv.n, get("omega"), mode,
+                                                                 lv.w.as<double>());
+            else
+                k_weights<float><<<g, kBlock, 0, ctx->stream>>>(A64.diag.as<double>(), lv.n, get("omega"), mode,
+                                                                lv.w.as<float>());
+            ctx->launches++;
+            UGPU_LAUNCH_CHECK();
+            if (sm == 2) {
+                auto lu = cast_matrix(A64, UGPU_F64);
+                k_zero_diag<<<g, kBlock, 0, ctx->stream>>>(lu->rowptr.as<int32_t>(), lu->colidx.as<int32_t>(),
+                                                           lu->vals.as<double>(), lu->nrows);
+                ctx->launches++;
+                finalize_matrix(*lu);
+                int sdt = int(get("precision"));
+                lv.LU = (sdt == UGPU_F64) ? std::move(lu) : cast_matrix(*lu, sdt);
+            }
+        } else {
+            power_method(lv, rng);
+            // Chebyshev3level::solve recurrence coefficients (utopia_Chebyshev3level.hpp:138-156)
+            const int nu = std::max(int(get("pre_smoothing_steps")), int(get("post_smoothing_steps")));
+            const double avg = (lv.emax + lv.emin) / 2.0, dif = (lv.emax - lv.emin) / 2.0;
+            lv.cheb_alpha.assign(std::max(nu, 1), 0.0);
+            lv.cheb_beta.assign(std::max(nu, 1), 0.0);
+            double alpha = 1.0 / avg;
+            lv.cheb_alpha[0] = alpha;
+            for (int k = 1; k < nu; ++k) {
+                double da = dif * alpha;
+                double beta = (k == 1 ? 0.5 : 0.25) * da * da;
+                alpha = 1.0 / (avg - (beta / alpha));
+                lv.cheb_beta[k] = beta;
+                lv.cheb_alpha[k] = alpha;
+            }
+        }
+    }
+
+    // PowerMethod::get_max_eig / compute_max_eig (utopia_PowerMethod.hpp:95-146) in FP64;
+    // Chebyshev3level::init_eigs scales the result (utopia_Chebyshev3level.hpp:118-121)
+    void power_method(Level &lv, GlibcRand &rng) {
+        const int64_t n = lv.n;
+        std::vector<double> h(n);
+        for (int64_t i = 0; i < n; ++i) h[i] = (double(rng.next()) / 2147483647.0) + 1;
+        Buffer v, w;
+        v.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        w.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        UGPU_CUDA(cudaMemcpyAsync(v.ptr, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
+        auto norm = [&](const Buffer &b) {
+            DotArgs d{};
+            d.nd = 1;
+            d.a[0] = d.b[0] = b.ptr;
+            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
+            double s;
+            host_dots(*ctx, n, d, &s);
+            return std::sqrt(s);
+        };
+        Vec vv, ww;
+        vv.ctx = ww.ctx = ctx;
+        vv.n = ww.n = n;
+        vv.buf.borrow(v.ptr, v.bytes);
+        ww.buf.borrow(w.ptr, w.bytes);
+        double s = 1. / norm(v);
+        launch_axpby(*ctx, n, s, vv, 0.0, vv);  // v = s * v
+        const double tol = get("power_method_tol");
+        const int64_t max_it = int64_t(get("power_method_max_it"));
+        double lambda = 0, lambda_old = 0;
+        int64_t it = 0;
+        bool conv = false;
+        while (!conv) {
+            SpmvArgs a;
+            a.x = v.ptr;
+            a.y = w.ptr;
+            a.vec_dtype = UGPU_F64;
+            launch_spmv(*ctx, *lv.A64, a);
+            lambda = norm(w);
+            launch_axpby(*ctx, n, 1. / lambda, ww, 0.0, vv);  // v = (1/lambda) w
+            it++;
+            conv = (std::fabs(lambda_old - lambda) < tol) || it > max_it;
+            lambda_old = lambda;
+        }
+        lv.emax = get("scale_max_eig") * lambda;
+        lv.emin = get("scale_min_eig") * lv.emax;
+    }
+
+    // ---------------------------------------------------------------- cycle ----
+    void spmv(const Mat &A, SpmvArgs a, const int *done) {
+        a.vec_dtype = vdt_;
+        a.done = done;
+        launch_spmv(*ctx, A, a);
+    }
+
+    // smoothing sweeps of Jacobi / PointJacobi from the iterate in bufs[cur]; returns
+    // the buffer index holding the result.  first_from_zero: the iterate is zero.
+    int jacobi_sweeps(Level &lv, int sm, const void *rhs, void *bufs[2], int cur, int nu, bool from_zero,
+                      const int *done) {
+        const Mat &Aop = (sm == 2) ? *lv.LU : *lv.A();
+        for (int s = 0; s < nu; ++s) {
+            if (from_zero && s == 0) {
+                // Jacobi: x = 0 + w .* (rhs - A*0) = w .* rhs; PointJacobi: x = w .* (rhs - LU*0)
+                enq_scale_into(*ctx, vdt_, lv.n, lv.w.ptr, rhs, bufs[cur], done);
+                continue;
+            }
+            SpmvArgs a;
+            a.x = bufs[cur];
+            a.v = rhs;
+            a.w = lv.w.ptr;
+            a.y = bufs[cur ^ 1];
+            a.epilogue = (sm == 2) ? EPI_PJACOBI : EPI_JACOBI;
+            spmv(Aop, a, done);
+            cur ^= 1;
+        }
+        return cur;
+    }
+
+    int jacobi_swaps(int nu, bool from_zero) const {
+        if (nu <= 0) return 0;
+        return from_zero ? nu - 1 : nu;
+    }
+
+    // Chebyshev3level::smooth(rhs, x) with nu iterations, x updated in place.
+    void chebyshev(Level &lv, const void *rhs, void *x, int nu, bool from_zero, const int *done) {
+        if (nu <= 0) return;
+        void *p[2] = {lv.p0.ptr, lv.p1.ptr};
+        if (from_zero) {
+            // r = A*0 - b = -b ; p = -1 * r
+            enq_neg_copy(*ctx, vdt_, lv.n, rhs, lv.rr.ptr, p[0], done);
+        } else {
+            SpmvArgs a;
+            a.x = x;
+            a.v = rhs;
+            a.vout = lv.rr.ptr;
+            a.y = p[0];
+            a.epilogue = EPI_CHEB0;
+            spmv(*lv.A(), a, done);
+        }
+        int cur = 0;
+        for (int k = 1; k < nu; ++k) {
+            SpmvArgs a;
+            a.x = p[cur];
+            a.vout = lv.rr.ptr;
+            a.x2 = x;
+            a.y = p[cur ^ 1];
+            a.s0 = lv.cheb_alpha[k - 1];
+            a.s1 = lv.cheb_beta[k];
+            a.s2 = lv.cheb_alpha[k];
+            a.s3 = (k == 1) ? lv.cheb_alpha[0] : 0.0;
+            a.epilogue = EPI_CHEB;
+            spmv(*lv.A(), a, done);
+            cur ^= 1;
+        }
+        if (nu == 1) enq_axpy(*ctx, vdt_, lv.n, lv.cheb_alpha[0], p[0], x, done);
+    }
+
+    // Multigrid::standard_cycle (utopia_Multigrid.hpp:252-367), V-cycle, c from zero.
+    void cycle(int l, const void *r, void *c_out, const int *done) {
+        if (l == 0) {
+            coarse_.solve(r, vdt_, c_out, vdt_, done);
+            return;
+        }
+        Level &lv = levels_[l];
+        Level &lc = levels_[l - 1];
+        const Transfer &t = transfers_[l - 1];
+        const int sm = int(get("smoother"));
+        const int pre = int(get("pre_smoothing_steps")), post = int(get("post_smoothing_steps"));
+        void *c;
+        int cur = 0;
+        void *bufs[2] = {c_out, lv.c2.ptr};
+        if (sm == 1) {
+            c = c_out;
+            if (pre <= 0) enq_set(*ctx, vdt_, lv.n, 0.0, c, done);
+            chebyshev(lv, r, c, pre, true, done);
+        } else {
+            const int swaps = jacobi_swaps(pre, true) + jacobi_swaps(post, false);
+            cur = swaps & 1;  // start so that the last sweep lands in c_out
+            if (pre <= 0) enq_set(*ctx, vdt_, lv.n, 0.0, bufs[cur], done);
+            cur = jacobi_sweeps(lv, sm, r, bufs, cur, pre, true, done);
+            c = bufs[cur];
+        }
+        // r_R = r - A c ; r_{l-1} = mask .* (R r_R)
+        {
+            SpmvArgs a;
+            a.x = c;
+            a.v = r;
+            a.y = lv.rR.ptr;
+            a.epilogue = EPI_RESIDUAL;
+            spmv(*lv.A(), a, done);
+        }
+        {
+            SpmvArgs a;
+            a.x = lv.rR.ptr;
+            a.y = lc.r.ptr;
+            if (lc.has_mask) {
+                a.w = lc.mask.ptr;
+                a.epilogue = EPI_SCALE;
+            }
+            spmv(*t.R(), a, done);
+        }
+        cycle(l - 1, lc.r.ptr, lc.c.ptr, done);
+        // c += I c_{l-1}
+        {
+            SpmvArgs a;
+            a.x = lc.c.ptr;
+            a.v = c;
+            a.y = c;
+            a.epilogue = EPI_ADD;
+            spmv(*t.P(), a, done);
+        }
+        if (sm == 1) {
+            chebyshev(lv, r, c, post, false, done);
+        } else {
+            cur = jacobi_sweeps(lv, sm, r, bufs, cur, post, false, done);
+            UGPU_CHECK(bufs[cur] == c_out, UGPU_ERR_INTERNAL, "multigrid: smoother buffer bookkeeping");
+        }
+    }
+};
+
+}  // namespace
+
+std::unique_ptr<Solver> make_multigrid(Context *c) { return std::make_unique<Multigrid>(c); }
+
+int mg_n_levels(const Solver *s) {
+    auto m = dynamic_cast<const Multigrid *>(s);
+    UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
+    return m->n_levels();
+}
+
+std::unique_ptr<Mat> mg_level_matrix(const Solver *s, int l) {
+    auto m = dynamic_cast<const Multigrid *>(s);
+    UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
+    UGPU_CHECK(l >= 0 && l < m->n_levels(), UGPU_ERR_ARG, "level out of range");
+    return cast_matrix(*m->level(l).A64, UGPU_F64);
+}
+
+void mg_eigs(const Solver *s, int l, double *emax, double *emin) {
+    auto m = dynamic_cast<const Multigrid *>(s);
+    UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
+    UGPU_CHECK(l >= 0 && l < m->n_levels(), UGPU_ERR_ARG, "level out of range");
+    m->eigs(l, emax, emin);
+}
+
+void mg_set_transfers(Solver *s, const std::vector<const Mat *> &P) {
+    auto m = dynamic_cast<Multigrid *>(s);
+    UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
+    m->set_transfers(P);
+}
+
+}  // namespace ugpu

@@ -1,0 +1,505 @@
+// Transpose, SpGEMM and the Galerkin product P^T A P.
+//
+// Reference: utopia::ptap -> PETSc MatPtAP (utopia/backend/petsc/eval/utopia_petsc_Eval_Multiply.cpp:12-61)
+// and the explicit R = transpose(I) of IPRTransfer
+// (utopia/solvers/multilevel/transfer/utopia_IPRTransfer.hpp:28-39).
+//
+// SpGEMM C = A B keeps the full symbolic structure (every structurally produced
+// entry, numerical zeros included) with ascending columns.  Each output row is
+// owned by one warp (or one CTA for long rows) with an open-addressing hash table
+// in shared memory.  Products are enumerated j-by-j in A-row order; within one j the
+// columns of B_j are distinct, so lanes never collide on a value slot and every
+// output entry sums its terms in A-row order: the result is deterministic and uses
+// the same summation order as the CPU oracle.
+#include <algorithm>
+
+#include "abi_util.cuh"
+#include "device_util.cuh"
+
+namespace ugpu {
+
+namespace {
+
+// ------------------------------------------------------------------------------------
+// exclusive scan of int64 (3 phases: per-CTA scan, scan of CTA sums, add)
+// ------------------------------------------------------------------------------------
+constexpr int kScanBlock = 512;
+constexpr int kScanItems = 8;
+
+__device__ __forceinline__ int64_t block_exclusive_scan(int64_t v, int64_t &total) {
+    __shared__ int64_t sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int64_t s = lane < nw ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int64_t y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) sh[lane] = s;
+    }
+    __syncthreads();
+    int64_t before = (w > 0 ? sh[w - 1] : 0) + x - v;
+    total = sh[nw - 1];
+    __syncthreads();
+    return before;
+}
+
+// in: n values; out: n+1 values (out[0] = 0, out[n] = total); block sums to bsum
+__global__ void k_scan_local(const int64_t *in, int64_t *out, int64_t n, int64_t *bsum) {
+    const int64_t base = int64_t(blockIdx.x) * kScanBlock * kScanItems;
+    int64_t loc[kScanItems];
+    int64_t s = 0;
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        int64_t i = base + int64_t(threadIdx.x) * kScanItems + q;
+        loc[q] = (i < n) ? in[i] : 0;
+        s += loc[q];
+    }
+    int64_t total;
+    int64_t pre = block_exclusive_scan(s, total);
+#pragma unroll
+    for (int q = 0; q < kScanItems; ++q) {
+        int64_t i = base + int64_t(threadIdx.x) * kScanItems + q;
+        if (i < n) out[i] = pre;
+        pre += loc[q];
+    }
+    if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+__global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *boff) {
+    const int64_t base = int64_t(blockIdx.x) * kScanBlock * kScanItems;
+    int64_t add = boff[blockIdx.x];
+    for (int q = 0; q < kScanItems; ++q) {
+        int64_t i = base + int64_t(threadIdx.x) * kScanItems + q;
+        if (i < n) out[i] += add;
+    }
+}
+
+__global__ void k_i64_to_i32(const int64_t *in, int32_t *out, int64_t n) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = int32_t(in[i]);
+}
+
+// ------------------------------------------------------------------------------------
+// transpose
+// ------------------------------------------------------------------------------------
+__global__ void k_col_count(const int32_t *ci, int64_t nnz, int64_t *cnt) {
+    for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nnz; k += int64_t(gridDim.x) * blockDim.x)
+        atomicAdd(reinterpret_cast<unsigned long long *>(cnt + ci[k]), 1ull);
+}
+
+template <class V>
+__global__ void k_transpose_scatter(const int32_t *rp, const int32_t *ci, const V *cv, int64_t n, int64_t *fill,
+                                    const int64_t *tp, int32_t *tci, V *tcv) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+            int32_t c = ci[k];
+            int64_t pos = tp[c] + int64_t(atomicAdd(reinterpret_cast<unsigned long long *>(fill + c), 1ull));
+            tci[pos] = int32_t(i);
+            tcv[pos] = cv[k];
+        }
+    }
+}
+
+// sort every row by column (insertion sort; rows of transposed transfer operators are short)
+template <class V>
+__global__ void k_sort_rows(const int64_t *tp, int64_t n, int32_t *tci, V *tcv) {
+    for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n; r += int64_t(gridDim.x) * blockDim.x) {
+        int64_t a = tp[r], b = tp[r + 1];
+        for (int64_t i = a + 1; i < b; ++i) {
+            int32_t key = tci[i];
+            V val = tcv[i];
+            int64_t j = i - 1;
+            while (j >= a && tci[j] > key) {
+                tci[j + 1] = tci[j];
+                tcv[j + 1] = tcv[j];
+                --j;
+            }
+            tci[j + 1] = key;
+            tcv[j + 1] = val;
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------
+// SpGEMM
+// ------------------------------------------------------------------------------------
+__global__ void k_row_upper_bound(const int32_t *arp, const int32_t *aci, const int32_t *brp, int64_t m,
+                                  int64_t *ub) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m; i += int64_t(gridDim.x) * blockDim.x) {
+        int64_t s = 0;
+        for (int32_t k = arp[i]; k < arp[i + 1]; ++k) {
+            int32_t j = aci[k];
+            s += brp[j + 1] - brp[j];
+        }
+        ub[i] = s;
+    }
+}
+
+constexpr int kWarpTable = 2048;      // max slots per warp (rows with upper bound <= 1024)
+constexpr int kWarpRowsUb = 1024;
+constexpr int kWarpsPerCta = 4;
+constexpr int kCtaTable = 8192;       // slots per CTA (rows with upper bound <= 4096)
+constexpr int kCtaRowsUb = 4096;
+constexpr int kCtaThreads = 256;
+
+__device__ __forceinline__ uint32_t hash_col(int32_t c, int mask) { return (uint32_t(c) * 2654435761u) & mask; }
+
+// insert column c; concurrent inserters hold distinct columns.  Returns the slot.
+__device__ __forceinline__ int hash_insert(int32_t *keys, int mask, int32_t c, int *n_unique) {
+    volatile int32_t *vk = keys;
+    uint32_t h = hash_col(c, mask);
+    while (true) {
+        int32_t k = vk[h];
+        if (k == c) return int(h);
+        if (k == -1) {
+            int32_t old = atomicCAS(&keys[h], -1, c);
+            if (old == -1) {
+                if (n_unique) atomicAdd(n_unique, 1);
+                return int(h);
+            }
+            if (old == c) return int(h);
+        }
+        h = (h + 1) & mask;
+    }
+}
+
+template <bool CTA>
+__device__ __forceinline__ void group_sync() {
+    if constexpr (CTA) __syncthreads();
+    else __syncwarp();
+}
+
+// table size for a row: power of two >= 2 * upper bound (load factor <= 1/2)
+__device__ __forceinline__ int table_size(int64_t ub, int cap) {
+    int t = 64;
+    while (t < 2 * ub && t < cap) t <<= 1;
+    return t;
+}
+
+// One output row with G cooperating threads.  NUMERIC = false: count unique columns;
+// true: accumulate values and write the row sorted by column.
+template <class V, bool NUMERIC, bool CTA>
+__device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, double *vals, int32_t *lkeys,
+                            double *lvals, int *s_count, const int32_t *arp, const int32_t *aci, const V *acv,
+                            const int32_t *brp, const int32_t *bci, const V *bcv, int64_t *cnt_out,
+                            const int32_t *crp, int32_t *cci, V *ccv) {
+    const int mask = TS - 1;
+    for (int s = tid; s < TS; s += G) {
+        keys[s] = -1;
+        if (NUMERIC) vals[s] = 0.0;
+    }
+    if (tid == 0) *s_count = 0;
+    group_sync<CTA>();
+    for (int32_t ka = arp[i]; ka < arp[i + 1]; ++ka) {
+        const int32_t j = aci[ka];
+        const double a = NUMERIC ? cvt<double>(acv[ka]) : 0.0;
+        const int32_t b1 = brp[j + 1];
+        for (int32_t kb = brp[j] + tid; kb < b1; kb += G) {
+            const int slot = hash_insert(keys, mask, bci[kb], NUMERIC ? nullptr : s_count);
+            if (NUMERIC) vals[slot] = fma(a, cvt<double>(bcv[kb]), vals[slot]);
+        }
+        group_sync<CTA>();  // every product of this j lands before the next j
+    }
+    if (!NUMERIC) {
+        if (tid == 0) cnt_out[i] = *s_count;
+        group_sync<CTA>();
+        return;
+    }
+    // compact the occupied slots, then place each entry at its rank (sorted by column)
+    for (int s = tid; s < TS; s += G) {
+        const int32_t k = keys[s];
+        if (k >= 0) {
+            const int p = atomicAdd(s_count, 1);
+            lkeys[p] = k;
+            lvals[p] = vals[s];
+        }
+    }
+    group_sync<CTA>();
+    const int u = *s_count;
+    const int32_t base = crp[i];
+    for (int e = tid; e < u; e += G) {
+        const int32_t k = lkeys[e];
+        int rank = 0;
+        for (int t = 0; t < u; ++t) rank += (lkeys[t] < k);
+        cci[base + rank] = k;
+        ccv[base + rank] = cvt<V>(lvals[e]);
+    }
+    group_sync<CTA>();
+}
+
+constexpr size_t kWarpSmem = (sizeof(int32_t) + sizeof(double)) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta;
+constexpr size_t kCtaSmem = (sizeof(int32_t) + sizeof(double)) * (kCtaTable + kCtaRowsUb);
+
+template <class V, bool NUMERIC>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_spgemm_warp(int64_t m, const int64_t *ub, const int32_t *arp,
+                                                                   const int32_t *aci, const V *acv,
+                                                                   const int32_t *brp, const int32_t *bci,
+                                                                   const V *bcv, int64_t *cnt, const int32_t *crp,
+                                                                   int32_t *cci, V *ccv, int *big_rows,
+                                                                   int *n_big) {
+    extern __shared__ unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *vals = reinterpret_cast<double *>(smem) + size_t(w) * kWarpTable;
+    double *lvals = reinterpret_cast<double *>(smem) + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
+    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta);
+    int32_t *keys = ibase + size_t(w) * kWarpTable;
+    int32_t *lkeys = ibase + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
+    __shared__ int s_count[kWarpsPerCta];
+    const int64_t gw = int64_t(blockIdx.x) * kWarpsPerCta + w;
+    const int64_t nw = int64_t(gridDim.x) * kWarpsPerCta;
+    for (int64_t i = gw; i < m; i += nw) {
+        const int64_t u = ub[i];
+        if (u > kWarpRowsUb) {
+            if (!NUMERIC && lane == 0) big_rows[atomicAdd(n_big, 1)] = int(i);
+            continue;
+        }
+        row_product<V, NUMERIC, false>(i, lane, 32, table_size(u, kWarpTable), keys, vals, lkeys, lvals,
+                                       &s_count[w], arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    }
+}
+
+template <class V, bool NUMERIC>
+__global__ void __launch_bounds__(kCtaThreads) k_spgemm_cta(const int *big_rows, int n_big, const int64_t *ub,
+                                                            const int32_t *arp, const int32_t *aci, const V *acv,
+                                                            const int32_t *brp, const int32_t *bci, const V *bcv,
+                                                            int64_t *cnt, const int32_t *crp, int32_t *cci, V *ccv) {
+    extern __shared__ unsigned char smem[];
+    double *vals = reinterpret_cast<double *>(smem);
+    double *lvals = vals + kCtaTable;
+    int32_t *keys = reinterpret_cast<int32_t *>(lvals + kCtaRowsUb);
+    int32_t *lkeys = keys + kCtaTable;
+    __shared__ int s_count;
+    for (int b = blockIdx.x; b < n_big; b += gridDim.x) {
+        const int64_t i = big_rows[b];
+        row_product<V, NUMERIC, true>(i, threadIdx.x, blockDim.x, table_size(ub[i], kCtaTable), keys, vals, lkeys,
+                                      lvals, &s_count, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    }
+}
+
+}  // namespace
+
+// host: exclusive scan of n int64 -> out[0..n] (out[n] = total); returns total
+int64_t device_exclusive_scan(Context &ctx, const int64_t *in, int64_t *out, int64_t n) {
+    const int64_t per = int64_t(kScanBlock) * kScanItems;
+    const int64_t nb = (n + per - 1) / per;
+    if (n == 0) {
+        UGPU_CUDA(cudaMemsetAsync(out, 0, sizeof(int64_t), ctx.stream));
+        return 0;
+    }
+    Buffer bsum, boff;
+    bsum.alloc(sizeof(int64_t) * nb);
+    boff.alloc(sizeof(int64_t) * (nb + 1));
+    k_scan_local<<<int(nb), kScanBlock, 0, ctx.stream>>>(in, out, n, bsum.as<int64_t>());
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    if (nb > 1) {
+        device_exclusive_scan(ctx, bsum.as<int64_t>(), boff.as<int64_t>(), nb);
+        k_scan_add<<<int(nb), kScanBlock, 0, ctx.stream>>>(out, n, boff.as<int64_t>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    } else {
+        UGPU_CUDA(cudaMemsetAsync(boff.ptr, 0, sizeof(int64_t), ctx.stream));
+    }
+    // total = last exclusive value + last input
+    int64_t last_ex = 0, last_in = 0;
+    UGPU_CUDA(cudaMemcpyAsync(&last_ex, out + n - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.stream));
+    UGPU_CUDA(cudaMemcpyAsync(&last_in, in + n - 1, sizeof(int64_t), cudaMemcpyDeviceToHost, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    int64_t total = last_ex + last_in;
+    UGPU_CUDA(cudaMemcpyAsync(out + n, &total, sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    return total;
+}
+
+std::unique_ptr<Mat> transpose(const Mat &A) {
+    Context &ctx = *A.ctx;
+    Buffer cnt, tp64, fill;
+    cnt.alloc(sizeof(int64_t) * std::max<int64_t>(A.ncols, 1));
+    tp64.alloc(sizeof(int64_t) * (A.ncols + 1));
+    fill.alloc(sizeof(int64_t) * std::max<int64_t>(A.ncols, 1));
+    UGPU_CUDA(cudaMemsetAsync(cnt.ptr, 0, cnt.bytes, ctx.stream));
+    UGPU_CUDA(cudaMemsetAsync(fill.ptr, 0, fill.bytes, ctx.stream));
+    if (A.nnz) {
+        k_col_count<<<stream_grid(ctx, A.nnz), kBlock, 0, ctx.stream>>>(A.colidx.as<int32_t>(), A.nnz,
+                                                                        cnt.as<int64_t>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    device_exclusive_scan(ctx, cnt.as<int64_t>(), tp64.as<int64_t>(), A.ncols);
+    auto T = make_csr_device(ctx, A.ncols, A.nrows, A.nnz, A.vdtype);
+    auto go = [&](auto tag) {
+        using V = decltype(tag);
+        if (A.nrows)
+            k_transpose_scatter<V><<<stream_grid(ctx, A.nrows), kBlock, 0, ctx.stream>>>(
+                A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), A.vals.as<V>(), A.nrows, fill.as<int64_t>(),
+                tp64.as<int64_t>(), T->colidx.as<int32_t>(), T->vals.as<V>());
+        if (A.ncols)
+            k_sort_rows<V><<<stream_grid(ctx, A.ncols), kBlock, 0, ctx.stream>>>(tp64.as<int64_t>(), A.ncols,
+                                                                                T->colidx.as<int32_t>(),
+                                                                                T->vals.as<V>());
+        ctx.launches += 2;
+    };
+    if (A.vdtype == UGPU_F64) go(double{});
+    else if (A.vdtype == UGPU_F32) go(float{});
+    else go(__nv_bfloat16{});
+    UGPU_LAUNCH_CHECK();
+    k_i64_to_i32<<<stream_grid(ctx, A.ncols + 1), kBlock, 0, ctx.stream>>>(tp64.as<int64_t>(),
+                                                                           T->rowptr.as<int32_t>(), A.ncols + 1);
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    finalize_matrix(*T);
+    return T;
+}
+
+std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
+    Context &ctx = *A.ctx;
+    UGPU_CHECK(A.ncols == B.nrows, UGPU_ERR_ARG, "spgemm: inner dimensions differ");
+    UGPU_CHECK(A.vdtype == UGPU_F64 && B.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "spgemm: FP64 operands");
+    const int64_t m = A.nrows;
+    Buffer ub, cnt, crp64, big, nbig;
+    ub.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
+    cnt.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
+    crp64.alloc(sizeof(int64_t) * (m + 1));
+    big.alloc(sizeof(int) * std::max<int64_t>(m, 1));
+    nbig.alloc(sizeof(int));
+    UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
+    const size_t warp_smem = kWarpSmem;
+    const size_t cta_smem = kCtaSmem;
+    static bool attr_done = false;
+    if (!attr_done) {
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(cta_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(cta_smem)));
+        attr_done = true;
+    }
+    const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
+    const int32_t *brp = B.rowptr.as<int32_t>(), *bci = B.colidx.as<int32_t>();
+    const double *acv = A.vals.as<double>(), *bcv = B.vals.as<double>();
+    if (m) {
+        k_row_upper_bound<<<stream_grid(ctx, m), kBlock, 0, ctx.stream>>>(arp, aci, brp, m, ub.as<int64_t>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    // largest per-row upper bound decides whether every row fits a shared-memory table
+    int64_t max_ub = 0;
+    {
+        std::vector<int64_t> h(m);
+        if (m) {
+            UGPU_CUDA(cudaMemcpyAsync(h.data(), ub.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, ctx.stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+        }
+        for (auto v : h) max_ub = std::max(max_ub, v);
+    }
+    UGPU_CHECK(max_ub <= kCtaRowsUb, UGPU_ERR_UNSUPPORTED,
+               "spgemm: a row has more than 4096 intermediate products (shared-memory hash table limit)");
+    const int gw = int(std::min<int64_t>((m + kWarpsPerCta - 1) / kWarpsPerCta, int64_t(ctx.sms) * 16));
+    // symbolic
+    if (m) {
+        k_spgemm_warp<double, false><<<std::max(gw, 1), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
+            m, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr, nullptr, nullptr,
+            big.as<int>(), nbig.as<int>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    int h_nbig = 0;
+    UGPU_CUDA(cudaMemcpyAsync(&h_nbig, nbig.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (h_nbig) {
+        k_spgemm_cta<double, false><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, cta_smem, ctx.stream>>>(
+            big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr,
+            nullptr, nullptr);
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    int64_t nnz = device_exclusive_scan(ctx, cnt.as<int64_t>(), crp64.as<int64_t>(), m);
+    UGPU_CHECK(nnz < (1ll << 31), UGPU_ERR_UNSUPPORTED, "spgemm: product has more than 2^31 entries");
+    auto C = make_csr_device(ctx, m, B.ncols, nnz, UGPU_F64);
+    k_i64_to_i32<<<stream_grid(ctx, m + 1), kBlock, 0, ctx.stream>>>(crp64.as<int64_t>(), C->rowptr.as<int32_t>(),
+                                                                     m + 1);
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    if (m) {
+        UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
+        k_spgemm_warp<double, true><<<std::max(gw, 1), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
+            m, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr, C->rowptr.as<int32_t>(),
+            C->colidx.as<int32_t>(), C->vals.as<double>(), big.as<int>(), nbig.as<int>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    if (h_nbig) {
+        k_spgemm_cta<double, true><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, cta_smem, ctx.stream>>>(
+            big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr, C->rowptr.as<int32_t>(),
+            C->colidx.as<int32_t>(), C->vals.as<double>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    finalize_matrix(*C);
+    return C;
+}
+
+std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P) {
+    UGPU_CHECK(A.nrows == A.ncols && P.nrows == A.nrows, UGPU_ERR_ARG, "ptap: dimension mismatch");
+    auto R = transpose(P);
+    auto AP = spgemm(A, P);
+    return spgemm(*R, *AP);
+}
+
+}  // namespace ugpu
+
+using namespace ugpu;
+
+extern "C" {
+
+int ugpu_transpose(const ugpu_mat *A, ugpu_mat **out) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(out);
+    auto T = transpose(A->impl);
+    auto h = new ugpu_mat;
+    h->impl = std::move(*T);
+    *out = h;
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
+
+int ugpu_spgemm(const ugpu_mat *A, const ugpu_mat *B, ugpu_mat **out) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(B);
+    UGPU_REQUIRE(out);
+    auto C = spgemm(A->impl, B->impl);
+    auto h = new ugpu_mat;
+    h->impl = std::move(*C);
+    *out = h;
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
+
+int ugpu_ptap(const ugpu_mat *A, const ugpu_mat *P, ugpu_mat **out) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(P);
+    UGPU_REQUIRE(out);
+    auto C = ptap(A->impl, P->impl);
+    auto h = new ugpu_mat;
+    h->impl = std::move(*C);
+    *out = h;
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
+
+}  // extern "C"
