@@ -223,6 +223,10 @@ UGPU_API int ugpu_solver_solve(ugpu_solver *s, const ugpu_mat *A, const ugpu_vec
  * utopia/solvers/nonlinear/constrained/utopia_BoxConstraints.hpp:281) */
 UGPU_API int ugpu_qp_set_box_constraints(ugpu_solver *s, const ugpu_vec *lb, const ugpu_vec *ub);
 UGPU_API int ugpu_solver_status(const ugpu_solver *s, ugpu_solution_status *out);
+/* colouring used by the multicolour projected Gauss-Seidel sweep (greedy first-fit in index
+ * order; red-black (x + y) mod 2 on the 5-point grid).  The reference sweeps rows
+ * lexicographically (utopia_ProjectedGaussSeidel.hpp:213-254); colour may be NULL. */
+UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *ncolours);
 
 /* ---------------------------------------------------------------- box constraints ---- */
 /* project(lb, ub, x) (utopia/solvers/nonlinear/constrained/utopia_VariableBoundSolverInterface.hpp:134-155) */

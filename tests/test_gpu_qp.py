@@ -1,0 +1,102 @@
+"""Box-constrained QP on the GPU: MPRGP and multicolour projected Gauss-Seidel against the
+oracle (same algorithms restated on the CPU); active sets compared bit-exactly."""
+import numpy as np
+import pytest
+
+import utopia_gb300 as U
+from utopia_gb300 import problems as P
+
+pytestmark = pytest.mark.gpu
+
+
+def obstacle(N, scaled):
+    h = 1.0 / (N + 1)
+    return P.obstacle_qp(N, seed=3, rhs=-5 * h * h if scaled else -1.0)
+
+
+def active(x, lb):
+    return x == lb
+
+
+@pytest.mark.parametrize("N,scaled", [(64, True), (128, False)])
+def test_mprgp_matches_oracle(ctx, oracle, N, scaled):
+    A, b, lb, ub = obstacle(N, scaled)
+    Am = oracle.Matrix(A)
+    xo, so = oracle.mprgp_solve(Am, b, lb, ub, atol=1e-10, rtol=1e-14, max_it=5000)
+    s = U.MPRGP(ctx, atol=1e-10, rtol=1e-14, max_it=5000)
+    vlb, vub = U.Vector(ctx, lb), U.Vector(ctx, ub)
+    s.set_box_constraints(vlb, vub)
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    st = s.solution_status()
+    xg = x.numpy()
+    assert st["converged"] and so["converged"]
+    np.testing.assert_allclose(s.get("lambda_max"), so["lambda_max"], rtol=1e-10)
+    assert np.array_equal(active(xg, lb), active(xo, lb))
+    assert np.linalg.norm(xg - xo) <= 1e-8 * np.linalg.norm(xo)
+    assert oracle.projected_gradient_norm(Am, b, lb, ub, xg) <= 1e-9
+    assert abs(st["iterates"] - so["iterates"]) <= max(2, 0.05 * so["iterates"])
+
+
+def test_mprgp_unbounded_is_cg_like(ctx, oracle):
+    A, b = P.poisson2d_cg(24, 2)
+    s = U.MPRGP(ctx, atol=1e-10, rtol=1e-14, max_it=2000)
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    assert np.linalg.norm(A.matvec(x.numpy()) - b) <= 1e-9
+
+
+def test_pgs_colouring_is_red_black(ctx, oracle):
+    A, b, lb, ub = obstacle(40, True)
+    s = U.ProjectedGaussSeidel(ctx)
+    s.update(U.SparseMatrix(ctx, A))
+    col, nc = s.colouring()
+    ocol, onc = oracle.colouring(oracle.Matrix(A))
+    assert nc == onc == 2
+    np.testing.assert_array_equal(col, ocol)
+    i = np.arange(A.nrows)
+    np.testing.assert_array_equal(col, ((i % 40) + (i // 40)) % 2)
+
+
+def test_pgs_colouring_general_graph(ctx, oracle):
+    A = P.lognormal_diffusion_3d(12, 1)[0]  # 7-point: 2 colours
+    L = P.CSR.from_scipy(P.interpolation_3d(8).to_scipy() @ P.interpolation_3d(8).to_scipy().T)  # denser graph
+    for M in (A, L):
+        s = U.ProjectedGaussSeidel(ctx)
+        s.update(U.SparseMatrix(ctx, M))
+        col, nc = s.colouring()
+        ocol, onc = oracle.colouring(oracle.Matrix(M))
+        assert nc == onc
+        np.testing.assert_array_equal(col, ocol)
+
+
+def test_pgs_multicolour_matches_oracle(ctx, oracle):
+    A, b, lb, ub = obstacle(48, True)
+    Am = oracle.Matrix(A)
+    col, nc = oracle.colouring(Am)
+    xo, so = oracle.pgs_solve(Am, b, lb, ub, stol=1e-10, max_it=20000, colour=col)
+    s = U.ProjectedGaussSeidel(ctx, stol=1e-10, max_it=20000)
+    s.set_box_constraints(U.Vector(ctx, lb), U.Vector(ctx, ub))
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    st = s.solution_status()
+    xg = x.numpy()
+    assert st["converged"]
+    assert abs(st["iterates"] - so["iterates"]) <= 1
+    assert np.array_equal(active(xg, lb), active(xo, lb))
+    assert np.linalg.norm(xg - xo) <= 1e-7 * np.linalg.norm(xo)
+
+
+def test_pgs_and_mprgp_agree_on_the_active_set(ctx, oracle):
+    A, b, lb, ub = obstacle(48, True)
+    Am = oracle.Matrix(A)
+    xm, _ = oracle.mprgp_solve(Am, b, lb, ub, atol=1e-11, rtol=1e-14, max_it=5000)
+    s = U.ProjectedGaussSeidel(ctx, atol=1e-9, max_it=200000, projected_gradient_stop=1)
+    s.set_box_constraints(U.Vector(ctx, lb), U.Vector(ctx, ub))
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    xg = x.numpy()
+    assert s.solution_status()["converged"]
+    assert oracle.projected_gradient_norm(Am, b, lb, ub, xg) <= 1e-9
+    # same contact set away from the free boundary's rounding band
+    assert (np.abs(xg - lb) < 1e-12).sum() == pytest.approx((np.abs(xm - lb) < 1e-12).sum(), abs=2)

@@ -373,3 +373,11 @@ class MPRGP(_QPSolver):
 
 class ProjectedGaussSeidel(_QPSolver):
     KIND = _abi.SOLVER_PGS
+
+    def colouring(self):
+        nc = C.c_int()
+        self.ctx.check(self.ctx.lib.ugpu_pgs_colouring(self.h, None, C.byref(nc)))
+        n = self._keep[-1].nrows
+        out = np.empty(n, np.int32)
+        self.ctx.check(self.ctx.lib.ugpu_pgs_colouring(self.h, _ptr(out), C.byref(nc)))
+        return out, nc.value

@@ -106,6 +106,7 @@ SIGNATURES = {
     "ugpu_qp_set_box_constraints": [_vp, _vp, _vp],
     "ugpu_solver_status": [_vp, C.POINTER(SolutionStatus)],
     "ugpu_project": [_vp, _vp, _vp],
+    "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
 }
 
 

@@ -245,6 +245,7 @@ struct SpmvArgs {
     void *vout = nullptr;       // in/out vector of the Chebyshev epilogues (residual)
     void *x2 = nullptr;         // in/out iterate of the Chebyshev epilogues
     double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+    int x2_zero = 0;            // Chebyshev: the iterate x2 starts at zero (not read)
     // fused CG direction: xin = x + beta_scale * (*beta_ptr) * p, written back to pout
     const void *p = nullptr;
     void *pout = nullptr;
@@ -256,6 +257,7 @@ struct SpmvArgs {
     double *dot_out = nullptr;       // final dot (written by the last CTA)
     unsigned int *dot_counter = nullptr;
     const int *done = nullptr;       // if set and *done != 0: the kernel does nothing
+    const int *gate = nullptr;       // if set and *gate == 0: the kernel does nothing
     bool use_csr = false;
 };
 void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);

@@ -503,11 +503,15 @@ private:
             a.s1 = lv.cheb_beta[k];
             a.s2 = lv.cheb_alpha[k];
             a.s3 = (k == 1) ? lv.cheb_alpha[0] : 0.0;
+            a.x2_zero = (k == 1 && from_zero) ? 1 : 0;  // x = 0 + alpha_0 p_0 + alpha_1 p_1
             a.epilogue = EPI_CHEB;
             spmv(*lv.A(), a, done);
             cur ^= 1;
         }
-        if (nu == 1) enq_axpy(*ctx, vdt_, lv.n, lv.cheb_alpha[0], p[0], x, done);
+        if (nu == 1) {
+            if (from_zero) enq_set(*ctx, vdt_, lv.n, 0.0, x, done);
+            enq_axpy(*ctx, vdt_, lv.n, lv.cheb_alpha[0], p[0], x, done);
+        }
     }
 
     // Multigrid::standard_cycle (utopia_Multigrid.hpp:252-367), V-cycle, c from zero.

@@ -1,8 +1,844 @@
-// Box-constrained QP solvers (placeholder factories until the kernels land).
+// Box-constrained QP solvers: MPRGP and multicolour projected Gauss-Seidel.
+//
+// MPRGP mirrors utopia::MPRGP::solve (non-Hardik variant, no preconditioner;
+// utopia/solvers/nonlinear/constrained/quadratic_programming/utopia_MPRGP.hpp:57-262) with
+// get_fi / get_beta / get_alpha_f (:266-348) and its power method (:351-387).  The
+// branch decisions of every iteration (proportional vs proportioning, CG vs expansion
+// step, negative curvature, convergence) are taken on the device by the last CTA of
+// the kernel that produces the deciding dots; the kernels of the branches that are
+// not taken return at once, so a batch of iterations runs without host round trips.
+//
+// ProjectedGaussSeidel mirrors utopia::ProjectedGaussSeidel::apply/step
+// (utopia_ProjectedGaussSeidel.hpp:71-112,197-318) with the lexicographic row loop
+// replaced by a multicolour sweep: rows of one colour are relaxed in parallel, colours
+// in order (then in reverse order for the symmetric sweep).  The colouring is the
+// greedy first-fit colouring in index order (red-black for the 5-point grid), computed
+// on the device by dependency rounds that reproduce the sequential result exactly.
+#include <cmath>
+
 #include "abi_util.cuh"
+#include "device_util.cuh"
 #include "solver.cuh"
 
 namespace ugpu {
-std::unique_ptr<Solver> make_mprgp(Context *) { throw Error(UGPU_ERR_UNSUPPORTED, "MPRGP not built yet"); }
-std::unique_ptr<Solver> make_pgs(Context *) { throw Error(UGPU_ERR_UNSUPPORTED, "PGS not built yet"); }
+
+namespace {
+
+#define QP_LOOP(i, n) \
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < (n); i += int64_t(gridDim.x) * blockDim.x)
+
+struct QpDev {
+    double beta_Abeta, g_betta;   // written by the proportioning SpMV (in this order)
+    double pAp, gp_dot;           // written by the CG SpMV (in this order)
+    double alpha_cg, alpha_f, beta_sc;
+    double beta_beta, fi_fi, gnorm, gnorm0;
+    long long it, iterates;
+    int done, reason, converged;
+    int gate_cg, gate_prop, gate_exp;   // branch of the current iteration
+    int step;                           // 0: CG step, 1: expansion step
+};
+
+__device__ __forceinline__ double proj(double l, double u, double x) { return (l >= x) ? l : ((u <= x) ? u : x); }
+__device__ __forceinline__ double phi(double l, double u, double x, double g) { return (l < x && x < u) ? g : 0.0; }
+__device__ __forceinline__ double chopped(double l, double u, double x, double g) {
+    return (fabs(l - x) < 1e-14) ? fmin(0.0, g) : ((fabs(u - x) < 1e-14) ? fmax(0.0, g) : 0.0);
+}
+
+__device__ __forceinline__ void qp_stop(QpDev *d, int reason, int converged) {
+    d->done = 1;
+    d->reason = reason;
+    d->converged = converged;
+    d->iterates = d->it;
+}
+
+// initial: x = P(x); (then g = A x - b by SpMV); this kernel: fi, beta, p = fi, dots
+__global__ void k_qp_project(int64_t n, const double *lb, const double *ub, double *x) {
+    QP_LOOP(i, n) x[i] = proj(lb[i], ub[i], x[i]);
+}
+
+// c: alpha_cg = (g,p)/(p,Ap) (negative curvature stops), alpha_f = min(h1, h2), step choice
+__global__ void __launch_bounds__(kBlock) k_mprgp_alpha_f(int64_t n, const double *x, const double *p,
+                                                         const double *lb, const double *ub, QpDev *dev,
+                                                         double *partials, unsigned int *counter) {
+    if (dev->done || !dev->gate_cg) return;
+    if (dev->pAp <= 0.0) {
+        // `if (pAp <= 0.0) return true;` (negative curvature)
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            qp_stop(dev, UGPU_DIVERGED_INDEFINITE, 1);
+            dev->gate_exp = 0;
+        }
+        return;
+    }
+    double m = DBL_MAX_D;
+    QP_LOOP(i, n) {
+        const double xi = x[i], pi = p[i];
+        const double h1 = (pi > 0) ? ((xi - lb[i]) / pi) : 1e15;
+        const double h2 = (pi < 0) ? ((xi - ub[i]) / pi) : 1e15;
+        m = fmin(m, fmin(h1, h2));
+    }
+    m = block_reduce_min(m);
+    if (threadIdx.x == 0) partials[blockIdx.x] = m;
+    __threadfence();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (!last) return;
+    double v = DBL_MAX_D;
+    for (int j = threadIdx.x; j < gridDim.x; j += blockDim.x) v = fmin(v, __ldcg(partials + j));
+    v = block_reduce_min(v);
+    if (threadIdx.x == 0) {
+        const double alpha_cg = dev->gp_dot / dev->pAp;
+        dev->alpha_cg = alpha_cg;
+        dev->alpha_f = v;
+        dev->step = (alpha_cg <= v) ? 0 : 1;
+        dev->gate_exp = dev->step;
+        *counter = 0u;
+    }
+}
+
+// d: the row-local part of the taken branch
+__global__ void __launch_bounds__(kBlock) k_mprgp_update(int64_t n, double *x, double *g, const double *p,
+                                                        const double *Ap, const double *beta, const double *Abeta,
+                                                        const double *lb, const double *ub, double alpha_bar,
+                                                        QpDev *dev, double *partials, unsigned int *counter) {
+    if (dev->done) return;
+    const int prop = dev->gate_prop;
+    const int step = dev->step;
+    double alpha;
+    if (prop) {
+        if (dev->beta_Abeta <= 0.0) {
+            if (blockIdx.x == 0 && threadIdx.x == 0) qp_stop(dev, UGPU_DIVERGED_INDEFINITE, 1);
+            return;
+        }
+        alpha = dev->g_betta / dev->beta_Abeta;
+    } else {
+        alpha = (step == 0) ? dev->alpha_cg : dev->alpha_f;
+    }
+    double acc = 0.0;
+    QP_LOOP(i, n) {
+        if (prop) {
+            x[i] = x[i] - alpha * beta[i];
+            g[i] = g[i] - alpha * Abeta[i];
+        } else {
+            const double xi = x[i] - alpha * p[i];
+            const double gi = g[i] - alpha * Ap[i];
+            g[i] = gi;
+            const double fi = phi(lb[i], ub[i], xi, gi);
+            if (step == 0) {
+                x[i] = xi;
+                acc = fma(fi, Ap[i], acc);
+            } else {
+                x[i] = proj(lb[i], ub[i], xi - alpha_bar * fi);
+            }
+        }
+    }
+    if (prop || step != 0) return;
+    double a[1] = {acc};
+    block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
+    double s[1];
+    if (finish_last_block(1, partials, gridDim.x, s, counter) && threadIdx.x == 0) dev->beta_sc = s[0] / dev->pAp;
+}
+
+// f: fi, beta, gp = fi + beta, next direction p, three dots, convergence and next branch
+__global__ void __launch_bounds__(kBlock) k_mprgp_final(int64_t n, const double *x, const double *g, double *p,
+                                                       double *beta, const double *lb, const double *ub, QpDev *dev,
+                                                       double *partials, unsigned int *counter, double atol,
+                                                       double rtol, long long max_it, int first) {
+    if (dev->done) return;
+    const bool cgstep = !first && dev->gate_cg && dev->step == 0;
+    const double bsc = cgstep ? dev->beta_sc : 0.0;
+    double a0 = 0, a1 = 0, a2 = 0;
+    QP_LOOP(i, n) {
+        const double l = lb[i], u = ub[i], xi = x[i], gi = g[i];
+        const double fi = phi(l, u, xi, gi);
+        const double bi = chopped(l, u, xi, gi);
+        beta[i] = bi;
+        p[i] = cgstep ? fi - bsc * p[i] : fi;
+        const double gp = fi + bi;
+        a0 = fma(bi, bi, a0);
+        a1 = fma(fi, fi, a1);
+        a2 = fma(gp, gp, a2);
+    }
+    double a[3] = {a0, a1, a2};
+    block_reduce_store<3>(a, 3, partials, gridDim.x, blockIdx.x);
+    double s[3];
+    if (finish_last_block(3, partials, gridDim.x, s, counter) && threadIdx.x == 0) {
+        dev->beta_beta = s[0];
+        dev->fi_fi = s[1];
+        if (!first) {
+            const double gnorm = sqrt(s[2]);
+            dev->gnorm = gnorm;
+            if (dev->it == 0) dev->gnorm0 = gnorm;
+            dev->it += 1;
+            // check_convergence(it, gnorm, gnorm / gnorm0, 1)
+            const double rel = gnorm / dev->gnorm0;
+            int reason = 0;
+            if (gnorm <= atol) reason = UGPU_CONVERGED_FNORM_ABS;
+            if (rel <= rtol) reason = UGPU_CONVERGED_FNORM_RELATIVE;
+            if (dev->it >= max_it) reason = UGPU_DIVERGED_MAX_IT;
+            if (reason) qp_stop(dev, reason, reason > 0);
+        }
+        const int cgpath = s[0] <= s[1];  // beta_beta <= gamma^2 fi_fi, gamma = 1
+        dev->gate_cg = cgpath;
+        dev->gate_prop = !cgpath;
+        dev->gate_exp = 0;
+        dev->step = 0;
+    }
+}
+
+__global__ void k_qp_init(QpDev *d) {
+    QpDev z{};
+    z.gnorm = -1;
+    z.gnorm0 = -1;
+    *d = z;
+}
+
+// ------------------------------------------------------------------ PGS -------------
+// multicolour projected sweep over the rows of one colour
+__global__ void __launch_bounds__(kBlock) k_pgs_colour(const int32_t *rows, int64_t nrows_c, const int32_t *rp,
+                                                      const int32_t *ci, const double *cv, const double *r,
+                                                      const double *dinv, const double *x, const double *lb,
+                                                      const double *ub, double *c, const int *done) {
+    if (*done) return;
+    QP_LOOP(q, nrows_c) {
+        const int32_t i = rows[q];
+        double s = r[i];
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+            const int32_t j = ci[k];
+            if (j != i) s -= cv[k] * c[j];
+        }
+        const double xi = x[i];
+        c[i] = fmax(fmin(dinv[i] * s, ub[i] - xi), lb[i] - xi);
+    }
+}
+
+struct PgsDev {
+    double diff, pgnorm;
+    long long it, iterates;
+    int done, reason, converged, pad;
+};
+
+// x += c; ||x_new - x_old||; convergence (stol on the step, or atol on the projected gradient)
+__global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, const double *c, PgsDev *dev,
+                                                      double *partials, unsigned int *counter, double stol,
+                                                      long long max_it, int pg_stop) {
+    if (dev->done) return;
+    double acc = 0;
+    QP_LOOP(i, n) {
+        const double xo = x[i];
+        const double xn = xo + c[i];
+        x[i] = xn;
+        const double d = xn - xo;
+        acc = fma(d, d, acc);
+    }
+    double a[1] = {acc};
+    block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
+    double s[1];
+    if (finish_last_block(1, partials, gridDim.x, s, counter) && threadIdx.x == 0) {
+        const double diff = sqrt(s[0]);
+        dev->diff = diff;
+        // check_convergence(iteration, 1, 1, diff): stol on the step, then max_it
+        int reason = 0;
+        if (!pg_stop && diff <= stol) reason = UGPU_CONVERGED_SNORM_RELATIVE;
+        if (dev->it >= max_it) reason = UGPU_DIVERGED_MAX_IT;
+        if (reason) {
+            dev->done = 1;
+            dev->reason = reason;
+            dev->converged = reason > 0;
+            dev->iterates = dev->it;
+        }
+        dev->it += 1;
+    }
+}
+
+// projected-gradient norm || P(x - g) - x || with g = -r (r = b - A x); optional stop test
+__global__ void __launch_bounds__(kBlock) k_pgs_pgnorm(int64_t n, const double *x, const double *r, const double *lb,
+                                                      const double *ub, PgsDev *dev, double *partials,
+                                                      unsigned int *counter, double atol, int pg_stop) {
+    if (dev->done) return;
+    double acc = 0;
+    QP_LOOP(i, n) {
+        const double xi = x[i];
+        const double d = proj(lb[i], ub[i], xi + r[i]) - xi;
+        acc = fma(d, d, acc);
+    }
+    double a[1] = {acc};
+    block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
+    double s[1];
+    if (finish_last_block(1, partials, gridDim.x, s, counter) && threadIdx.x == 0) {
+        const double pg = sqrt(s[0]);
+        dev->pgnorm = pg;
+        if (pg_stop && pg <= atol) {
+            dev->done = 1;
+            dev->reason = UGPU_CONVERGED_FNORM_ABS;
+            dev->converged = 1;
+            dev->iterates = dev->it;
+        }
+    }
+}
+
+// greedy colouring by dependency rounds: row i takes the smallest colour not used by its
+// lower-index neighbours once all of them are coloured (the sequential first-fit result)
+__global__ void k_colour_round(const int32_t *rp, const int32_t *ci, int64_t n, int *colour, unsigned int *left) {
+    unsigned int mine = 0;
+    QP_LOOP(i, n) {
+        if (colour[i] >= 0) continue;
+        unsigned long long used = 0;
+        bool ready = true;
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) {
+            const int32_t j = ci[k];
+            if (j >= i) continue;
+            const int cj = atomicAdd(&colour[j], 0);
+            if (cj < 0) {
+                ready = false;
+                break;
+            }
+            if (cj < 64) used |= 1ull << cj;
+        }
+        if (!ready) {
+            mine++;
+            continue;
+        }
+        int cc = 0;
+        while (cc < 63 && (used >> cc) & 1ull) ++cc;
+        atomicExch(&colour[i], cc);
+    }
+    if (mine) atomicAdd(left, mine);
+}
+
+__global__ void k_colour_flags(const int *colour, int64_t n, int c, int64_t *flag) {
+    QP_LOOP(i, n) flag[i] = (colour[i] == c) ? 1 : 0;
+}
+
+__global__ void k_colour_scatter(const int *colour, const int64_t *pos, int64_t n, int c, int32_t *rows) {
+    QP_LOOP(i, n) if (colour[i] == c) rows[pos[i]] = int32_t(i);
+}
+
+__global__ void k_recip(int64_t n, const double *d, double *out) {
+    QP_LOOP(i, n) out[i] = 1. / d[i];
+}
+
+__global__ void k_fill(int64_t n, double v, double *out) {
+    QP_LOOP(i, n) out[i] = v;
+}
+
+}  // namespace
+
+// ======================================================================================
+class QpBase : public Solver {
+public:
+    QpBase(Context *c, int k) : Solver(c, k) {}
+    void set_box(const Vec *lb, const Vec *ub) override {
+        for (const Vec *v : {lb, ub})
+            UGPU_CHECK(!v || v->dtype == UGPU_F64, UGPU_ERR_ARG, "box constraints must be FP64 vectors");
+        lb_ = lb;
+        ub_ = ub;
+    }
+
+protected:
+    const Vec *lb_ = nullptr, *ub_ = nullptr;
+    Buffer lbfill_, ubfill_;
+
+    // BoxConstraints::fill_empty_bounds: missing bounds become -+max double
+    void bounds(int64_t n, const double **lb, const double **ub) {
+        UGPU_CHECK(!lb_ || lb_->n == n, UGPU_ERR_ARG, "lower bound size mismatch");
+        UGPU_CHECK(!ub_ || ub_->n == n, UGPU_ERR_ARG, "upper bound size mismatch");
+        if (!lb_) {
+            lbfill_.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+            k_fill<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, -DBL_MAX_D, lbfill_.as<double>());
+            ctx->launches++;
+        }
+        if (!ub_) {
+            ubfill_.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+            k_fill<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, DBL_MAX_D, ubfill_.as<double>());
+            ctx->launches++;
+        }
+        *lb = lb_ ? lb_->as<double>() : lbfill_.as<double>();
+        *ub = ub_ ? ub_->as<double>() : ubfill_.as<double>();
+    }
+};
+
+class Mprgp final : public QpBase {
+public:
+    explicit Mprgp(Context *c) : QpBase(c, UGPU_SOLVER_MPRGP) {
+        prm["eig_comp_tol"] = 1e-1;        // MPRGP(): eps_eig_est_(1e-1), power_method_max_it_(10)
+        prm["power_method_max_it"] = 10;
+        prm["graph_batch"] = 8;
+        prm["use_graphs"] = 1;
+        prm["lambda_max"] = 0;             // read-only: the power-method estimate of the last apply()
+    }
+    ~Mprgp() override { drop_graph(); }
+    void set(const std::string &k, double v) override {
+        Solver::set(k, v);
+        drop_graph();
+    }
+    double lambda_max = 0;
+
+    void update(const Mat *A) override {
+        UGPU_CHECK(A && A->nrows == A->ncols && A->vdtype == UGPU_F64, UGPU_ERR_ARG, "MPRGP: square FP64 operator");
+        op = A;
+        const size_t b = sizeof(double) * std::max<int64_t>(A->nrows, 1);
+        for (Buffer *v : {&fi_, &beta_, &p_, &Ap_, &Abeta_, &g_, &h1_, &h2_}) v->alloc(b);
+        dev_.alloc(sizeof(QpDev));
+        part_.alloc(sizeof(double) * 8 * std::max(kSpmvDotGrid, kRedBlocks));
+        cnt_.alloc(sizeof(unsigned int) * 8);
+        UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
+        if (!host_) UGPU_CUDA(cudaMallocHost(&host_, sizeof(QpDev)));
+        drop_graph();
+    }
+
+    void apply(const Vec &rhs, Vec &x) override {
+        UGPU_CHECK(op, UGPU_ERR_STATE, "MPRGP: update() first");
+        const int64_t n = op->nrows;
+        UGPU_CHECK(rhs.n == n && x.n == n && rhs.dtype == UGPU_F64 && x.dtype == UGPU_F64, UGPU_ERR_ARG,
+                   "MPRGP: FP64 vectors of the operator size");
+        double t0 = now_s();
+        int64_t l0 = ctx->launches;
+        st = ugpu_solution_status{};
+        const double *lb, *ub;
+        bounds(n, &lb, &ub);
+        lambda_max = power_method();
+        prm["lambda_max"] = lambda_max;
+        alpha_bar_ = 1.95 / lambda_max;
+        k_qp_project<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, lb, ub, x.as<double>());
+        ctx->launches++;
+        {   // g = A x - b
+            SpmvArgs a;
+            a.x = x.data();
+            a.v = rhs.data();
+            a.y = g_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_SUB;
+            launch_spmv(*ctx, *op, a);
+        }
+        k_qp_init<<<1, 1, 0, ctx->stream>>>(dev_.as<QpDev>());
+        ctx->launches++;
+        // fi, beta, p = fi, (beta,beta), (fi,fi) and the first branch
+        final_kernel(x.as<double>(), lb, ub, 1);
+        const bool graphs = get("use_graphs") != 0;
+        const int batch = std::max(1, int(get("graph_batch")));
+        const int64_t limit = int64_t(get("max_it")) + 2 * batch + 2;
+        int64_t launched = 0;
+        rhs_ = rhs.as<double>();
+        while (true) {
+            if (graphs) {
+                ensure_graph(batch, x.as<double>(), lb, ub);
+                UGPU_CUDA(cudaGraphLaunch(exec_, ctx->stream));
+                ctx->launches += graph_kernels_;
+            } else {
+                for (int k = 0; k < batch; ++k) iteration(x.as<double>(), lb, ub);
+            }
+            launched += batch;
+            UGPU_CUDA(cudaMemcpyAsync(host_, dev_.ptr, sizeof(QpDev), cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (host_->done) break;
+            UGPU_CHECK(launched <= limit, UGPU_ERR_INTERNAL, "MPRGP: stop flag never set");
+        }
+        st.iterates = host_->iterates;
+        st.gradient_norm = host_->gnorm;
+        st.relative_gradient_norm = host_->gnorm0 > 0 ? host_->gnorm / host_->gnorm0 : 1;
+        st.step_norm = 1;
+        st.reason = host_->reason;
+        st.converged = host_->converged;
+        st.spmv_count = host_->it;
+        st.execution_time = now_s() - t0;
+        st.kernel_launches = ctx->launches - l0;
+    }
+
+private:
+    Buffer fi_, beta_, p_, Ap_, Abeta_, g_, h1_, h2_, dev_, part_, cnt_;
+    QpDev *host_ = nullptr;
+    double alpha_bar_ = 1;
+    const double *rhs_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int graph_batch_ = 0;
+    int64_t graph_kernels_ = 0;
+    const void *gx_ = nullptr, *glb_ = nullptr, *gub_ = nullptr, *grhs_ = nullptr;
+    double galpha_ = 0;
+
+    void drop_graph() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+        exec_ = nullptr;
+        graph_ = nullptr;
+    }
+
+    void ensure_graph(int batch, double *x, const double *lb, const double *ub) {
+        if (exec_ && graph_batch_ == batch && gx_ == x && glb_ == lb && gub_ == ub && grhs_ == rhs_ &&
+            galpha_ == alpha_bar_)
+            return;
+        drop_graph();
+        int64_t l0 = ctx->launches;
+        UGPU_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int k = 0; k < batch; ++k) iteration(x, lb, ub);
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(ctx->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        UGPU_CUDA(cudaStreamEndCapture(ctx->stream, &graph_));
+        UGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+        graph_kernels_ = ctx->launches - l0;
+        ctx->launches = l0;
+        graph_batch_ = batch;
+        gx_ = x;
+        glb_ = lb;
+        gub_ = ub;
+        grhs_ = rhs_;
+        galpha_ = alpha_bar_;
+    }
+
+    void final_kernel(double *x, const double *lb, const double *ub, int first) {
+        const int64_t n = op->nrows;
+        k_mprgp_final<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
+            n, x, g_.as<double>(), p_.as<double>(), beta_.as<double>(), lb, ub, dev_.as<QpDev>(),
+            part_.as<double>() + 6 * kSpmvDotGrid, cnt_.as<unsigned int>() + 3, get("atol"), get("rtol"),
+            (long long)get("max_it"), first);
+        ctx->launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+
+    void iteration(double *x, const double *lb, const double *ub) {
+        const int64_t n = op->nrows;
+        QpDev *dev = dev_.as<QpDev>();
+        double *part = part_.as<double>();
+        unsigned int *cnt = cnt_.as<unsigned int>();
+        {   // a: Ap = A p ; (p, Ap), (p, g)   [proportional branch]
+            SpmvArgs a;
+            a.x = p_.ptr;
+            a.y = Ap_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.dot_partials = part;
+            a.dv = g_.ptr;
+            a.dot_out = &dev->pAp;
+            a.dot_counter = cnt + 0;
+            a.done = &dev->done;
+            a.gate = &dev->gate_cg;
+            launch_spmv(*ctx, *op, a);
+        }
+        {   // b: Abeta = A beta ; (beta, Abeta), (beta, g)   [proportioning branch]
+            SpmvArgs a;
+            a.x = beta_.ptr;
+            a.y = Abeta_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.dot_partials = part + 2 * kSpmvDotGrid;
+            a.dv = g_.ptr;
+            a.dot_out = &dev->beta_Abeta;
+            a.dot_counter = cnt + 1;
+            a.done = &dev->done;
+            a.gate = &dev->gate_prop;
+            launch_spmv(*ctx, *op, a);
+        }
+        // c
+        k_mprgp_alpha_f<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, p_.as<double>(), lb, ub, dev,
+                                                                    part + 4 * kSpmvDotGrid, cnt + 2);
+        // d
+        k_mprgp_update<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
+            n, x, g_.as<double>(), p_.as<double>(), Ap_.as<double>(), beta_.as<double>(), Abeta_.as<double>(), lb,
+            ub, alpha_bar_, dev, part + 5 * kSpmvDotGrid, cnt + 4);
+        ctx->launches += 2;
+        UGPU_LAUNCH_CHECK();
+        {   // e: g = A x - b   [expansion step]
+            SpmvArgs a;
+            a.x = x;
+            a.v = rhs_;
+            a.y = g_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_SUB;
+            a.done = &dev->done;
+            a.gate = &dev->gate_exp;
+            launch_spmv(*ctx, *op, a);
+        }
+        final_kernel(x, lb, ub, 0);
+    }
+
+    // MPRGP::power_method (utopia_MPRGP.hpp:351-387)
+    double power_method() {
+        const int64_t n = op->nrows;
+        Vec f1, f2, fi;
+        for (Vec *v : {&f1, &f2, &fi}) {
+            v->ctx = ctx;
+            v->n = n;
+        }
+        f1.buf.borrow(h1_.ptr, h1_.bytes);
+        f2.buf.borrow(h2_.ptr, h2_.bytes);
+        fi.buf.borrow(fi_.ptr, fi_.bytes);
+        launch_set(*ctx, f2, 1.0);
+        auto dot = [&](const Vec &a, const Vec &b) {
+            DotArgs d{};
+            d.nd = 1;
+            d.a[0] = a.data();
+            d.b[0] = b.data();
+            double v;
+            host_dots(*ctx, n, d, &v);
+            return v;
+        };
+        const double eps = get("eig_comp_tol");
+        const int64_t max_it = int64_t(get("power_method_max_it"));
+        double lambda = 0, lambda_old;
+        int64_t it = 0;
+        bool conv = false;
+        while (!conv) {
+            launch_convert(*ctx, f2.data(), UGPU_F64, f1.data(), UGPU_F64, n);  // help_f1 = help_f2
+            SpmvArgs a;
+            a.x = f1.data();
+            a.y = f2.data();
+            a.vec_dtype = UGPU_F64;
+            launch_spmv(*ctx, *op, a);
+            double s = 1.0 / std::sqrt(dot(f2, f2));
+            launch_axpby(*ctx, n, s, f2, 0.0, f2);
+            lambda_old = lambda;
+            a.x = f2.data();
+            a.y = f1.data();
+            launch_spmv(*ctx, *op, a);
+            lambda = dot(f2, f1);
+            launch_convert(*ctx, f2.data(), UGPU_F64, fi.data(), UGPU_F64, n);
+            launch_axpby(*ctx, n, -1.0, f1, 1.0, fi);  // fi = help_f2 - help_f1
+            double gnorm = std::sqrt(dot(fi, fi));
+            conv = (gnorm < eps) || (std::fabs(lambda_old - lambda) < eps) || it > max_it;
+            it++;
+        }
+        return lambda;
+    }
+};
+
+class Pgs final : public QpBase {
+public:
+    explicit Pgs(Context *c) : QpBase(c, UGPU_SOLVER_PGS) {
+        prm["n_local_sweeps"] = 3;          // ProjectedGaussSeidel(): n_local_sweeps_(3)
+        prm["use_symmetric_sweep"] = 1;
+        prm["projected_gradient_stop"] = 0; // 1: stop on ||P(x - g) - x|| <= atol instead of the step
+        prm["graph_batch"] = 4;
+        prm["use_graphs"] = 1;
+    }
+    ~Pgs() override { drop_graph(); }
+    void set(const std::string &k, double v) override {
+        Solver::set(k, v);
+        drop_graph();
+    }
+    int ncolours = 0;
+    std::vector<int64_t> colour_count;
+    Buffer colour;  // int per row
+
+    // ProjectedGaussSeidel::update -> init: d = diag(A), d_inv = 1/d; plus the colouring
+    void update(const Mat *A) override {
+        UGPU_CHECK(A && A->nrows == A->ncols && A->vdtype == UGPU_F64, UGPU_ERR_ARG, "PGS: square FP64 operator");
+        op = A;
+        const int64_t n = A->nrows;
+        Mat &M = const_cast<Mat &>(*A);
+        ensure_diag(M);
+        dinv_.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        k_recip<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, M.diag.as<double>(), dinv_.as<double>());
+        ctx->launches++;
+        for (Buffer *v : {&r_, &c_}) v->alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        dev_.alloc(sizeof(PgsDev));
+        part_.alloc(sizeof(double) * 2 * kRedBlocks);
+        cnt_.alloc(sizeof(unsigned int) * 4);
+        UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
+        if (!host_) UGPU_CUDA(cudaMallocHost(&host_, sizeof(PgsDev)));
+        make_colouring();
+        drop_graph();
+    }
+
+    void apply(const Vec &rhs, Vec &x) override {
+        UGPU_CHECK(op, UGPU_ERR_STATE, "PGS: update() first");
+        const int64_t n = op->nrows;
+        UGPU_CHECK(rhs.n == n && x.n == n && rhs.dtype == UGPU_F64 && x.dtype == UGPU_F64, UGPU_ERR_ARG,
+                   "PGS: FP64 vectors of the operator size");
+        double t0 = now_s();
+        int64_t l0 = ctx->launches;
+        st = ugpu_solution_status{};
+        const double *lb, *ub;
+        bounds(n, &lb, &ub);
+        UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
+        const bool graphs = get("use_graphs") != 0;
+        const int batch = std::max(1, int(get("graph_batch")));
+        const int64_t limit = int64_t(get("max_it")) + 2 * batch + 2;
+        int64_t launched = 0;
+        while (true) {
+            if (graphs) {
+                ensure_graph(batch, rhs.as<double>(), x.as<double>(), lb, ub);
+                UGPU_CUDA(cudaGraphLaunch(exec_, ctx->stream));
+                ctx->launches += graph_kernels_;
+            } else {
+                for (int k = 0; k < batch; ++k) step(rhs.as<double>(), x.as<double>(), lb, ub);
+            }
+            launched += batch;
+            UGPU_CUDA(cudaMemcpyAsync(host_, dev_.ptr, sizeof(PgsDev), cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+            if (host_->done) break;
+            UGPU_CHECK(launched <= limit, UGPU_ERR_INTERNAL, "PGS: stop flag never set");
+        }
+        st.iterates = host_->iterates;
+        st.gradient_norm = host_->pgnorm;
+        st.step_norm = host_->diff;
+        st.relative_gradient_norm = 1;
+        st.reason = host_->reason;
+        st.converged = host_->converged;
+        st.spmv_count = host_->it;
+        st.execution_time = now_s() - t0;
+        st.kernel_launches = ctx->launches - l0;
+    }
+
+    std::vector<int32_t> download_colouring() const {
+        std::vector<int32_t> h(op->nrows);
+        if (op->nrows)
+            UGPU_CUDA(cudaMemcpy(h.data(), colour.ptr, sizeof(int32_t) * op->nrows, cudaMemcpyDeviceToHost));
+        return h;
+    }
+
+private:
+    Buffer dinv_, r_, c_, dev_, part_, cnt_, rows_;
+    std::vector<int64_t> colour_off_;
+    PgsDev *host_ = nullptr;
+    cudaGraph_t graph_ = nullptr;
+    cudaGraphExec_t exec_ = nullptr;
+    int graph_batch_ = 0;
+    int64_t graph_kernels_ = 0;
+    const void *k_[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    void drop_graph() {
+        if (exec_) cudaGraphExecDestroy(exec_);
+        if (graph_) cudaGraphDestroy(graph_);
+        exec_ = nullptr;
+        graph_ = nullptr;
+    }
+
+    void ensure_graph(int batch, const double *b, double *x, const double *lb, const double *ub) {
+        const void *key[4] = {b, x, lb, ub};
+        if (exec_ && graph_batch_ == batch && std::equal(key, key + 4, k_)) return;
+        drop_graph();
+        int64_t l0 = ctx->launches;
+        UGPU_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+        try {
+            for (int k = 0; k < batch; ++k) step(b, x, lb, ub);
+        } catch (...) {
+            cudaGraph_t g;
+            cudaStreamEndCapture(ctx->stream, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        UGPU_CUDA(cudaStreamEndCapture(ctx->stream, &graph_));
+        UGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
+        graph_kernels_ = ctx->launches - l0;
+        ctx->launches = l0;
+        graph_batch_ = batch;
+        std::copy(key, key + 4, k_);
+    }
+
+    void make_colouring() {
+        const int64_t n = op->nrows;
+        colour.alloc(sizeof(int) * std::max<int64_t>(n, 1));
+        UGPU_CUDA(cudaMemsetAsync(colour.ptr, 0xff, sizeof(int) * std::max<int64_t>(n, 1), ctx->stream));
+        Buffer left;
+        left.alloc(sizeof(unsigned int));
+        unsigned int h = 1;
+        int64_t rounds = 0;
+        while (h && n) {
+            UGPU_CUDA(cudaMemsetAsync(left.ptr, 0, sizeof(unsigned int), ctx->stream));
+            for (int q = 0; q < 16; ++q) {
+                k_colour_round<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(
+                    op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(), n, colour.as<int>(), left.as<unsigned int>());
+                ctx->launches++;
+            }
+            UGPU_CUDA(cudaMemcpyAsync(&h, left.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+            rounds += 16;
+            UGPU_CHECK(rounds <= 16 * (n + 16), UGPU_ERR_INTERNAL, "colouring did not finish");
+        }
+        UGPU_LAUNCH_CHECK();
+        // colour-sorted row lists (ascending rows within a colour)
+        std::vector<int32_t> hc(n);
+        if (n) UGPU_CUDA(cudaMemcpy(hc.data(), colour.ptr, sizeof(int32_t) * n, cudaMemcpyDeviceToHost));
+        ncolours = 0;
+        for (auto v : hc) ncolours = std::max(ncolours, v + 1);
+        UGPU_CHECK(ncolours <= 63, UGPU_ERR_UNSUPPORTED, "PGS: more than 63 colours");
+        rows_.alloc(sizeof(int32_t) * std::max<int64_t>(n, 1));
+        Buffer flag, pos;
+        flag.alloc(sizeof(int64_t) * std::max<int64_t>(n, 1));
+        pos.alloc(sizeof(int64_t) * (n + 1));
+        colour_off_.assign(ncolours + 1, 0);
+        colour_count.assign(ncolours, 0);
+        for (int c = 0; c < ncolours; ++c) {
+            k_colour_flags<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(colour.as<int>(), n, c,
+                                                                            flag.as<int64_t>());
+            int64_t cnt = device_exclusive_scan(*ctx, flag.as<int64_t>(), pos.as<int64_t>(), n);
+            k_colour_scatter<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(
+                colour.as<int>(), pos.as<int64_t>(), n, c, rows_.as<int32_t>() + colour_off_[c]);
+            ctx->launches += 2;
+            colour_count[c] = cnt;
+            colour_off_[c + 1] = colour_off_[c] + cnt;
+        }
+        UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+
+    // ProjectedGaussSeidel::step (utopia_ProjectedGaussSeidel.hpp:197-318), multicolour
+    void step(const double *b, double *x, const double *lb, const double *ub) {
+        const int64_t n = op->nrows;
+        PgsDev *dev = dev_.as<PgsDev>();
+        const int pg_stop = get("projected_gradient_stop") != 0;
+        {   // r = b - A x
+            SpmvArgs a;
+            a.x = x;
+            a.v = b;
+            a.y = r_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_RESIDUAL;
+            a.done = &dev->done;
+            launch_spmv(*ctx, *op, a);
+        }
+        k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, r_.as<double>(), lb, ub, dev,
+                                                                 part_.as<double>(), cnt_.as<unsigned int>() + 0,
+                                                                 get("atol"), pg_stop);
+        ctx->launches++;
+        enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
+        const int sweeps = int(get("n_local_sweeps"));
+        const bool sym = get("use_symmetric_sweep") != 0;
+        auto colour_pass = [&](int c) {
+            int64_t m = colour_count[c];
+            if (!m) return;
+            k_pgs_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
+                rows_.as<int32_t>() + colour_off_[c], m, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
+                op->vals.as<double>(), r_.as<double>(), dinv_.as<double>(), x, lb, ub, c_.as<double>(), &dev->done);
+            ctx->launches++;
+        };
+        for (int il = 0; il < sweeps; ++il) {
+            for (int c = 0; c < ncolours; ++c) colour_pass(c);
+            if (sym)
+                for (int c = ncolours - 1; c >= 0; --c) colour_pass(c);
+        }
+        k_pgs_finish<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, c_.as<double>(), dev,
+                                                                 part_.as<double>() + kRedBlocks,
+                                                                 cnt_.as<unsigned int>() + 1, get("stol"),
+                                                                 (long long)get("max_it"), pg_stop);
+        ctx->launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+};
+
+std::unique_ptr<Solver> make_mprgp(Context *c) { return std::make_unique<Mprgp>(c); }
+std::unique_ptr<Solver> make_pgs(Context *c) { return std::make_unique<Pgs>(c); }
+
+std::vector<int32_t> pgs_colouring(const Solver *s, int *ncolours) {
+    auto p = dynamic_cast<const Pgs *>(s);
+    UGPU_CHECK(p, UGPU_ERR_ARG, "not a projected Gauss-Seidel solver");
+    UGPU_CHECK(p->op, UGPU_ERR_STATE, "update() first");
+    *ncolours = p->ncolours;
+    return p->download_colouring();
+}
+
 }  // namespace ugpu
+
+using namespace ugpu;
+
+extern "C" int ugpu_pgs_colouring(const ugpu_solver *s, int32_t *colour, int *ncolours) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(s);
+    UGPU_REQUIRE(ncolours);
+    auto v = pgs_colouring(s->impl.get(), ncolours);
+    if (colour) std::copy(v.begin(), v.end(), colour);
+    UGPU_ABI_END(s ? s->impl->ctx : nullptr)
+}

@@ -225,11 +225,13 @@ struct EpiParams {
     T *vout;         // Chebyshev residual (in/out)
     T *x2;           // Chebyshev iterate (in/out)
     T s0, s1, s2, s3;
+    int x2_zero;
     const T *dv;     // second dot operand
     double *dot_partials;
     double *dot_out;
     unsigned int *dot_counter;
     const int *done;
+    const int *gate;
 };
 
 template <class T, bool FUSEP>
@@ -256,7 +258,7 @@ __device__ __forceinline__ T epilogue(const EpiParams<T> &e, int64_t row, T acc,
         T r = e.vout[row] + e.s0 * acc;
         e.vout[row] = r;
         T pn = T(-1) * r + e.s1 * xrow;
-        T xv = e.x2[row];
+        T xv = e.x2_zero ? T(0) : e.x2[row];
         if (e.s3 != T(0)) xv = xv + e.s3 * xrow;  // deferred x += alpha_0 p_0 of the first step
         e.x2[row] = xv + e.s2 * pn;
         return pn;
@@ -277,7 +279,7 @@ constexpr int kSpmvWarps = 8;
 // One warp per slice (grid-stride); R rows per lane; slot-major vector loads.
 template <class V, class T, int R, int EPI, bool FUSEP, bool DOT>
 __global__ void __launch_bounds__(kSpmvWarps * 32) k_sell_spmv(SellView m, EpiParams<T> e) {
-    if (e.done && *e.done) return;
+    if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
     constexpr int S = 32 * R;
     using LV = typename std::conditional<std::is_same<V, __nv_bfloat16>::value, float, V>::type;
     const int lane = threadIdx.x & 31;
@@ -350,7 +352,7 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_sell_spmv(SellView m, EpiPa
 template <class V, class T, int G, int EPI, bool FUSEP, bool DOT>
 __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                                                   const V *__restrict__ cv, int64_t nrows, EpiParams<T> e) {
-    if (e.done && *e.done) return;
+    if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
     constexpr int RPW = 32 / G;  // rows per warp step
     const int lane = threadIdx.x & 31;
     const int sub = lane % G;
@@ -405,11 +407,13 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.s1 = T(a.s1);
     e.s2 = T(a.s2);
     e.s3 = T(a.s3);
+    e.x2_zero = a.x2_zero;
     e.dv = static_cast<const T *>(a.dv);
     e.dot_partials = a.dot_partials;
     e.dot_out = a.dot_out;
     e.dot_counter = a.dot_counter;
     e.done = a.done;
+    e.gate = a.gate;
     return e;
 }
 
