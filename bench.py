@@ -1,0 +1,353 @@
+#!/usr/bin/env python
+"""Benchmark of the sparse-solver hot path on one GB300.
+
+Workload (the headline metric "MG-PCG time-to-1e-8 at 192^3, mixed vs FP64"):
+-div(k grad u) on a 192^3 grid (7,077,888 unknowns, 49,324,032 nonzeros), k = exp(g)
+with g a unit Gaussian field of correlation length 8 cells (seed 2), b ~ U[-1,1].
+Multigrid-preconditioned CG: 5 levels, trilinear interpolation, R = P^T, Galerkin
+RAP, Jacobi (omega 0.8) 2+2 sweeps, dense FP64 Cholesky on the 12^3 coarse level.
+Stop at ||r||_2 <= 1e-8 ||b||_2, checked in FP64.
+
+  * value: wall time of the mixed-precision solve (FP64 flexible CG outer iteration,
+    BF16-stored FP32 V-cycle), hierarchy already built, CUDA events on the library's
+    stream; lower is better.  The plain FP64 form is timed the same way (fp64_ms).
+  * roofline: the dominant kernel of the solve timed alone with CUDA events.
+  * e2e: the same solve through the public C ABI from host arrays: matrix and
+    transfer upload, hierarchy set-up, solve, download of x.
+  * cpu_baseline: the CPU oracle (a restatement of the reference's algorithms) on all
+    host cores: one complete FP64 solve of the same problem (hierarchy built untimed).
+
+--impl reference times only that CPU implementation (rank 0; other ranks exit).
+Multi-GPU: the path is not sharded here (one GPU per box); N ranks run N replicas.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_GRID = 192
+LEVELS = 5
+RTOL = 1e-8
+METRIC = "MG-PCG time-to-1e-8 at 192^3 (mixed BF16/FP32 V-cycle in FP64 FCG)"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in self.lines:
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = max(mx, float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_problem(n_grid):
+    from utopia_gb300 import problems as P
+
+    return P.lognormal_mg(n_grid, LEVELS, seed=2)
+
+
+def oracle_setup(A, Ps):
+    import oracle as O
+
+    O.build()
+    Am = O.Matrix(A)
+    t0 = time.perf_counter()
+    mg = O.Multigrid(Am, Ps, smoother="jacobi", pre=2, post=2, omega=0.8)
+    return O, Am, mg, time.perf_counter() - t0
+
+
+def oracle_solve(O, Am, mg, b):
+    """One complete FP64 MG-PCG solve on the CPU oracle (hierarchy already built)."""
+    nb = float(np.linalg.norm(b))
+    t0 = time.perf_counter()
+    x, st = O.cg_solve(Am, b, precond="mg", mg=mg, atol=RTOL * nb)
+    return time.perf_counter() - t0, st
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    A, Ps, b = make_problem(args.size)
+    O, Am, mg, setup_s = oracle_setup(A, Ps)
+    times = []
+    for k in range(args.warmup + args.steps):
+        dt, st = oracle_solve(O, Am, mg, b)
+        if k >= args.warmup:
+            times.append(dt)
+    ms = float(np.mean(times)) * 1e3
+    line = {
+        "impl": "reference", "metric": METRIC, "value": ms, "unit": "ms", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"lognormal diffusion {args.size}^3, FP64 MG-PCG (5 levels, Jacobi 0.8 2+2, "
+                               "Galerkin RAP, dense Cholesky coarse) on the CPU oracle", "grid": args.size,
+                   "timed": "solve phase per step (hierarchy built before the timed region)"},
+        "iterations": st["iterates"] + 1,
+        "cpu_baseline": {"value": ms, "unit": "ms", "cores": O.max_threads(), "kind": "port",
+                         "sample": f"complete FP64 solves to ||r|| <= 1e-8 ||b|| ({st['iterates'] + 1} "
+                                   f"iterations); hierarchy set-up {setup_s:.1f} s untimed"},
+        "e2e": {"value": ms, "unit": "ms", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--size", type=int, default=N_GRID)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="one warm-up and one timed solve only (for ncu)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+
+    import utopia_gb300 as U
+    from utopia_gb300 import _abi
+
+    if not os.path.exists(_abi.LIB_PATH):
+        from utopia_gb300 import build
+
+        build.build()
+
+    A, Ps, b = make_problem(args.size)
+    n, nnz = A.nrows, A.nnz
+    nb = float(np.linalg.norm(b))
+    ctx = U.Context(local)
+    stream = torch.cuda.ExternalStream(ctx.stream, device=local)
+
+    Am = U.SparseMatrix(ctx, A)
+    Pm = [U.SparseMatrix(ctx, p) for p in Ps]
+    bv = U.Vector(ctx, b)
+
+    def solver(precision, flexible):
+        mg = U.Multigrid(ctx, smoother="jacobi", omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+                         precision=precision)
+        mg.set_transfer_operators(Pm)
+        cg = U.ConjugateGradient(ctx, atol=RTOL * nb, flexible=flexible)
+        cg.set_preconditioner(mg)
+        t0 = time.perf_counter()
+        cg.update(Am)
+        ctx.synchronize()
+        return cg, mg, time.perf_counter() - t0
+
+    mixed, mg_mixed, setup_mixed = solver(U.BF16, 1)
+    plain, mg_plain, setup_plain = solver(U.F64, 0)
+    x = U.Vector(ctx, n=n)
+
+    def timed_solves(cg, k):
+        evs = []
+        for _ in range(k):
+            x.set(0.0)
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            cg.apply(bv, x)
+            e.record(stream)
+            evs.append((s, e))
+        torch.cuda.synchronize()
+        return [s.elapsed_time(e) for s, e in evs], cg.solution_status()
+
+    steps = 1 if args.profile else args.steps
+    warm = 1 if args.profile else args.warmup
+    timed_solves(mixed, warm)
+    timed_solves(plain, warm)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.launch_count()
+    with ClockSampler(local) as clk:
+        t_mixed, st_mixed = timed_solves(mixed, steps)
+    launches = (ctx.launch_count() - l0) // max(steps, 1)
+    x_mixed = x.numpy()
+    t_plain, st_plain = timed_solves(plain, steps)
+    x_plain = x.numpy()
+    if dist:
+        t = torch.tensor([max(t_mixed)], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_mixed = float(np.mean(t_mixed))
+    ms_plain = float(np.mean(t_plain))
+    res_mixed = float(np.linalg.norm(b - A.matvec(x_mixed)) / nb)
+    res_plain = float(np.linalg.norm(b - A.matvec(x_plain)) / nb)
+    err_mixed_vs_fp64 = float(np.linalg.norm(x_mixed - x_plain) / np.linalg.norm(x_plain))
+
+    # ---- roofline: the FP64 fine-level SpMV, timed alone (CSR byte model of the survey) ----
+    hbm, peak_kind = peaks()
+    y = U.Vector(ctx, n=n)
+    xr = U.Vector(ctx, np.random.default_rng(0).standard_normal(n))
+
+    def time_kernel(fn, reps=30):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        for _ in range(reps):
+            fn()
+        e.record(stream)
+        e.synchronize()
+        return s.elapsed_time(e) / reps * 1e-3
+
+    t_spmv = time_kernel(lambda: Am.apply(xr, y))
+    csr_bytes = nnz * (8 + 4) + 4 * (n + 1) + 2 * n * 8
+    sell = Am.sell_info()
+    moved_bytes = sell["nstored"] * 8 + 2 * n * 8 + 4 * sell["nslices"] * 3
+    spmv = {"kernel": "k_sell_spmv<double,double,2,EPI_STORE>", "us": t_spmv * 1e6,
+            "csr_model_gbs": csr_bytes / t_spmv / 1e9, "format_bytes_gbs": moved_bytes / t_spmv / 1e9,
+            "csr_model_bytes": csr_bytes, "format_bytes": moved_bytes}
+    Am.set_format(U.FORMAT_CSR)
+    t_csr = time_kernel(lambda: Am.apply(xr, y))
+    Am.set_format(U.FORMAT_SELL)
+    spmv["csr_kernel_us"] = t_csr * 1e6
+    spmv["csr_kernel_gbs"] = csr_bytes / t_csr / 1e9
+    roofline = {"bound": "hbm", "achieved": csr_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
+                "frac": csr_bytes / t_spmv / 1e9 / hbm, "traffic": None,
+                "kernel": spmv["kernel"], "peak_kind": f"{peak_kind} hbm_gbs",
+                "bytes_model": "nnz*(8+4) + 4(n+1) + 2n*8 per launch (CSR model); the diagonal-keyed "
+                               "sliced ELL reads no column indices, format_bytes_gbs is the traffic it moves"}
+
+    # ---- e2e through the public C ABI from host arrays ----
+    def e2e_once():
+        t0 = time.perf_counter()
+        A_d = U.SparseMatrix(ctx, A)
+        P_d = [U.SparseMatrix(ctx, p) for p in Ps]
+        b_d = U.Vector(ctx, b)
+        mg = U.Multigrid(ctx, smoother="jacobi", omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+                         precision=U.BF16)
+        mg.set_transfer_operators(P_d)
+        cg = U.ConjugateGradient(ctx, atol=RTOL * nb, flexible=1)
+        cg.set_preconditioner(mg)
+        x_d = U.Vector(ctx, n=n)
+        cg.solve(A_d, b_d, x_d)
+        out = x_d.numpy()
+        dt = time.perf_counter() - t0
+        return dt, out
+
+    e2e_runs = [e2e_once()[0] for _ in range(1 if args.profile else 2)]
+    h2d = (A.rowptr.nbytes + A.colidx.nbytes + A.values.nbytes + b.nbytes
+           + sum(p.rowptr.nbytes + p.colidx.nbytes + p.values.nbytes for p in Ps))
+    e2e = {"value": min(e2e_runs) * 1e3, "unit": "ms", "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(n * 8),
+           "includes": "CSR + transfer upload, Galerkin hierarchy + coarse Cholesky set-up, solve, download"}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu and not args.profile:
+        O, Aor, mgor, setup_s = oracle_setup(A, Ps)
+        dt, st = oracle_solve(O, Aor, mgor, b)
+        cpu = {"value": dt * 1e3, "unit": "ms", "cores": O.max_threads(), "kind": "port",
+               "sample": f"one complete FP64 MG-PCG solve of the same {args.size}^3 problem on the oracle "
+                         f"({st['iterates'] + 1} iterations); hierarchy set-up {setup_s:.1f} s untimed"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": ms_mixed, "unit": "ms", "n_gpus": world, "steps": steps,
+            "warmup": warm, "ms_per_step": ms_mixed, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32/bf16", "data": "synthetic",
+            "config": {"workload": f"lognormal diffusion -div(k grad u), {args.size}^3 (n={n}, nnz={nnz}), "
+                                   "MG-PCG 5 levels Jacobi(0.8) 2+2, Galerkin RAP, dense Cholesky 12^3",
+                       "grid": args.size, "tolerance": f"||r|| <= {RTOL} ||b|| (FP64)",
+                       "timed": "solve phase per step (hierarchy built before the timed region)",
+                       "l2": "inputs larger than L2 (FP64 operator 395 MB), no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "mixed": {"ms": ms_mixed, "iterations": st_mixed["iterates"] + 1, "rel_residual_fp64": res_mixed,
+                      "rel_err_vs_fp64": err_mixed_vs_fp64, "setup_ms": setup_mixed * 1e3,
+                      "precision": "BF16-stored level matrices, FP32 V-cycle, FP64 FCG"},
+            "fp64": {"ms": ms_plain, "iterations": st_plain["iterates"] + 1, "rel_residual_fp64": res_plain,
+                     "setup_ms": setup_plain * 1e3},
+            "speedup_mixed_vs_fp64": ms_plain / ms_mixed,
+            "spmv": spmv,
+            "roofline": roofline,
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -47,7 +47,7 @@ def test_cg_graph_and_eager_are_bitwise_equal(ctx):
     A, b = P.poisson2d_cg(64, 0)
     outs = []
     for graphs in (1, 0, 1):
-        s = cg(ctx, U.InvDiagPreconditioner(ctx), atol=1e-9, use_graphs=graphs, graph_batch=6)
+        s = cg(ctx, U.InvDiagPreconditioner(ctx), atol=1e-9, use_graphs=graphs)
         x = U.Vector(ctx, n=A.nrows)
         s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
         outs.append((x.numpy(), s.solution_status()["iterates"]))

@@ -7,16 +7,20 @@
 //
 // The reference evaluates alpha, beta and the stopping test on the host after every
 // dot.  Here the dots finish in the last CTA of the kernel that produces them, the
-// scalars live in device memory, and a device flag stops every later kernel of the
-// iteration.  The host launches a CUDA graph of `graph_batch` iterations and reads the
-// flag once per batch, so the iteration count and the stopping iterate are exactly
-// those of the per-iteration loop.
+// scalars live in device memory, and a device flag stops every later kernel.  The
+// whole solve is one CUDA graph launch: a conditional WHILE node re-runs the captured
+// iteration until the flag is set (use_graphs = 0 runs the same kernels eagerly with a
+// host check after every iteration), so the iteration count and the stopping iterate
+// are exactly those of the per-iteration loop.
 //
-// Per iteration (Jacobi preconditioner): 2 kernels
-//   K1  p = z + beta p ; Ap = A p ; (p,Ap)                       [SpMV, fused]
+// Per iteration (Jacobi preconditioner): 3 kernels
+//   K0  p = z + beta p
+//   K1  Ap = A p ; (p,Ap)                                          [SpMV + last-CTA dot]
 //   K2  alpha ; x += alpha p ; r -= alpha Ap ; ||r|| ; z = D^+ r ; (z,r) ; beta ; stop test
-// With a multigrid preconditioner: K1, K2 (without z), the V-cycle, and
+// With a multigrid preconditioner: K0, K1, K2 (without z), the V-cycle, and
 //   K3  (z,r) [and (z,Ap)] ; beta ; max_it test
+// (K0 is not folded into the SpMV: gathering z and p per nonzero doubles the FP64 FMAs of
+// the product, and FP64 FMA throughput, not HBM, then bounds it on GB300.)
 #include <cmath>
 
 #include "abi_util.cuh"
@@ -129,9 +133,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
 }
 
 // K3: (z, r) [and (z, Ap)] of the preconditioned residual; z may arrive in FP32
-// (mixed form) and is then widened into z64 for the next direction update.
+// (mixed form).
 template <class ZT>
-__global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__restrict__ zin, double *__restrict__ z64,
+__global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__restrict__ zin,
                                                      const double *__restrict__ r, const double *__restrict__ q,
                                                      CgDev *dev, double *partials, unsigned int *counter,
                                                      long long max_it, int flexible) {
@@ -139,7 +143,6 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
     double a0 = 0.0, a1 = 0.0;
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
         double zi = double(zin[i]);
-        if constexpr (!std::is_same<ZT, double>::value) z64[i] = zi;
         a0 = fma(zi, r[i], a0);
         if (flexible) a1 = fma(zi, q[i], a1);
     }
@@ -157,6 +160,16 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
         if (dev->it >= max_it) cg_stop(dev, UGPU_DIVERGED_MAX_IT, 0);
         else dev->it += 1;
     }
+}
+
+// K0: p = z + beta p (z in FP64 or, for the mixed form, FP32)
+template <class ZT>
+__global__ void __launch_bounds__(kBlock) k_cg_pupdate(int64_t n, const ZT *__restrict__ z, double *__restrict__ p,
+                                                       const CgDev *dev) {
+    if (dev->done) return;
+    const double beta = dev->beta;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        p[i] = double(z[i]) + beta * p[i];
 }
 
 __global__ void k_cg_init(CgDev *dev, double rz, double rnorm, long long it0) {
@@ -211,20 +224,17 @@ public:
     explicit ConjugateGradient(Context *c) : Solver(c, UGPU_SOLVER_CG) {
         prm["reset_initial_guess"] = 0;
         prm["flexible"] = 0;
-        prm["graph_batch"] = 8;
-        prm["use_graphs"] = 1;
-        prm["format"] = -1;  // -1: the matrix's own SpMV layout
+        prm["use_graphs"] = 1;  // 1: the solve is one graph launch (conditional WHILE node)
     }
-    ~ConjugateGradient() override { drop_graph(); }
 
     void set_preconditioner(Solver *p) override {
         pc_ = p;
-        drop_graph();
+        loop_.reset();
     }
 
     void set(const std::string &k, double v) override {
         Solver::set(k, v);
-        drop_graph();
+        loop_.reset();
     }
 
     // PreconditionedSolver::update propagates the operator to the preconditioner
@@ -237,8 +247,7 @@ public:
         const size_t b = sizeof(double) * std::max<int64_t>(n, 1);
         r_.alloc(b);
         z_.alloc(b);
-        p_[0].alloc(b);
-        p_[1].alloc(b);
+        p_.alloc(b);
         Ap_.alloc(b);
         r32_.release();
         z32_.release();
@@ -251,7 +260,11 @@ public:
         cnt_.alloc(sizeof(unsigned int) * 8);
         UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
         if (!host_dev_) UGPU_CUDA(cudaMallocHost(&host_dev_, sizeof(CgDev)));
-        drop_graph();
+        loop_.reset();
+    }
+
+    ~ConjugateGradient() override {
+        if (host_dev_) cudaFreeHost(host_dev_);
     }
 
     void apply(const Vec &b, Vec &x) override {
@@ -263,8 +276,11 @@ public:
         int64_t l0 = ctx->launches;
         st = ugpu_solution_status{};
         if (get("reset_initial_guess") != 0) enq_set(*ctx, UGPU_F64, n, 0.0, x.data(), nullptr);
-        mode_ = !pc_ ? CG_PLAIN : (dynamic_cast<InvDiag *>(pc_) ? CG_JACOBI : CG_GENERIC);
-        flexible_ = get("flexible") != 0 && mode_ != CG_PLAIN;
+        const int mode = !pc_ ? CG_PLAIN : (dynamic_cast<InvDiag *>(pc_) ? CG_JACOBI : CG_GENERIC);
+        const bool flexible = get("flexible") != 0 && mode != CG_PLAIN;
+        if (mode != mode_ || flexible != flexible_) loop_.reset();
+        mode_ = mode;
+        flexible_ = flexible;
         // r = b - A x
         {
             SpmvArgs a;
@@ -275,132 +291,94 @@ public:
             a.epilogue = EPI_RESIDUAL;
             launch_spmv(*ctx, *op, a);
         }
-        // z = M r (z = r for the unpreconditioned form); rz = (r, z)
-        double rz = 0.0, rr = 0.0;
-        if (mode_ == CG_PLAIN) {
-            enq_copy(*ctx, UGPU_F64, n, r_.ptr, z_.ptr, nullptr);
-        } else {
-            precondition(nullptr);
+        // z = M r (the unpreconditioned form uses r itself); rz = (r, z)
+        if (mode_ != CG_PLAIN) {
+            if (pc_->pc_dtype() == UGPU_F32) {
+                enq_convert(*ctx, UGPU_F64, r_.ptr, UGPU_F32, r32_.ptr, n, nullptr);
+                pc_->pc_enqueue(r32_.ptr, z32_.ptr, nullptr);
+            } else {
+                pc_->pc_enqueue(r_.ptr, z_.ptr, nullptr);
+            }
         }
+        double rz, rr;
         {
             DotArgs d{};
             d.nd = 2;
             d.a[0] = r_.ptr;
-            d.b[0] = z_.ptr;
+            d.b[0] = (mode_ == CG_PLAIN) ? r_.ptr : (z32_.ptr ? z32_.ptr : z_.ptr);
             d.a[1] = r_.ptr;
             d.b[1] = r_.ptr;
-            d.dtype_a[0] = d.dtype_b[0] = d.dtype_a[1] = d.dtype_b[1] = UGPU_F64;
+            d.dtype_a[0] = d.dtype_a[1] = d.dtype_b[1] = UGPU_F64;
+            d.dtype_b[0] = (mode_ != CG_PLAIN && z32_.ptr) ? UGPU_F32 : UGPU_F64;
             double out[2];
             host_dots(*ctx, n, d, out);
             rz = out[0];
             rr = out[1];
         }
-        // unpreconditioned form starts with r_norm = norm2(r); the preconditioned one with 9e9
+        // the unpreconditioned form starts with r_norm = norm2(r); the preconditioned one with 9e9
         const double rnorm0 = (mode_ == CG_PLAIN) ? std::sqrt(rr) : 9e9;
-        UGPU_CUDA(cudaMemsetAsync(p_[0].ptr, 0, p_[0].bytes, ctx->stream));
-        UGPU_CUDA(cudaMemsetAsync(p_[1].ptr, 0, p_[1].bytes, ctx->stream));
+        UGPU_CUDA(cudaMemsetAsync(p_.ptr, 0, p_.bytes, ctx->stream));  // p = z + 0 * 0 = z first
         // the unpreconditioned loop starts at it = 1 (utopia_ConjugateGradient_impl.hpp:128)
         k_cg_init<<<1, 1, 0, ctx->stream>>>(dev_.as<CgDev>(), rz, rnorm0, mode_ == CG_PLAIN ? 1 : 0);
         ctx->launches++;
         if (mode_ == CG_PLAIN && rr == 0.0) {
             // `rho = dot(r, r); if (rho == 0.) { converged = true; break; }`
-            finish(x, t0, l0, /*done_now=*/true, rnorm0);
+            finish(t0, l0, /*done_now=*/true, rnorm0);
             return;
         }
         const int64_t max_it = int64_t(get("max_it"));
-        const bool graphs = get("use_graphs") != 0;
-        int batch = std::max(2, int(get("graph_batch")));
-        batch += batch & 1;  // even: the direction buffers alternate per iteration
-        int64_t launched = 0;
-        const int64_t limit = max_it + 2 * batch + 2;
-        while (true) {
-            if (graphs) {
-                ensure_graph(batch, x.data());
-                UGPU_CUDA(cudaGraphLaunch(exec_, ctx->stream));
-                ctx->launches += graph_kernels_;
-            } else {
-                for (int k = 0; k < batch; ++k) iteration(k & 1, x.data());
+        if (get("use_graphs") != 0) {
+            if (!loop_.built() || graph_x_ != x.data()) {
+                loop_.build(*ctx, [&] { iteration(x.data()); }, &dev_.as<CgDev>()->done,
+                            int(std::min<int64_t>(max_it + 8, 1 << 30)));
+                graph_x_ = x.data();
             }
-            launched += batch;
+            loop_.run(*ctx);
             UGPU_CUDA(cudaMemcpyAsync(host_dev_, dev_.ptr, sizeof(CgDev), cudaMemcpyDeviceToHost, ctx->stream));
             UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
-            if (host_dev_->done) break;
-            UGPU_CHECK(launched <= limit, UGPU_ERR_INTERNAL, "CG: stop flag never set");
+        } else {
+            const int64_t limit = max_it + 8;
+            for (int64_t k = 0;; ++k) {
+                iteration(x.data());
+                UGPU_CUDA(cudaMemcpyAsync(host_dev_, dev_.ptr, sizeof(CgDev), cudaMemcpyDeviceToHost, ctx->stream));
+                UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+                if (host_dev_->done) break;
+                UGPU_CHECK(k <= limit, UGPU_ERR_INTERNAL, "CG: stop flag never set");
+            }
         }
-        finish(x, t0, l0, false, 0);
+        UGPU_CHECK(host_dev_->done, UGPU_ERR_INTERNAL, "CG: loop ended without the stop flag");
+        finish(t0, l0, false, 0);
     }
 
 private:
     Solver *pc_ = nullptr;
-    int mode_ = CG_PLAIN;
+    int mode_ = -1;
     bool flexible_ = false;
-    Buffer r_, z_, p_[2], Ap_, r32_, z32_, dev_, part_, cnt_;
+    Buffer r_, z_, p_, Ap_, r32_, z32_, dev_, part_, cnt_;
     CgDev *host_dev_ = nullptr;
-    cudaGraph_t graph_ = nullptr;
-    cudaGraphExec_t exec_ = nullptr;
-    int graph_batch_ = 0;
-    int64_t graph_kernels_ = 0;
+    DeviceLoop loop_;
     const void *graph_x_ = nullptr;
 
-    void drop_graph() {
-        if (exec_) cudaGraphExecDestroy(exec_);
-        if (graph_) cudaGraphDestroy(graph_);
-        exec_ = nullptr;
-        graph_ = nullptr;
-        graph_batch_ = 0;
-    }
-
-    void ensure_graph(int batch, void *x) {
-        if (exec_ && graph_batch_ == batch && graph_x_ == x) return;
-        drop_graph();
-        int64_t l0 = ctx->launches;
-        UGPU_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            for (int k = 0; k < batch; ++k) iteration(k & 1, x);
-        } catch (...) {
-            cudaGraph_t g;
-            cudaStreamEndCapture(ctx->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            throw;
-        }
-        UGPU_CUDA(cudaStreamEndCapture(ctx->stream, &graph_));
-        UGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
-        graph_kernels_ = ctx->launches - l0;
-        ctx->launches = l0;
-        graph_batch_ = batch;
-        graph_x_ = x;
-    }
-
-    void precondition(const int *done) {
-        const int64_t n = op->nrows;
-        if (pc_->pc_dtype() == UGPU_F32) {
-            pc_->pc_enqueue(r32_.ptr ? (done ? r32_.ptr : to32(n)) : nullptr, z32_.ptr, done);
-            if (!done) enq_convert(*ctx, UGPU_F32, z32_.ptr, UGPU_F64, z_.ptr, n, nullptr);
-        } else {
-            pc_->pc_enqueue(r_.ptr, z_.ptr, done);
-        }
-    }
-
-    void *to32(int64_t n) {
-        enq_convert(*ctx, UGPU_F64, r_.ptr, UGPU_F32, r32_.ptr, n, nullptr);
-        return r32_.ptr;
-    }
-
-    // one iteration; `par` selects which direction buffer holds the previous p
-    void iteration(int par, void *x) {
+    // one iteration of ConjugateGradient::preconditioned_solve (or unpreconditioned_solve)
+    void iteration(void *x) {
         const int64_t n = op->nrows;
         CgDev *dev = dev_.as<CgDev>();
-        const int *done = &dev->done;
-        double *pin = p_[par].as<double>(), *pout = p_[par ^ 1].as<double>();
         double *part = part_.as<double>();
         unsigned int *cnt = cnt_.as<unsigned int>();
-        // K1: p = z + beta p ; Ap = A p ; (p, Ap) [, (p, r)]
+        const int g = reduce_grid(n);
+        const bool f32 = mode_ == CG_GENERIC && pc_->pc_dtype() == UGPU_F32;
+        // K0: p = z + beta p   (plain CG: p = r + beta p)
+        if (f32)
+            k_cg_pupdate<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), p_.as<double>(), dev);
+        else
+            k_cg_pupdate<double><<<g, kBlock, 0, ctx->stream>>>(n, (mode_ == CG_PLAIN) ? r_.as<double>()
+                                                                                       : z_.as<double>(),
+                                                                p_.as<double>(), dev);
+        ctx->launches++;
+        // K1: Ap = A p ; (p, Ap) [, (p, r)]
         {
             SpmvArgs a;
-            a.x = (mode_ == CG_PLAIN) ? r_.ptr : z_.ptr;  // plain CG: p = r + beta p
-            a.p = pin;
-            a.pout = pout;
-            a.beta_ptr = &dev->beta;
+            a.x = p_.ptr;
             a.y = Ap_.ptr;
             a.vec_dtype = UGPU_F64;
             a.epilogue = EPI_STORE;
@@ -408,48 +386,43 @@ private:
             a.dot_out = &dev->pAp;
             a.dot_counter = cnt + 0;
             if (flexible_) a.dv = r_.ptr;
-            a.done = done;
+            a.done = &dev->done;
             launch_spmv(*ctx, *op, a);
         }
         // K2
         {
-            const bool r32 = mode_ == CG_GENERIC && pc_->pc_dtype() == UGPU_F32;
             const double atol = get("atol");
             const long long max_it = (long long)get("max_it");
-            const int g = reduce_grid(n);
             const double *dinv = (mode_ == CG_JACOBI) ? static_cast<InvDiag *>(pc_)->d.as<double>() : nullptr;
 #define UGPU_CG_UPD(M, R)                                                                                          \
-    k_cg_update<M, R><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<double *>(x), pout, r_.as<double>(),             \
+    k_cg_update<M, R><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<double *>(x), p_.as<double>(), r_.as<double>(), \
                                                      Ap_.as<double>(), dinv, z_.as<double>(), r32_.as<float>(), dev,  \
                                                      part + 2 * kSpmvDotGrid, cnt + 1, atol, max_it, int(flexible_))
             if (mode_ == CG_PLAIN) UGPU_CG_UPD(CG_PLAIN, false);
             else if (mode_ == CG_JACOBI) UGPU_CG_UPD(CG_JACOBI, false);
-            else if (r32) UGPU_CG_UPD(CG_GENERIC, true);
+            else if (f32) UGPU_CG_UPD(CG_GENERIC, true);
             else UGPU_CG_UPD(CG_GENERIC, false);
 #undef UGPU_CG_UPD
             ctx->launches++;
             UGPU_LAUNCH_CHECK();
         }
-        if (mode_ == CG_PLAIN || mode_ == CG_JACOBI) return;
+        if (mode_ != CG_GENERIC) return;
         // z = M r, then K3
-        const bool f32 = pc_->pc_dtype() == UGPU_F32;
-        pc_->pc_enqueue(f32 ? r32_.ptr : r_.ptr, f32 ? z32_.ptr : z_.ptr, done);
-        const int g = reduce_grid(n);
+        pc_->pc_enqueue(f32 ? r32_.ptr : r_.ptr, f32 ? z32_.ptr : z_.ptr, &dev->done);
         const long long max_it = (long long)get("max_it");
         if (f32)
-            k_cg_zdots<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), z_.as<double>(), r_.as<double>(),
-                                                             Ap_.as<double>(), dev, part + 4 * kSpmvDotGrid, cnt + 2,
-                                                             max_it, int(flexible_));
+            k_cg_zdots<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), r_.as<double>(), Ap_.as<double>(),
+                                                             dev, part + 4 * kSpmvDotGrid, cnt + 2, max_it,
+                                                             int(flexible_));
         else
-            k_cg_zdots<double><<<g, kBlock, 0, ctx->stream>>>(n, z_.as<double>(), nullptr, r_.as<double>(),
-                                                              Ap_.as<double>(), dev, part + 4 * kSpmvDotGrid, cnt + 2,
-                                                              max_it, int(flexible_));
+            k_cg_zdots<double><<<g, kBlock, 0, ctx->stream>>>(n, z_.as<double>(), r_.as<double>(), Ap_.as<double>(),
+                                                              dev, part + 4 * kSpmvDotGrid, cnt + 2, max_it,
+                                                              int(flexible_));
         ctx->launches++;
         UGPU_LAUNCH_CHECK();
     }
 
-    void finish(Vec &x, double t0, int64_t l0, bool done_now, double rnorm0) {
-        (void)x;
+    void finish(double t0, int64_t l0, bool done_now, double rnorm0) {
         if (done_now) {
             st.iterates = 0;
             st.gradient_norm = rnorm0;

@@ -339,6 +339,43 @@ protected:
     const Vec *lb_ = nullptr, *ub_ = nullptr;
     Buffer lbfill_, ubfill_;
 
+    struct LoopKey {
+        const void *p[4] = {nullptr, nullptr, nullptr, nullptr};
+        double s = 0;
+    };
+
+    // run the solve as one device loop (rebuilt when the captured pointers change), or
+    // eagerly with a host check per iteration; dev/host: the solver's device state
+    template <class Body>
+    void run_loop(DeviceLoop &loop, LoopKey &key, std::initializer_list<const void *> ptrs, double s, Body body,
+                  const int *done, Buffer &dev, void *host, size_t bytes) {
+        const int64_t max_it = int64_t(get("max_it"));
+        if (get("use_graphs") != 0) {
+            LoopKey k;
+            int i = 0;
+            for (auto *q : ptrs) k.p[i++] = q;
+            k.s = s;
+            if (!loop.built() || !std::equal(k.p, k.p + 4, key.p) || k.s != key.s) {
+                loop.build(*ctx, body, done, int(std::min<int64_t>(max_it + 8, 1 << 30)));
+                key = k;
+            }
+            loop.run(*ctx);
+            UGPU_CUDA(cudaMemcpyAsync(host, dev.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        } else {
+            for (int64_t it = 0;; ++it) {
+                body();
+                UGPU_CUDA(cudaMemcpyAsync(host, dev.ptr, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+                UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+                if (*static_cast<const int *>(static_cast<const void *>(static_cast<const char *>(host) +
+                                                                        (reinterpret_cast<const char *>(done) -
+                                                                         static_cast<const char *>(dev.ptr)))))
+                    break;
+                UGPU_CHECK(it <= max_it + 8, UGPU_ERR_INTERNAL, "stop flag never set");
+            }
+        }
+    }
+
     // BoxConstraints::fill_empty_bounds: missing bounds become -+max double
     void bounds(int64_t n, const double **lb, const double **ub) {
         UGPU_CHECK(!lb_ || lb_->n == n, UGPU_ERR_ARG, "lower bound size mismatch");
@@ -363,14 +400,15 @@ public:
     explicit Mprgp(Context *c) : QpBase(c, UGPU_SOLVER_MPRGP) {
         prm["eig_comp_tol"] = 1e-1;        // MPRGP(): eps_eig_est_(1e-1), power_method_max_it_(10)
         prm["power_method_max_it"] = 10;
-        prm["graph_batch"] = 8;
-        prm["use_graphs"] = 1;
+        prm["use_graphs"] = 1;             // 1: the solve is one graph launch (conditional WHILE node)
         prm["lambda_max"] = 0;             // read-only: the power-method estimate of the last apply()
     }
-    ~Mprgp() override { drop_graph(); }
+    ~Mprgp() override {
+        if (host_) cudaFreeHost(host_);
+    }
     void set(const std::string &k, double v) override {
         Solver::set(k, v);
-        drop_graph();
+        loop_.reset();
     }
     double lambda_max = 0;
 
@@ -384,7 +422,7 @@ public:
         cnt_.alloc(sizeof(unsigned int) * 8);
         UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
         if (!host_) UGPU_CUDA(cudaMallocHost(&host_, sizeof(QpDev)));
-        drop_graph();
+        loop_.reset();
     }
 
     void apply(const Vec &rhs, Vec &x) override {
@@ -415,25 +453,9 @@ public:
         ctx->launches++;
         // fi, beta, p = fi, (beta,beta), (fi,fi) and the first branch
         final_kernel(x.as<double>(), lb, ub, 1);
-        const bool graphs = get("use_graphs") != 0;
-        const int batch = std::max(1, int(get("graph_batch")));
-        const int64_t limit = int64_t(get("max_it")) + 2 * batch + 2;
-        int64_t launched = 0;
         rhs_ = rhs.as<double>();
-        while (true) {
-            if (graphs) {
-                ensure_graph(batch, x.as<double>(), lb, ub);
-                UGPU_CUDA(cudaGraphLaunch(exec_, ctx->stream));
-                ctx->launches += graph_kernels_;
-            } else {
-                for (int k = 0; k < batch; ++k) iteration(x.as<double>(), lb, ub);
-            }
-            launched += batch;
-            UGPU_CUDA(cudaMemcpyAsync(host_, dev_.ptr, sizeof(QpDev), cudaMemcpyDeviceToHost, ctx->stream));
-            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
-            if (host_->done) break;
-            UGPU_CHECK(launched <= limit, UGPU_ERR_INTERNAL, "MPRGP: stop flag never set");
-        }
+        run_loop(loop_, key_, {x.data(), lb, ub, rhs_}, alpha_bar_, [&] { iteration(x.as<double>(), lb, ub); },
+                 &dev_.as<QpDev>()->done, dev_, host_, sizeof(QpDev));
         st.iterates = host_->iterates;
         st.gradient_norm = host_->gnorm;
         st.relative_gradient_norm = host_->gnorm0 > 0 ? host_->gnorm / host_->gnorm0 : 1;
@@ -450,46 +472,8 @@ private:
     QpDev *host_ = nullptr;
     double alpha_bar_ = 1;
     const double *rhs_ = nullptr;
-    cudaGraph_t graph_ = nullptr;
-    cudaGraphExec_t exec_ = nullptr;
-    int graph_batch_ = 0;
-    int64_t graph_kernels_ = 0;
-    const void *gx_ = nullptr, *glb_ = nullptr, *gub_ = nullptr, *grhs_ = nullptr;
-    double galpha_ = 0;
-
-    void drop_graph() {
-        if (exec_) cudaGraphExecDestroy(exec_);
-        if (graph_) cudaGraphDestroy(graph_);
-        exec_ = nullptr;
-        graph_ = nullptr;
-    }
-
-    void ensure_graph(int batch, double *x, const double *lb, const double *ub) {
-        if (exec_ && graph_batch_ == batch && gx_ == x && glb_ == lb && gub_ == ub && grhs_ == rhs_ &&
-            galpha_ == alpha_bar_)
-            return;
-        drop_graph();
-        int64_t l0 = ctx->launches;
-        UGPU_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            for (int k = 0; k < batch; ++k) iteration(x, lb, ub);
-        } catch (...) {
-            cudaGraph_t g;
-            cudaStreamEndCapture(ctx->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            throw;
-        }
-        UGPU_CUDA(cudaStreamEndCapture(ctx->stream, &graph_));
-        UGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
-        graph_kernels_ = ctx->launches - l0;
-        ctx->launches = l0;
-        graph_batch_ = batch;
-        gx_ = x;
-        glb_ = lb;
-        gub_ = ub;
-        grhs_ = rhs_;
-        galpha_ = alpha_bar_;
-    }
+    DeviceLoop loop_;
+    LoopKey key_;
 
     void final_kernel(double *x, const double *lb, const double *ub, int first) {
         const int64_t n = op->nrows;
@@ -611,13 +595,14 @@ public:
         prm["n_local_sweeps"] = 3;          // ProjectedGaussSeidel(): n_local_sweeps_(3)
         prm["use_symmetric_sweep"] = 1;
         prm["projected_gradient_stop"] = 0; // 1: stop on ||P(x - g) - x|| <= atol instead of the step
-        prm["graph_batch"] = 4;
-        prm["use_graphs"] = 1;
+        prm["use_graphs"] = 1;              // 1: the solve is one graph launch (conditional WHILE node)
     }
-    ~Pgs() override { drop_graph(); }
+    ~Pgs() override {
+        if (host_) cudaFreeHost(host_);
+    }
     void set(const std::string &k, double v) override {
         Solver::set(k, v);
-        drop_graph();
+        loop_.reset();
     }
     int ncolours = 0;
     std::vector<int64_t> colour_count;
@@ -640,7 +625,7 @@ public:
         UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
         if (!host_) UGPU_CUDA(cudaMallocHost(&host_, sizeof(PgsDev)));
         make_colouring();
-        drop_graph();
+        loop_.reset();
     }
 
     void apply(const Vec &rhs, Vec &x) override {
@@ -654,24 +639,9 @@ public:
         const double *lb, *ub;
         bounds(n, &lb, &ub);
         UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
-        const bool graphs = get("use_graphs") != 0;
-        const int batch = std::max(1, int(get("graph_batch")));
-        const int64_t limit = int64_t(get("max_it")) + 2 * batch + 2;
-        int64_t launched = 0;
-        while (true) {
-            if (graphs) {
-                ensure_graph(batch, rhs.as<double>(), x.as<double>(), lb, ub);
-                UGPU_CUDA(cudaGraphLaunch(exec_, ctx->stream));
-                ctx->launches += graph_kernels_;
-            } else {
-                for (int k = 0; k < batch; ++k) step(rhs.as<double>(), x.as<double>(), lb, ub);
-            }
-            launched += batch;
-            UGPU_CUDA(cudaMemcpyAsync(host_, dev_.ptr, sizeof(PgsDev), cudaMemcpyDeviceToHost, ctx->stream));
-            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
-            if (host_->done) break;
-            UGPU_CHECK(launched <= limit, UGPU_ERR_INTERNAL, "PGS: stop flag never set");
-        }
+        run_loop(loop_, key_, {x.data(), lb, ub, rhs.data()}, 0.0,
+                 [&] { step(rhs.as<double>(), x.as<double>(), lb, ub); }, &dev_.as<PgsDev>()->done, dev_, host_,
+                 sizeof(PgsDev));
         st.iterates = host_->iterates;
         st.gradient_norm = host_->pgnorm;
         st.step_norm = host_->diff;
@@ -694,40 +664,8 @@ private:
     Buffer dinv_, r_, c_, dev_, part_, cnt_, rows_;
     std::vector<int64_t> colour_off_;
     PgsDev *host_ = nullptr;
-    cudaGraph_t graph_ = nullptr;
-    cudaGraphExec_t exec_ = nullptr;
-    int graph_batch_ = 0;
-    int64_t graph_kernels_ = 0;
-    const void *k_[4] = {nullptr, nullptr, nullptr, nullptr};
-
-    void drop_graph() {
-        if (exec_) cudaGraphExecDestroy(exec_);
-        if (graph_) cudaGraphDestroy(graph_);
-        exec_ = nullptr;
-        graph_ = nullptr;
-    }
-
-    void ensure_graph(int batch, const double *b, double *x, const double *lb, const double *ub) {
-        const void *key[4] = {b, x, lb, ub};
-        if (exec_ && graph_batch_ == batch && std::equal(key, key + 4, k_)) return;
-        drop_graph();
-        int64_t l0 = ctx->launches;
-        UGPU_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        try {
-            for (int k = 0; k < batch; ++k) step(b, x, lb, ub);
-        } catch (...) {
-            cudaGraph_t g;
-            cudaStreamEndCapture(ctx->stream, &g);
-            if (g) cudaGraphDestroy(g);
-            throw;
-        }
-        UGPU_CUDA(cudaStreamEndCapture(ctx->stream, &graph_));
-        UGPU_CUDA(cudaGraphInstantiate(&exec_, graph_, 0));
-        graph_kernels_ = ctx->launches - l0;
-        ctx->launches = l0;
-        graph_batch_ = batch;
-        std::copy(key, key + 4, k_);
-    }
+    DeviceLoop loop_;
+    LoopKey key_;
 
     void make_colouring() {
         const int64_t n = op->nrows;

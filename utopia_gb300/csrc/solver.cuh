@@ -12,6 +12,7 @@
 // flag (`done`) and do nothing once the outer iteration has stopped.
 #pragma once
 #include <chrono>
+#include <functional>
 #include <map>
 #include <string>
 
@@ -86,6 +87,19 @@ void enq_axpy(Context &c, int dt, int64_t n, double alpha, const void *x, void *
 void enq_set(Context &c, int dt, int64_t n, double v, void *y, const int *done);
 void enq_convert(Context &c, int sdt, const void *src, int ddt, void *dst, int64_t n, const int *done);
 void enq_copy(Context &c, int dt, int64_t n, const void *src, void *dst, const int *done);
+
+// A whole solve as one graph launch (loop.cu): WHILE(!*done) { body }
+struct DeviceLoop {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    Buffer state;          // [0] body executions, [1] cap overrun flag
+    int64_t kernels = 0;   // kernels per body execution (instrumentation)
+    ~DeviceLoop();
+    void reset();
+    bool built() const { return exec != nullptr; }
+    void build(Context &ctx, const std::function<void()> &body, const int *done, int cap);
+    int run(Context &ctx);
+};
 
 std::unique_ptr<Solver> make_cg(Context *c);
 std::unique_ptr<Solver> make_multigrid(Context *c);

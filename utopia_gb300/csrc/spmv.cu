@@ -276,9 +276,26 @@ __device__ __forceinline__ T epilogue(const EpiParams<T> &e, int64_t row, T acc,
 
 constexpr int kSpmvWarps = 8;
 
+// tuning knobs of the sliced-ELL kernel: slot-loop unroll depth and the minimum CTAs
+// per SM promised to the register allocator (0: no promise)
+#ifndef UGPU_SELL_UNROLL
+#define UGPU_SELL_UNROLL 4
+#endif
+#ifndef UGPU_SELL_MINB
+#define UGPU_SELL_MINB 4
+#endif
+#define UGPU_XSTR(x) UGPU_STR(x)
+#define UGPU_STR(x) #x
+#define UGPU_PRAGMA_UNROLL(n) _Pragma(UGPU_XSTR(unroll n))
+#if UGPU_SELL_MINB > 0
+#define UGPU_SELL_BOUNDS __launch_bounds__(kSpmvWarps * 32, UGPU_SELL_MINB)
+#else
+#define UGPU_SELL_BOUNDS __launch_bounds__(kSpmvWarps * 32)
+#endif
+
 // One warp per slice (grid-stride); R rows per lane; slot-major vector loads.
 template <class V, class T, int R, int EPI, bool FUSEP, bool DOT>
-__global__ void __launch_bounds__(kSpmvWarps * 32) k_sell_spmv(SellView m, EpiParams<T> e) {
+__global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
     constexpr int S = 32 * R;
     using LV = typename std::conditional<std::is_same<V, __nv_bfloat16>::value, float, V>::type;
@@ -298,21 +315,29 @@ __global__ void __launch_bounds__(kSpmvWarps * 32) k_sell_spmv(SellView m, EpiPa
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = T(0);
         if (w >= 0) {
+            // the slice's offsets are read once (coalesced) and broadcast by shuffle, so the
+            // gathers of a slot depend on no load but the value stream's
             const int32_t *offs = m.offs + aux;
+            const int32_t off_lo = (lane < w) ? __ldg(offs + lane) : 0;
+            const int32_t off_hi = (lane + 32 < w) ? __ldg(offs + 32 + lane) : 0;
+            const int r0i = int(row0);  // nrows, ncols < 2^31
+            const int cmax = int(m.ncols) - 1;
+            UGPU_PRAGMA_UNROLL(UGPU_SELL_UNROLL)
             for (int k = 0; k < w; ++k) {
-                const int32_t off = __ldg(offs + k);
+                const int32_t off = __shfl_sync(0xffffffffu, k < 32 ? off_lo : off_hi, k & 31);
                 LV v[R];
                 VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    int64_t c = row0 + r + off;
-                    c = c < 0 ? 0 : (c >= m.ncols ? m.ncols - 1 : c);
+                    int c = r0i + r + off;
+                    c = c < 0 ? 0 : (c > cmax ? cmax : c);
                     acc[r] = fma(T(v[r]), xin_at<T, FUSEP>(e, beta, c), acc[r]);
                 }
             }
         } else {
             const int wd = -w;
             const int32_t *cols = m.cols + aux;
+#pragma unroll 2
             for (int k = 0; k < wd; ++k) {
                 LV v[R];
                 int32_t c[R];
