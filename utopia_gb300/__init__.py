@@ -120,6 +120,13 @@ class Vector:
         self.ctx.check(self.ctx.lib.ugpu_vec_download(self.h, _ptr(out)))
         return out
 
+    def upload_from(self, host_ptr: int):
+        """Copy n elements from host memory at host_ptr (e.g. pinned) into the vector."""
+        self.ctx.check(self.ctx.lib.ugpu_vec_upload(self.h, C.c_void_p(host_ptr)))
+
+    def download_to(self, host_ptr: int):
+        self.ctx.check(self.ctx.lib.ugpu_vec_download(self.h, C.c_void_p(host_ptr)))
+
     def upload(self, data):
         data = np.ascontiguousarray(data, dtype=_NP[self.dtype])
         assert data.size == self.n

@@ -162,6 +162,7 @@ struct Sell {
     int64_t nstored = 0;   // stored value slots (incl. padding)
     int64_t ndiag_slices = 0;
     int max_width = 0;
+    Buffer hdr;         // int4[nslices] packed {value offset lo, hi, width, aux} read by the kernels
     Buffer slice_ptr;   // int64[nslices+1] value offset of slice (elements)
     Buffer slice_w;     // int32[nslices]   width (slots); negative: explicit-column slice
     Buffer slice_aux;   // int64[nslices]   diagonal slices: index into offs; explicit: index into cols
@@ -246,6 +247,7 @@ struct SpmvArgs {
     void *x2 = nullptr;         // in/out iterate of the Chebyshev epilogues
     double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
     int x2_zero = 0;            // Chebyshev: the iterate x2 starts at zero (not read)
+    int xmode = 0;              // input vector: 0 x; 1 x + beta*p (p, pout, beta_ptr); 2 w .* v (no x)
     // fused CG direction: xin = x + beta_scale * (*beta_ptr) * p, written back to pout
     const void *p = nullptr;
     void *pout = nullptr;

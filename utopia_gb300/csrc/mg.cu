@@ -448,23 +448,36 @@ private:
         launch_spmv(*ctx, A, a);
     }
 
-    // smoothing sweeps of Jacobi / PointJacobi from the iterate in bufs[cur]; returns
-    // the buffer index holding the result.  first_from_zero: the iterate is zero.
+    // smoothing sweeps of Jacobi / PointJacobi from the iterate in bufs[cur]; returns the
+    // buffer index holding the result.  from_zero: the iterate is zero, so the first sweep
+    // is x1 = w .* rhs and is folded into the second (its product gathers w .* rhs).
     int jacobi_sweeps(Level &lv, int sm, const void *rhs, void *bufs[2], int cur, int nu, bool from_zero,
                       const int *done) {
         const Mat &Aop = (sm == 2) ? *lv.LU : *lv.A();
-        for (int s = 0; s < nu; ++s) {
-            if (from_zero && s == 0) {
-                // Jacobi: x = 0 + w .* (rhs - A*0) = w .* rhs; PointJacobi: x = w .* (rhs - LU*0)
+        const int epi = (sm == 2) ? EPI_PJACOBI : EPI_JACOBI;
+        int s = 0;
+        if (from_zero && nu >= 1) {
+            if (nu == 1) {
+                // Jacobi: x = 0 + w .* (rhs - A*0); PointJacobi: x = w .* (rhs - LU*0)
                 enq_scale_into(*ctx, vdt_, lv.n, lv.w.ptr, rhs, bufs[cur], done);
-                continue;
+                return cur;
             }
+            SpmvArgs a;
+            a.xmode = 2;  // x1 = w .* rhs on the fly; x2 = x1 + w .* (rhs - A x1)
+            a.v = rhs;
+            a.w = lv.w.ptr;
+            a.y = bufs[cur];
+            a.epilogue = epi;
+            spmv(Aop, a, done);
+            s = 2;
+        }
+        for (; s < nu; ++s) {
             SpmvArgs a;
             a.x = bufs[cur];
             a.v = rhs;
             a.w = lv.w.ptr;
             a.y = bufs[cur ^ 1];
-            a.epilogue = (sm == 2) ? EPI_PJACOBI : EPI_JACOBI;
+            a.epilogue = epi;
             spmv(Aop, a, done);
             cur ^= 1;
         }
@@ -473,7 +486,7 @@ private:
 
     int jacobi_swaps(int nu, bool from_zero) const {
         if (nu <= 0) return 0;
-        return from_zero ? nu - 1 : nu;
+        return from_zero ? std::max(nu - 2, 0) : nu;
     }
 
     // Chebyshev3level::smooth(rhs, x) with nu iterations, x updated in place.

@@ -164,7 +164,14 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp
 // ------------------------------------------------------------------------------------
 // SpMV kernels
 // ------------------------------------------------------------------------------------
+struct SliceHdr {
+    int64_t base;  // value offset of the slice (elements)
+    int w;         // width; negative: explicit-column slice
+    int aux;       // diagonal slices: index into offs; explicit slices: index into cols
+};
+
 struct SellView {
+    const int4 *hdr;
     const int64_t *sptr;
     const int32_t *width;
     const int64_t *aux;
@@ -234,10 +241,14 @@ struct EpiParams {
     const int *gate;
 };
 
-template <class T, bool FUSEP>
+// the product's input vector: x (XM 0), x + beta*p (XM 1), or w .* v formed on the fly
+// (XM 2: the first Jacobi iterate from zero, x1 = w .* rhs)
+template <class T, int XM>
 __device__ __forceinline__ T xin_at(const EpiParams<T> &e, T beta, int64_t j) {
-    if constexpr (FUSEP) {
+    if constexpr (XM == 1) {
         return __ldg(e.x + j) + beta * __ldg(e.wvec + j);
+    } else if constexpr (XM == 2) {
+        return __ldg(e.w + j) * __ldg(e.v + j);
     } else {
         return __ldg(e.x + j);
     }
@@ -294,7 +305,7 @@ constexpr int kSpmvWarps = 8;
 #endif
 
 // One warp per slice (grid-stride); R rows per lane; slot-major vector loads.
-template <class V, class T, int R, int EPI, bool FUSEP, bool DOT>
+template <class V, class T, int R, int EPI, int XM, bool DOT>
 __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
     constexpr int S = 32 * R;
@@ -304,22 +315,50 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     const V *vals = static_cast<const V *>(m.vals);
     T beta = T(0);
-    if constexpr (FUSEP) beta = T(*e.beta_ptr);
+    if constexpr (XM == 1) beta = T(*e.beta_ptr);
     double dacc = 0.0, dacc2 = 0.0;
-    for (int64_t s = warp0; s < m.nslices; s += nwarps) {
-        const int w = __ldg(m.width + s);
-        const int64_t base = __ldg(m.sptr + s);
-        const int64_t aux = __ldg(m.aux + s);
+    // Slices are interleaved over warps (neighbouring warps stream neighbouring slices, which
+    // keeps DRAM pages and the x-gathers local).  Each slice's header is one 16-byte load;
+    // headers are fetched two slices ahead and diagonal offsets one slice ahead, so a slice
+    // never waits on a chain of dependent loads.
+    const int64_t ns = m.nslices;
+    auto load_hdr = [&](int64_t s) -> SliceHdr {
+        SliceHdr h{0, 0, 0};
+        if (s < ns) {
+            const int4 q = __ldg(reinterpret_cast<const int4 *>(m.hdr) + s);
+            h.base = (int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x);
+            h.w = q.z;
+            h.aux = q.w;
+        }
+        return h;
+    };
+    auto load_offs = [&](const SliceHdr &h, int64_t s, int32_t &lo, int32_t &hi) {
+        const bool diag = s < ns && h.w >= 0;
+        lo = (diag && lane < h.w) ? __ldg(m.offs + h.aux + lane) : 0;
+        hi = (diag && lane + 32 < h.w) ? __ldg(m.offs + h.aux + 32 + lane) : 0;
+    };
+    SliceHdr h_cur = load_hdr(warp0), h_nxt = load_hdr(warp0 + nwarps);
+    int32_t o_lo, o_hi;
+    load_offs(h_cur, warp0, o_lo, o_hi);
+    for (int64_t s = warp0; s < ns; s += nwarps) {
+        int32_t n_lo, n_hi;
+        load_offs(h_nxt, s + nwarps, n_lo, n_hi);
+        const SliceHdr h_nn = load_hdr(s + 2 * nwarps);
+        const int w = h_cur.w;
+        const int64_t base = h_cur.base;
+        const int64_t aux = h_cur.aux;
+        const int32_t off_lo = o_lo, off_hi = o_hi;
+        h_cur = h_nxt;
+        h_nxt = h_nn;
+        o_lo = n_lo;
+        o_hi = n_hi;
         const int64_t row0 = s * S + int64_t(lane) * R;
         T acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = T(0);
         if (w >= 0) {
-            // the slice's offsets are read once (coalesced) and broadcast by shuffle, so the
-            // gathers of a slot depend on no load but the value stream's
-            const int32_t *offs = m.offs + aux;
-            const int32_t off_lo = (lane < w) ? __ldg(offs + lane) : 0;
-            const int32_t off_hi = (lane + 32 < w) ? __ldg(offs + 32 + lane) : 0;
+            // the slice's offsets were read once (coalesced) and are broadcast by shuffle, so
+            // the gathers of a slot depend on no load but the value stream's
             const int r0i = int(row0);  // nrows, ncols < 2^31
             const int cmax = int(m.ncols) - 1;
             UGPU_PRAGMA_UNROLL(UGPU_SELL_UNROLL)
@@ -331,7 +370,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 for (int r = 0; r < R; ++r) {
                     int c = r0i + r + off;
                     c = c < 0 ? 0 : (c > cmax ? cmax : c);
-                    acc[r] = fma(T(v[r]), xin_at<T, FUSEP>(e, beta, c), acc[r]);
+                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
                 }
             }
         } else {
@@ -344,7 +383,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
                 load_cols<R>(cols + int64_t(k) * S + lane * R, c);
 #pragma unroll
-                for (int r = 0; r < R; ++r) acc[r] = fma(T(v[r]), xin_at<T, FUSEP>(e, beta, c[r]), acc[r]);
+                for (int r = 0; r < R; ++r) acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c[r]), acc[r]);
             }
         }
 #pragma unroll
@@ -352,8 +391,8 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
             const int64_t row = row0 + r;
             if (row < m.nrows) {
                 T xr = T(0);
-                if constexpr (FUSEP || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, FUSEP>(e, beta, row);
-                if constexpr (FUSEP) e.pout[row] = xr;
+                if constexpr (XM != 0 || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, XM>(e, beta, row);
+                if constexpr (XM == 1) e.pout[row] = xr;
                 T out = epilogue<T, EPI>(e, row, acc[r], xr);
                 e.y[row] = out;
                 if constexpr (DOT) {
@@ -374,7 +413,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
 // CSR baseline: G lanes per row, lane-strided accumulation, shuffle reduction.
 // The loop is warp-uniform (each warp covers 32/G rows per step) so the shuffles
 // always see the full warp.
-template <class V, class T, int G, int EPI, bool FUSEP, bool DOT>
+template <class V, class T, int G, int EPI, int XM, bool DOT>
 __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                                                   const V *__restrict__ cv, int64_t nrows, EpiParams<T> e) {
     if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
@@ -384,7 +423,7 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
     const int64_t warp0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     T beta = T(0);
-    if constexpr (FUSEP) beta = T(*e.beta_ptr);
+    if constexpr (XM == 1) beta = T(*e.beta_ptr);
     double dacc = 0.0, dacc2 = 0.0;
     for (int64_t wb = warp0 * RPW; wb < nrows; wb += nwarps * RPW) {
         const int64_t row = wb + lane / G;
@@ -392,14 +431,14 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
         if (row < nrows) {
             const int32_t k1 = __ldg(rp + row + 1);
             for (int32_t k = __ldg(rp + row) + sub; k < k1; k += G)
-                acc = fma(cvt<T>(__ldcs(cv + k)), xin_at<T, FUSEP>(e, beta, __ldcs(ci + k)), acc);
+                acc = fma(cvt<T>(__ldcs(cv + k)), xin_at<T, XM>(e, beta, __ldcs(ci + k)), acc);
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (row < nrows && sub == 0) {
             T xr = T(0);
-            if constexpr (FUSEP || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, FUSEP>(e, beta, row);
-            if constexpr (FUSEP) e.pout[row] = xr;
+            if constexpr (XM != 0 || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, XM>(e, beta, row);
+            if constexpr (XM == 1) e.pout[row] = xr;
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
             if constexpr (DOT) {
@@ -450,17 +489,26 @@ int spmv_grid(const Context &ctx, int64_t units_per_cta_work, int64_t total) {
     return int(g);
 }
 
-template <class V, class T, int R, int EPI, bool FUSEP, bool DOT>
+template <class V, class T, int R, int EPI, int XM, bool DOT>
 void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
-    SellView m{s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(), s.offs.as<int32_t>(),
+    SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
+               s.offs.as<int32_t>(),
                s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols};
-    int g = spmv_grid(ctx, kSpmvWarps, s.nslices);
+    // one wave of resident CTAs (grid-stride over slices)
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        UGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sell_spmv<V, T, R, EPI, XM, DOT>,
+                                                                kSpmvWarps * 32, 0));
+        if (per_sm < 1) per_sm = 1;
+    }
+    int64_t want = (s.nslices + kSpmvWarps - 1) / kSpmvWarps;
+    int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * per_sm)));
     if constexpr (DOT) g = std::min(g, kSpmvDotGrid);
-    k_sell_spmv<V, T, R, EPI, FUSEP, DOT><<<g, kSpmvWarps * 32, 0, ctx.stream>>>(m, make_epi<T>(a));
+    k_sell_spmv<V, T, R, EPI, XM, DOT><<<g, kSpmvWarps * 32, 0, ctx.stream>>>(m, make_epi<T>(a));
 }
 
-template <class V, class T, int EPI, bool FUSEP, bool DOT>
+template <class V, class T, int EPI, int XM, bool DOT>
 void csr_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     double avg = A.nrows ? double(A.nnz) / double(A.nrows) : 0;
     const int32_t *rp = A.rowptr.as<int32_t>();
@@ -471,7 +519,7 @@ void csr_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
         constexpr int G = decltype(Gc)::value;
         int g = spmv_grid(ctx, 256 / G, A.nrows);
         if constexpr (DOT) g = std::min(g, kSpmvDotGrid);
-        k_csr_spmv<V, T, G, EPI, FUSEP, DOT><<<g, 256, 0, ctx.stream>>>(rp, ci, cv, A.nrows, e);
+        k_csr_spmv<V, T, G, EPI, XM, DOT><<<g, 256, 0, ctx.stream>>>(rp, ci, cv, A.nrows, e);
     };
     if (avg <= 2) go(std::integral_constant<int, 1>{});
     else if (avg <= 6) go(std::integral_constant<int, 4>{});
@@ -479,39 +527,49 @@ void csr_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     else go(std::integral_constant<int, 32>{});
 }
 
-template <class V, class T, int EPI, bool FUSEP, bool DOT>
+template <class V, class T, int EPI, int XM, bool DOT>
 void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (a.use_csr || A.format == UGPU_FORMAT_CSR || !A.sell) {
-        csr_launch<V, T, EPI, FUSEP, DOT>(ctx, A, a);
+        csr_launch<V, T, EPI, XM, DOT>(ctx, A, a);
     } else {
         constexpr int R = std::is_same<V, double>::value ? 2 : 4;
         UGPU_CHECK(A.sell->R == R, UGPU_ERR_INTERNAL, "sliced-ELL rows-per-thread mismatch");
-        sell_launch<V, T, R, EPI, FUSEP, DOT>(ctx, A, a);
+        sell_launch<V, T, R, EPI, XM, DOT>(ctx, A, a);
     }
 }
 
 template <class V, class T>
 void dispatch_epi(Context &ctx, const Mat &A, const SpmvArgs &a) {
-    const bool fusep = a.p != nullptr;
+    const int xm = a.p ? 1 : a.xmode;
     const bool dot = a.dot_partials != nullptr;
-#define UGPU_EPI_CASE(E)                                                   \
-    case E:                                                                \
-        UGPU_CHECK(!fusep && !dot, UGPU_ERR_INTERNAL, "fused forms need EPI_STORE"); \
-        dispatch_fmt<V, T, E, false, false>(ctx, A, a);                    \
+    UGPU_CHECK(xm >= 0 && xm <= 2, UGPU_ERR_INTERNAL, "unknown SpMV input mode");
+#define UGPU_EPI_CASE(E)                                                                   \
+    case E:                                                                                \
+        UGPU_CHECK(xm == 0 && !dot, UGPU_ERR_INTERNAL, "fused forms need EPI_STORE/EPI_JACOBI"); \
+        dispatch_fmt<V, T, E, 0, false>(ctx, A, a);                                        \
         break;
     switch (a.epilogue) {
         case EPI_STORE:
-            if (fusep && dot) dispatch_fmt<V, T, EPI_STORE, true, true>(ctx, A, a);
-            else if (fusep) dispatch_fmt<V, T, EPI_STORE, true, false>(ctx, A, a);
-            else if (dot) dispatch_fmt<V, T, EPI_STORE, false, true>(ctx, A, a);
-            else dispatch_fmt<V, T, EPI_STORE, false, false>(ctx, A, a);
+            UGPU_CHECK(xm != 2, UGPU_ERR_INTERNAL, "scaled input needs a Jacobi epilogue");
+            if (xm == 1 && dot) dispatch_fmt<V, T, EPI_STORE, 1, true>(ctx, A, a);
+            else if (xm == 1) dispatch_fmt<V, T, EPI_STORE, 1, false>(ctx, A, a);
+            else if (dot) dispatch_fmt<V, T, EPI_STORE, 0, true>(ctx, A, a);
+            else dispatch_fmt<V, T, EPI_STORE, 0, false>(ctx, A, a);
+            break;
+        case EPI_JACOBI:
+            UGPU_CHECK(xm != 1 && !dot, UGPU_ERR_INTERNAL, "Jacobi sweep: plain or scaled input");
+            if (xm == 2) dispatch_fmt<V, T, EPI_JACOBI, 2, false>(ctx, A, a);
+            else dispatch_fmt<V, T, EPI_JACOBI, 0, false>(ctx, A, a);
+            break;
+        case EPI_PJACOBI:
+            UGPU_CHECK(xm != 1 && !dot, UGPU_ERR_INTERNAL, "PointJacobi sweep: plain or scaled input");
+            if (xm == 2) dispatch_fmt<V, T, EPI_PJACOBI, 2, false>(ctx, A, a);
+            else dispatch_fmt<V, T, EPI_PJACOBI, 0, false>(ctx, A, a);
             break;
         UGPU_EPI_CASE(EPI_ADD)
         UGPU_EPI_CASE(EPI_RESIDUAL)
-        UGPU_EPI_CASE(EPI_JACOBI)
         UGPU_EPI_CASE(EPI_SUB)
         UGPU_EPI_CASE(EPI_SCALE)
-        UGPU_EPI_CASE(EPI_PJACOBI)
         UGPU_EPI_CASE(EPI_CHEB)
         UGPU_EPI_CASE(EPI_CHEB0)
         default: throw Error(UGPU_ERR_ARG, "unknown SpMV epilogue");
@@ -575,6 +633,13 @@ void build_sell(Mat &A) {
     s->offs.alloc(sizeof(int32_t) * std::max<int64_t>(noffs, 1));
     s->cols.alloc(sizeof(int32_t) * std::max<int64_t>(ncol, 4));
     s->vals.alloc(size_t(sval) * std::max<int64_t>(s->nstored, 8));
+    UGPU_CHECK(noffs < (1ll << 31) && ncol < (1ll << 31), UGPU_ERR_UNSUPPORTED, "sliced ELL: index space above 2^31");
+    std::vector<int4> hh(std::max<int64_t>(ns, 1));
+    for (int64_t i = 0; i < ns; ++i)
+        hh[i] = make_int4(int(uint32_t(uint64_t(sptr[i]) & 0xffffffffu)), int(uint32_t(uint64_t(sptr[i]) >> 32)),
+                          hw[i], int(aux[i]));
+    s->hdr.alloc(sizeof(int4) * std::max<int64_t>(ns, 1));
+    if (ns) UGPU_CUDA(cudaMemcpyAsync(s->hdr.ptr, hh.data(), sizeof(int4) * ns, cudaMemcpyHostToDevice, ctx.stream));
     UGPU_CUDA(cudaMemcpyAsync(s->slice_ptr.ptr, sptr.data(), sizeof(int64_t) * (ns + 1), cudaMemcpyHostToDevice,
                               ctx.stream));
     if (ns) {
