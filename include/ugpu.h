@@ -129,6 +129,19 @@ UGPU_API int ugpu_norm2(const ugpu_vec *a, double *out);
 UGPU_API int ugpu_pointwise(int op, const ugpu_vec *a, const ugpu_vec *b, ugpu_vec *out);
 /* e_pseudo_inv (utopia/utopia_core/utopia_ElementWisePseudoInverse.hpp:20-65) */
 UGPU_API int ugpu_pseudo_inverse(const ugpu_vec *in, ugpu_vec *out, double tol);
+/* Allocation-free fused dots (no counterpart in the reference).  For callers that cannot
+ * allocate device memory -- host codes whose device memory belongs to their own pool or
+ * memory space, and hot loops that cannot afford cudaFree's device-wide synchronisation.
+ * Same deterministic result as ugpu_dots: out[i] = sum_j a[i][j] * b[i][j] (FP64
+ * accumulation) for i < k, written to the DEVICE array d_out on `stream` (no context,
+ * no synchronisation).  a, b: host arrays of k device pointers; dtype_a/dtype_b: their
+ * element types.  Scratch is a fixed 38.9 KB device array inside the library (held by
+ * every GPU that loads it until exit): k is limited to 8 pairs, larger k is rejected
+ * with UGPU_ERR_ARG.  The first call on a device looks up the array's device address;
+ * make that first call before any stream capture.  All calls share the one array, so
+ * calls that overlap on the GPU (different streams, or several host threads) race. */
+UGPU_API int ugpu_dots_noalloc(int k, const void *const *a, const void *const *b, const int *dtype_a,
+                               const int *dtype_b, int64_t n, double *d_out, void *stream);
 /* multi_min (utopia/utopia_core/eval/utopia_MultiReduce.hpp:14-24), FP64 vectors */
 UGPU_API int ugpu_multi_min(const ugpu_vec *a, const ugpu_vec *b, double *out);
 

@@ -538,3 +538,94 @@ int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x) {
 }
 
 }  // extern "C"
+
+// ======================================================================================
+// Allocation-free fused dots
+//
+// Some callers of this library cannot allocate device memory: host codes that have
+// handed all device memory to their own allocator or memory space up front (a PETSc /
+// Kokkos / PyTorch memory pool that must see no cudaMalloc or cudaFree from a library),
+// and hot loops that cannot afford the device-wide synchronisation cudaFree implies.
+// ugpu_dots_noalloc computes the same deterministic fused dots as ugpu_dots without a
+// context and without allocating: its scratch (the per-CTA partials and the last-CTA
+// ticket) is a file-scope device array of fixed size, reserved in every GPU that loads
+// the library until the process exits.
+// ======================================================================================
+#include <mutex>
+
+namespace {
+
+constexpr int kNoAllocMaxPairs = kMaxDots;               // at most 8 dot pairs per call
+constexpr int kNoAllocPartials = kMaxDots * kRedBlocks;  // 4864 doubles of CTA partials
+constexpr int kNoAllocMaxDevices = 64;
+
+// [0, kNoAllocPartials): CTA partials; the next 32 doubles hold the last-CTA ticket
+// (38.9 KB in total)
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPartials + 32];
+
+std::mutex g_noalloc_mutex;
+double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
+
+// Device address of the scratch array on the current device.  The array's name is a
+// host-side stand-in in host code, so the address comes from cudaGetSymbolAddress,
+// once per device (the first call on a device performs this set-up).
+double *noalloc_scratch(int device) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[device]) {
+        double *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            throw Error(UGPU_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noalloc_ptr[device] = p;
+    }
+    return g_noalloc_ptr[device];
+}
+
+}  // namespace
+
+extern "C" int ugpu_dots_noalloc(int k, const void *const *a, const void *const *b, const int *dtype_a,
+                                 const int *dtype_b, int64_t n, double *d_out, void *stream) {
+    UGPU_ABI_BEGIN
+    UGPU_CHECK(k >= 1, UGPU_ERR_ARG, "dots_noalloc: at least one pair");
+    UGPU_CHECK(k <= kNoAllocMaxPairs, UGPU_ERR_ARG,
+               "dots_noalloc: more than 8 pairs exceed the fixed scratch (8 x 608 CTA partials); split the call");
+    UGPU_CHECK(n >= 0, UGPU_ERR_ARG, "dots_noalloc: negative length");
+    UGPU_CHECK(a && b && dtype_a && dtype_b && d_out, UGPU_ERR_ARG, "dots_noalloc: null argument");
+    DotArgs args{};
+    args.nd = k;
+    for (int i = 0; i < k; ++i) {
+        UGPU_CHECK(n == 0 || (a[i] && b[i]), UGPU_ERR_ARG, "dots_noalloc: null vector");
+        UGPU_CHECK(dtype_a[i] >= UGPU_F64 && dtype_a[i] <= UGPU_BF16 && dtype_b[i] >= UGPU_F64 &&
+                       dtype_b[i] <= UGPU_BF16,
+                   UGPU_ERR_ARG, "dots_noalloc: unknown dtype");
+        args.a[i] = a[i];
+        args.b[i] = b[i];
+        args.dtype_a[i] = dtype_a[i];
+        args.dtype_b[i] = dtype_b[i];
+    }
+    int device = 0;
+    UGPU_CUDA(cudaGetDevice(&device));
+    UGPU_CHECK(device >= 0 && device < kNoAllocMaxDevices, UGPU_ERR_UNSUPPORTED, "dots_noalloc: device index");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (n == 0) {
+        UGPU_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * k, s));
+        return UGPU_OK;
+    }
+    double *partials = noalloc_scratch(device);
+    unsigned int *ticket = reinterpret_cast<unsigned int *>(partials + kNoAllocPartials);
+    UGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));  // the ticket must start at zero
+    bool all64 = true, all32 = true;
+    for (int i = 0; i < k; ++i) {
+        all64 &= args.dtype_a[i] == UGPU_F64 && args.dtype_b[i] == UGPU_F64;
+        all32 &= args.dtype_a[i] == UGPU_F32 && args.dtype_b[i] == UGPU_F32;
+    }
+    const int g = reduce_grid(n);  // at most kRedBlocks CTAs: the partials fit the scratch
+    if (all64)
+        k_dots<0><<<g, kBlock, 0, s>>>(n, args, partials, d_out, ticket);
+    else if (all32)
+        k_dots<1><<<g, kBlock, 0, s>>>(n, args, partials, d_out, ticket);
+    else
+        k_dots<2><<<g, kBlock, 0, s>>>(n, args, partials, d_out, ticket);
+    UGPU_CUDA(cudaGetLastError());
+    UGPU_ABI_END(nullptr)
+}
