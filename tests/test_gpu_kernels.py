@@ -96,6 +96,17 @@ def expected_diagonal_slots(A, S):
     return total
 
 
+def test_spmv_unaligned_wrapped_input(ctx, oracle):
+    """Wrapped caller memory that is not 16-byte aligned is read correctly (CSR path)."""
+    A = P.lognormal_diffusion_3d(12, 1)[0]
+    x = np.random.default_rng(4).standard_normal(A.ncols)
+    big = U.Vector(ctx, np.concatenate([[7.0], x]))  # x starts 8 bytes into the allocation
+    vx = U.Vector.wrap_device(ctx, big.device_ptr + 8, A.ncols)
+    vy = U.Vector(ctx, n=A.nrows)
+    U.SparseMatrix(ctx, A).apply(vx, vy)
+    np.testing.assert_allclose(vy.numpy(), oracle.Matrix(A).matvec(x), rtol=1e-13, atol=1e-13)
+
+
 def test_stencil_operators_use_diagonal_slices(ctx):
     for A in (P.laplacian_3d(32), P.lognormal_diffusion_3d(16, 1)[0], P.laplacian_3d(96, 96, 8)):
         info = U.SparseMatrix(ctx, A).sell_info()
