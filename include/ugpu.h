@@ -241,6 +241,26 @@ UGPU_API int ugpu_solver_status(const ugpu_solver *s, ugpu_solution_status *out)
  * lexicographically (utopia_ProjectedGaussSeidel.hpp:213-254); colour may be NULL. */
 UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *ncolours);
 
+/* ---------------------------------------------------------------- differentiable solve ---- */
+/* No reference counterpart (utopia/differentiable/ is symbolic autodiff of expressions, not an
+ * adjoint solver).  A graph with per-edge log-conductances theta:
+ *   A(theta) = sum_e exp(theta_e) (e_src - e_dst)(e_src - e_dst)^T + diag(boundary).
+ * edge_of_pos[k] names the edge of CSR entry k of A's pattern (-1 on the diagonal).  The
+ * adjoint of x = A^{-1} b reuses the forward solver (A is symmetric): lambda = A^{-1} dL/dx,
+ * dL/db = lambda, dL/dtheta_e = -exp(theta_e)(lambda_src - lambda_dst)(x_src - x_dst),
+ * dL/dA_ij = -lambda_i x_j. */
+typedef struct ugpu_graph ugpu_graph;
+UGPU_API int ugpu_graph_create(ugpu_ctx *ctx, int64_t n, int64_t E, const int32_t *src, const int32_t *dst,
+                               int64_t nnz, const int32_t *edge_of_pos, const double *boundary, ugpu_graph **out);
+UGPU_API int ugpu_graph_destroy(ugpu_graph *g);
+/* write A(theta) into the values of A (FP64, the n x n pattern edge_of_pos describes); theta FP32 or FP64 */
+UGPU_API int ugpu_graph_assemble(ugpu_graph *g, const ugpu_vec *theta, ugpu_mat *A);
+/* grad (dtype of theta) = dL/dtheta from lambda and x (FP64) */
+UGPU_API int ugpu_graph_edge_grad(ugpu_graph *g, const ugpu_vec *theta, const ugpu_vec *lam, const ugpu_vec *x,
+                                  ugpu_vec *grad);
+/* gvals[k] = -lambda_i x_j for every CSR entry k = (i, j) of A (FP64, length nnz) */
+UGPU_API int ugpu_pattern_grad(const ugpu_mat *A, const ugpu_vec *lam, const ugpu_vec *x, ugpu_vec *gvals);
+
 /* ---------------------------------------------------------------- box constraints ---- */
 /* project(lb, ub, x) (utopia/solvers/nonlinear/constrained/utopia_VariableBoundSolverInterface.hpp:134-155) */
 UGPU_API int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x);

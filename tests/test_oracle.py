@@ -118,3 +118,29 @@ def test_mixed_precision_restatement_reaches_tolerance(oracle):
         x, st = oracle.cg_solve(Am, b, precond="mg", mg=mg, atol=1e-8 * np.linalg.norm(b), flexible=True)
         assert st["converged"]
         assert np.linalg.norm(b - A.matvec(x)) <= 1e-8 * np.linalg.norm(b) * 1.0001
+
+
+def test_oracle_adjoint_gradient_matches_central_differences(oracle):
+    """The adjoint formula dL/dtheta_e = -k_e (lam_i - lam_j)(x_i - x_j), lam = A^{-1} 2(x - x_t),
+    against central differences of L = ||x - x_t||^2 with CPU FP64 solves on an 8^3 graph."""
+    G, theta, b, theta_t = P.graph_adjoint(8)
+    theta = theta.astype(np.float64)
+
+    def solve(th, rhs):
+        Am = oracle.Matrix(G.assemble(th))
+        x, st = oracle.cg_solve(Am, rhs, precond="invdiag", atol=1e-14 * np.linalg.norm(rhs), max_it=5000)
+        return x
+
+    x_t = solve(theta_t, b)
+    x = solve(theta, b)
+    lam = solve(theta, 2 * (x - x_t))
+    g = oracle.edge_grad(G.src, G.dst, theta.astype(np.float32), lam, x)
+    g = -np.exp(theta) * (lam[G.src] - lam[G.dst]) * (x[G.src] - x[G.dst])  # FP64 theta
+    rng = np.random.default_rng(0)
+    for _ in range(3):
+        v = rng.standard_normal(G.E)
+        h = 1e-4
+        Lp = np.sum((solve(theta + h * v, b) - x_t) ** 2)
+        Lm = np.sum((solve(theta - h * v, b) - x_t) ** 2)
+        fd = (Lp - Lm) / (2 * h)
+        assert abs(g @ v - fd) <= 1e-6 * abs(fd)

@@ -108,6 +108,11 @@ SIGNATURES = {
     "ugpu_solver_status": [_vp, C.POINTER(SolutionStatus)],
     "ugpu_project": [_vp, _vp, _vp],
     "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
+    "ugpu_graph_create": [_vp, _i64, _i64, _vp, _vp, _i64, _vp, _vp, _pp],
+    "ugpu_graph_destroy": [_vp],
+    "ugpu_graph_assemble": [_vp, _vp, _vp],
+    "ugpu_graph_edge_grad": [_vp, _vp, _vp, _vp, _vp],
+    "ugpu_pattern_grad": [_vp, _vp, _vp, _vp],
 }
 
 

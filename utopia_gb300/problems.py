@@ -283,6 +283,14 @@ class EdgeGraph:
         assert (out >= 0).all()
         return out.astype(np.int32)
 
+    def edge_of_pos(self):
+        """Edge id of every CSR entry of the Laplacian pattern (-1 on the diagonal)."""
+        eop = np.full(self.colidx.size, -1, dtype=np.int32)
+        e = np.arange(self.E, dtype=np.int32)
+        eop[self.pos_ij] = e
+        eop[self.pos_ji] = e
+        return eop
+
     def assemble(self, theta) -> CSR:
         """A(theta) = sum_e exp(theta_e) (e_i - e_j)(e_i - e_j)^T + unit Dirichlet faces."""
         k = np.exp(np.asarray(theta, dtype=np.float64))
