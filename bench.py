@@ -169,6 +169,32 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_spmv_only(args):
+    """The kernels of the roofline and of the V-cycle's fine sweeps, launched in a fixed order:
+    FP64 y = A x (x2), FP32 y = A x (x2), BF16 Jacobi sweep (x2), on the lognormal operator."""
+    import utopia_gb300 as U
+    from utopia_gb300 import problems as P
+
+    A, _, _ = P.lognormal_diffusion_3d(args.size, 2)
+    ctx = U.Context(0)
+    M = U.SparseMatrix(ctx, A)
+    M32, M16 = M.cast(U.F32), M.cast(U.BF16)
+    rng = np.random.default_rng(0)
+    x64 = U.Vector(ctx, rng.standard_normal(A.nrows))
+    y64 = U.Vector(ctx, n=A.nrows)
+    x32 = U.Vector(ctx, rng.standard_normal(A.nrows), dtype=U.F32)
+    b32 = U.Vector(ctx, rng.standard_normal(A.nrows), dtype=U.F32)
+    y32 = U.Vector(ctx, n=A.nrows, dtype=U.F32)
+    for _ in range(2):
+        M.apply(x64, y64)
+    for _ in range(2):
+        M32.apply(x32, y32)
+    for _ in range(2):
+        M16.jacobi_sweep(b32, x32, 0.8, y32)
+    ctx.synchronize()
+    print(json.dumps({"spmv_only": True, "n": A.nrows, "nnz": A.nnz}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -181,9 +207,15 @@ def main():
     ap.add_argument("--eager", action="store_true",
                     help="launch every kernel individually instead of one graph per solve (ncu does not "
                          "profile kernels inside conditional graph bodies)")
+    ap.add_argument("--spmv-only", action="store_true",
+                    help="profiling case: FP64 and FP32 products and a BF16 Jacobi sweep of the fine operator, "
+                         "two launches each, nothing else")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.spmv_only:
+        run_spmv_only(args)
         return
 
     import torch
@@ -301,11 +333,25 @@ def main():
     Am.set_format(U.FORMAT_SELL)
     spmv["csr_kernel_us"] = t_csr * 1e6
     spmv["csr_kernel_gbs"] = csr_bytes / t_csr / 1e9
+    # DRAM read+write bytes of one launch of this kernel, from an ncu capture of the 160^3
+    # operator (268.8 MB for 28,518,400 nonzeros) scaled by nonzeros (traffic grows with them)
+    traffic = 268.8e6 * nnz / 28518400
     roofline = {"bound": "hbm", "achieved": csr_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
-                "frac": csr_bytes / t_spmv / 1e9 / hbm, "traffic": None,
-                "kernel": spmv["kernel"], "peak_kind": f"{peak_kind} hbm_gbs",
+                "frac": csr_bytes / t_spmv / 1e9 / hbm, "traffic": traffic,
+                "kernel": spmv["kernel"], "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
                 "bytes_model": "nnz*(8+4) + 4(n+1) + 2n*8 per launch (CSR model); the diagonal-keyed "
-                               "sliced ELL reads no column indices, format_bytes_gbs is the traffic it moves"}
+                               "sliced ELL reads no column indices, format_bytes_gbs is the traffic it moves",
+                "limit": "FP64 pipe (GB300 ~1.6 DFMA/clk/SM; one DFMA per nonzero)"}
+    # the V-cycle's operator in the mixed form: BF16 values, FP32 vectors
+    A16 = Am.cast(U.BF16)
+    x16, y16 = U.Vector(ctx, np.ones(n, np.float32), dtype=U.F32), U.Vector(ctx, n=n, dtype=U.F32)
+    t16 = time_kernel(lambda: A16.apply(x16, y16))
+    s16 = A16.sell_info()
+    b16 = s16["nstored"] * 2 + 2 * n * 4
+    roofline_bf16 = {"kernel": "k_sell_spmv<bf16,float,4,EPI_STORE>", "us": t16 * 1e6,
+                     "format_bytes": b16, "achieved": b16 / t16 / 1e9, "peak": hbm, "unit": "GB/s",
+                     "frac": b16 / t16 / 1e9 / hbm, "csr_model_gbs": (nnz * 6 + 4 * (n + 1) + 2 * n * 4) / t16 / 1e9}
+    del A16
 
     # ---- e2e through the public C ABI with host buffers: per step, b from pinned host
     # memory to the device, the mixed solve, x back to pinned host memory ----
@@ -379,6 +425,7 @@ def main():
             "speedup_mixed_vs_fp64": ms_plain / ms_mixed,
             "spmv": spmv,
             "roofline": roofline,
+            "roofline_bf16_spmv": roofline_bf16,
             "e2e": e2e,
             "cold_path": {"ms": cold_ms, "h2d_bytes": int(cold_h2d),
                           "includes": "CSR + transfer upload from pageable host arrays, Galerkin hierarchy, "
