@@ -215,6 +215,12 @@ class SparseMatrix:
         self.ctx.check(self.ctx.lib.ugpu_mat_sell_info(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return {"nslices": a.value, "nstored": b.value, "ndiag_slices": c.value, "rows_per_slice": d.value}
 
+    def sell_interleaved(self) -> bool:
+        """True when the sliced-ELL rows are lane-interleaved (the staged kernel's layout)."""
+        v = C.c_int()
+        self.ctx.check(self.ctx.lib.ugpu_mat_sell_layout(self.h, C.byref(v)))
+        return bool(v.value)
+
     def update_values(self, values):
         v = np.ascontiguousarray(values, dtype=np.float64)
         assert v.size == self.nnz

@@ -23,7 +23,20 @@ Context::Context(int dev) : device(dev) {
     counters.alloc(sizeof(unsigned int) * 64);
     UGPU_CUDA(cudaMemset(counters.ptr, 0, counters.bytes));
     UGPU_CUDA(cudaMemset(scalars.ptr, 0, scalars.bytes));
+    kflags.alloc(sizeof(int) * 4);
+    UGPU_CUDA(cudaMemset(kflags.ptr, 0, kflags.bytes));
     UGPU_CUDA(cudaMallocHost(&host_scalars, sizeof(double) * 256));
+}
+
+void Context::check_kernel_flags() {
+    int h[4] = {0, 0, 0, 0};
+    UGPU_CUDA(cudaMemcpyAsync(h, kflags.ptr, sizeof(h), cudaMemcpyDeviceToHost, stream));
+    UGPU_CUDA(cudaStreamSynchronize(stream));
+    if (h[0]) {
+        UGPU_CUDA(cudaMemsetAsync(kflags.ptr, 0, kflags.bytes, stream));
+        throw Error(UGPU_ERR_CUDA, "a staged SpMV kernel timed out waiting for its shared-memory copies; "
+                                   "its output is invalid");
+    }
 }
 
 Context::~Context() {
@@ -344,7 +357,7 @@ const char *ugpu_last_error(const ugpu_ctx *ctx) {
 int ugpu_synchronize(ugpu_ctx *ctx) {
     UGPU_ABI_BEGIN
     UGPU_REQUIRE(ctx);
-    UGPU_CUDA(cudaStreamSynchronize(ctx->impl.stream));
+    ctx->impl.check_kernel_flags();
     UGPU_ABI_END(ctx ? &ctx->impl : nullptr)
 }
 
@@ -436,8 +449,8 @@ int ugpu_vec_download(const ugpu_vec *v, void *host) {
     if (v->impl.n) {
         UGPU_CUDA(cudaMemcpyAsync(host, v->impl.buf.ptr, v->impl.n * dtype_size(v->impl.dtype),
                                   cudaMemcpyDeviceToHost, c.stream));
-        UGPU_CUDA(cudaStreamSynchronize(c.stream));
     }
+    c.check_kernel_flags();
     UGPU_ABI_END(v ? v->impl.ctx : nullptr)
 }
 

@@ -109,6 +109,7 @@ struct Context {
     Buffer partials;   // kMaxDots * kRedBlocks doubles
     Buffer scalars;    // generic device scalars (results of reductions), 256 doubles
     Buffer counters;   // last-CTA tickets of the reductions
+    Buffer kflags;     // int[4] device error flags; [0]: a staged SpMV gave up waiting for its copies
     double *host_scalars = nullptr;  // pinned mirror
     int64_t launches = 0;            // kernels launched through this context (instrumentation)
     Context(int dev);
@@ -116,6 +117,8 @@ struct Context {
     double *d_partials() const { return partials.as<double>(); }
     double *d_scalars() const { return scalars.as<double>(); }
     unsigned int *d_counters() const { return counters.as<unsigned int>(); }
+    int *d_kflags() const { return kflags.as<int>(); }
+    void check_kernel_flags();  // throws (and clears) if a kernel recorded an error
 };
 
 // ------------------------------------------------------------------------------------
@@ -171,6 +174,11 @@ struct Sell {
     Buffer vals;        // value storage (dtype of the matrix)
     int64_t ncols_explicit = 0;
     int64_t noffs = 0;
+    // lane-interleaved rows: lane l owns rows l + 32 r of a slice and row 32 r + l is stored
+    // at slot position l R + r (FP32 / BF16 matrices whose slices are all diagonal, read by
+    // the shared-memory staged kernel); otherwise lane l owns rows l R + r at position l R + r
+    bool interleaved = false;
+    int xwin_max = 0;   // interleaved: most x-window floats one slice stages (staged kernel's grouping)
 };
 
 struct Mat {

@@ -159,7 +159,7 @@ int ugpu_solver_apply(ugpu_solver *s, const ugpu_vec *rhs, ugpu_vec *x) {
     UGPU_REQUIRE(rhs);
     UGPU_REQUIRE(x);
     s->impl->apply(rhs->impl, x->impl);
-    UGPU_CUDA(cudaStreamSynchronize(s->impl->ctx->stream));
+    s->impl->ctx->check_kernel_flags();
     UGPU_ABI_END(s ? s->impl->ctx : nullptr)
 }
 

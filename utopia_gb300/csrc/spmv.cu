@@ -112,12 +112,18 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_analyze(const int32_t 
     }
 }
 
+// Position of row rl of a slice inside one slot of S = 32 R entries: rl itself, or in the
+// lane-interleaved layout (lane l owns rows l + 32 r) l R + r for rl = 32 r + l.
+__host__ __device__ __forceinline__ int sell_pos(int rl, int S, bool interleaved) {
+    return interleaved ? (rl & 31) * (S >> 5) + (rl >> 5) : rl;
+}
+
 template <class V>
 __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp, const int32_t *ci, const V *cv,
                                                                 int64_t n, int64_t ncols, int S, int64_t nslices,
                                                                 const int32_t *width, const int64_t *sptr,
                                                                 const int64_t *aux, const int32_t *offs_tmp,
-                                                                int32_t *offs, int32_t *cols, V *vals) {
+                                                                int32_t *offs, int32_t *cols, V *vals, bool il) {
     __shared__ int32_t s_off[kMaxDiagSlots];
     for (int64_t s = blockIdx.x; s < nslices; s += gridDim.x) {
         int w = width[s];
@@ -138,7 +144,7 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp
                 for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
                     int32_t off = int32_t((long long)ci[k] - r);
                     while (slot < w && s_off[slot] < off) ++slot;
-                    if (slot < w && s_off[slot] == off) vals[base + int64_t(slot) * S + rl] = cv[k];
+                    if (slot < w && s_off[slot] == off) vals[base + int64_t(slot) * S + sell_pos(rl, S, il)] = cv[k];
                 }
             }
             __syncthreads();
@@ -151,10 +157,11 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp
                 int32_t start = (r < n) ? rp[r] : 0;
                 int32_t padcol = (len > 0) ? ci[start] : 0;
                 if (padcol >= ncols) padcol = 0;
+                const int p = sell_pos(rl, S, il);
                 for (int k = 0; k < wd; ++k) {
                     bool real = k < len;
-                    vals[base + int64_t(k) * S + rl] = real ? cv[start + k] : cvt<V>(0.0);
-                    cols[cb + int64_t(k) * S + rl] = real ? ci[start + k] : padcol;
+                    vals[base + int64_t(k) * S + p] = real ? cv[start + k] : cvt<V>(0.0);
+                    cols[cb + int64_t(k) * S + p] = real ? ci[start + k] : padcol;
                 }
             }
         }
@@ -179,6 +186,7 @@ struct SellView {
     const int32_t *cols;
     const void *vals;
     int64_t nslices, nrows, ncols;
+    int il;  // lane-interleaved rows
 };
 
 template <class V, int R>
@@ -239,7 +247,29 @@ struct EpiParams {
     unsigned int *dot_counter;
     const int *done;
     const int *gate;
+    int vec_ok;      // every vector pointer above is 16-byte aligned
 };
+
+// R consecutive entries of a vector as 16-byte loads / stores (R * sizeof(T) is 16 or 32;
+// the caller guarantees 16-byte alignment)
+template <class T, int R>
+__device__ __forceinline__ void ld16(const T *p, T (&a)[R]) {
+    static_assert((sizeof(T) * R) % 16 == 0, "16-byte rows");
+#pragma unroll
+    for (int i = 0; i < int(sizeof(T) * R / 16); ++i) {
+        const float4 t = __ldg(reinterpret_cast<const float4 *>(p) + i);
+        memcpy(reinterpret_cast<char *>(a) + 16 * i, &t, 16);
+    }
+}
+template <class T, int R>
+__device__ __forceinline__ void st16(T *p, const T (&a)[R]) {
+#pragma unroll
+    for (int i = 0; i < int(sizeof(T) * R / 16); ++i) {
+        float4 t;
+        memcpy(&t, reinterpret_cast<const char *>(a) + 16 * i, 16);
+        reinterpret_cast<float4 *>(p)[i] = t;
+    }
+}
 
 // the product's input vector: x (XM 0), x + beta*p (XM 1), or w .* v formed on the fly
 // (XM 2: the first Jacobi iterate from zero, x1 = w .* rhs)
@@ -254,16 +284,41 @@ __device__ __forceinline__ T xin_at(const EpiParams<T> &e, T beta, int64_t j) {
     }
 }
 
+// which per-row vectors an epilogue reads (besides the product input x)
+template <int EPI>
+constexpr bool epi_reads_v() {
+    return EPI == EPI_ADD || EPI == EPI_RESIDUAL || EPI == EPI_SUB || EPI == EPI_JACOBI || EPI == EPI_PJACOBI;
+}
+template <int EPI>
+constexpr bool epi_reads_w() {
+    return EPI == EPI_JACOBI || EPI == EPI_SCALE || EPI == EPI_PJACOBI;
+}
+template <int EPI, int XM, bool DOT>
+constexpr bool epi_reads_x() {
+    return XM != 0 || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT;
+}
+
+// the stateless epilogues, from the row's product acc, input x, vector v and weight w
+template <class T, int EPI>
+__device__ __forceinline__ T epi_row(T acc, T xrow, T vrow, T wrow) {
+    if constexpr (EPI == EPI_ADD) return acc + vrow;
+    if constexpr (EPI == EPI_RESIDUAL) return vrow - acc;
+    if constexpr (EPI == EPI_SUB) return acc - vrow;
+    if constexpr (EPI == EPI_JACOBI) return xrow + wrow * (vrow - acc);
+    if constexpr (EPI == EPI_SCALE) return wrow * acc;
+    if constexpr (EPI == EPI_PJACOBI) return wrow * (vrow - acc);
+    return acc;
+}
+
 // row epilogue; returns the value stored to y[row]
 template <class T, int EPI>
 __device__ __forceinline__ T epilogue(const EpiParams<T> &e, int64_t row, T acc, T xrow) {
-    if constexpr (EPI == EPI_STORE) return acc;
-    if constexpr (EPI == EPI_ADD) return acc + e.v[row];
-    if constexpr (EPI == EPI_RESIDUAL) return e.v[row] - acc;
-    if constexpr (EPI == EPI_SUB) return acc - e.v[row];
-    if constexpr (EPI == EPI_JACOBI) return xrow + e.w[row] * (e.v[row] - acc);
-    if constexpr (EPI == EPI_SCALE) return e.w[row] * acc;
-    if constexpr (EPI == EPI_PJACOBI) return e.w[row] * (e.v[row] - acc);
+    if constexpr (EPI != EPI_CHEB && EPI != EPI_CHEB0) {
+        T vrow = T(0), wrow = T(0);
+        if constexpr (epi_reads_v<EPI>()) vrow = e.v[row];
+        if constexpr (epi_reads_w<EPI>()) wrow = e.w[row];
+        return epi_row<T, EPI>(acc, xrow, vrow, wrow);
+    }
     if constexpr (EPI == EPI_CHEB) {
         // r = r + alpha_prev * (A p); p_new = -1 * r + beta * p; x = x + alpha * p_new
         T r = e.vout[row] + e.s0 * acc;
@@ -286,6 +341,7 @@ __device__ __forceinline__ T epilogue(const EpiParams<T> &e, int64_t row, T acc,
 }
 
 constexpr int kSpmvWarps = 8;
+constexpr int kStagedMaxWidth = 32;  // widest diagonal slice the staged kernel takes
 
 // tuning knobs of the sliced-ELL kernel: slot-loop unroll depth and the minimum CTAs
 // per SM promised to the register allocator (0: no promise)
@@ -352,7 +408,9 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
         h_nxt = h_nn;
         o_lo = n_lo;
         o_hi = n_hi;
-        const int64_t row0 = s * S + int64_t(lane) * R;
+        // a lane's rows: row0 + r * rs (consecutive, or 32 apart in the interleaved layout)
+        const int rs = m.il ? 32 : 1;
+        const int64_t row0 = s * S + (m.il ? int64_t(lane) : int64_t(lane) * R);
         T acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = T(0);
@@ -368,7 +426,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    int c = r0i + r + off;
+                    int c = r0i + r * rs + off;
                     c = c < 0 ? 0 : (c > cmax ? cmax : c);
                     acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
                 }
@@ -386,18 +444,62 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 for (int r = 0; r < R; ++r) acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c[r]), acc[r]);
             }
         }
+        constexpr bool kVecEpi = EPI != EPI_CHEB && EPI != EPI_CHEB0;
+        if (kVecEpi && e.vec_ok && !m.il && row0 + R <= m.nrows) {
+            // a lane's R rows are consecutive: its epilogue vectors are 16-byte loads
+            T xr[R], vr[R], wr[R], out[R];
+            if constexpr (epi_reads_x<EPI, XM, DOT>()) {
+                if constexpr (XM == 1) {
+                    T a[R], b[R];
+                    ld16<T, R>(e.x + row0, a);
+                    ld16<T, R>(e.wvec + row0, b);
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int64_t row = row0 + r;
-            if (row < m.nrows) {
-                T xr = T(0);
-                if constexpr (XM != 0 || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, XM>(e, beta, row);
-                if constexpr (XM == 1) e.pout[row] = xr;
-                T out = epilogue<T, EPI>(e, row, acc[r], xr);
-                e.y[row] = out;
-                if constexpr (DOT) {
-                    dacc = fma(double(xr), double(out), dacc);
-                    if (e.dv) dacc2 = fma(double(xr), double(e.dv[row]), dacc2);
+                    for (int r = 0; r < R; ++r) xr[r] = a[r] + beta * b[r];
+                    st16<T, R>(e.pout + row0, xr);
+                } else if constexpr (XM == 2) {
+                    T a[R], b[R];
+                    ld16<T, R>(e.w + row0, a);
+                    ld16<T, R>(e.v + row0, b);
+#pragma unroll
+                    for (int r = 0; r < R; ++r) xr[r] = a[r] * b[r];
+                } else {
+                    ld16<T, R>(e.x + row0, xr);
+                }
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) xr[r] = T(0);
+            }
+            if constexpr (epi_reads_v<EPI>()) ld16<T, R>(e.v + row0, vr);
+            if constexpr (epi_reads_w<EPI>()) ld16<T, R>(e.w + row0, wr);
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                out[r] = epi_row<T, EPI>(acc[r], xr[r], epi_reads_v<EPI>() ? vr[r] : T(0),
+                                         epi_reads_w<EPI>() ? wr[r] : T(0));
+            }
+            st16<T, R>(e.y + row0, out);
+            if constexpr (DOT) {
+                T dr[R];
+                if (e.dv) ld16<T, R>(e.dv + row0, dr);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    dacc = fma(double(xr[r]), double(out[r]), dacc);
+                    if (e.dv) dacc2 = fma(double(xr[r]), double(dr[r]), dacc2);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) {
+                const int64_t row = row0 + int64_t(r) * rs;
+                if (row < m.nrows) {
+                    T xr = T(0);
+                    if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row);
+                    if constexpr (XM == 1) e.pout[row] = xr;
+                    T out = epilogue<T, EPI>(e, row, acc[r], xr);
+                    e.y[row] = out;
+                    if constexpr (DOT) {
+                        dacc = fma(double(xr), double(out), dacc);
+                        if (e.dv) dacc2 = fma(double(xr), double(e.dv[row]), dacc2);
+                    }
                 }
             }
         }
@@ -410,7 +512,343 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     }
 }
 
-// CSR baseline: G lanes per row, lane-strided accumulation, shuffle reduction.
+// ------------------------------------------------------------------------------------
+// Shared-memory staged sliced-ELL product (FP32 vectors; FP32 or BF16 values; every slice
+// diagonal, lane-interleaved rows).
+//
+// The register kernel above keeps a few loads per lane in flight and waits on DRAM latency
+// at every slot and at the epilogue.  Here each warp owns a ring of NST stages in shared
+// memory and keeps NST slices in flight with bulk asynchronous copies (cp.async.bulk,
+// completion counted in bytes on one mbarrier per stage):
+//   * the slice's value stream (w slots x S rows, contiguous),
+//   * the x windows it gathers from: slot k reads x[row + off_k] for the slice's S rows,
+//     a contiguous window; offsets closer than kStagedGap share one window,
+//   * the slice's rows of the epilogue vectors (v, w, and x for the Jacobi form).
+// Every x gather and epilogue read then hits shared memory, and with the interleaved row
+// layout a warp's reads for one r are 32 consecutive floats (conflict-free).  Row sums run
+// over the slots in the same order as the register kernel, so both give identical bits.
+// ------------------------------------------------------------------------------------
+constexpr int kStagedWarps = 4;      // warps per CTA
+constexpr int kStagedMaxStages = 4;
+constexpr int kStagedGap = 16;       // offsets at most this far apart share one x window
+constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[32], xb[32]
+constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
+
+struct StagedCfg {
+    int nst;               // stages per warp
+    uint32_t warp_bytes;   // shared bytes per warp (barriers + descriptors + stages)
+    uint32_t hdr_bytes;    // barriers + descriptors
+    uint32_t stage_bytes;
+    uint32_t o_x, o_x2, o_xr, o_v, o_w;  // byte offsets inside a stage
+    int xcap;              // floats of one window region
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+    return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait for a stage's copies; false if they did not land within kStagedSpinCycles
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity)) {
+        if (clock64() - t0 > kStagedSpinCycles) return false;
+    }
+    return true;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+// global -> shared bulk copy (16-byte aligned addresses, size a multiple of 16)
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_addr(dst)),
+        "l"(src), "r"(bytes), "r"(smem_addr(bar))
+        : "memory");
+}
+
+// Floats of x that the staged kernel copies for slice s (offsets off[0..w) ascending): one
+// window per group of offsets at most kStagedGap apart, each covering the group's clamped
+// gathers rounded out to 16 bytes.  Same arithmetic as the kernel's issue step.
+__device__ __forceinline__ int staged_window_floats(const int32_t *off, int w, int r0, int S, int cmax) {
+    int total = 0;
+    for (int a = 0; a < w;) {
+        int b = a;
+        while (b + 1 < w && off[b + 1] - off[b] <= kStagedGap) ++b;
+        const int lo = min(max(r0 + off[a], 0), cmax);
+        const int hi = min(max(r0 + S - 1 + off[b], 0), cmax);
+        total += ((hi + 4) & ~3) - (lo & ~3);
+        a = b + 1;
+    }
+    return total;
+}
+
+__global__ void k_sell_window_max(const int4 *hdr, const int32_t *offs, int64_t ns, int S, int64_t ncols,
+                                  int *out) {
+    int best = 0;
+    for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < ns; s += int64_t(gridDim.x) * blockDim.x) {
+        const int4 q = hdr[s];
+        if (q.z > 0) best = max(best, staged_window_floats(offs + q.w, q.z, int(s * S), S, int(ncols) - 1));
+    }
+    best = max(best, __reduce_max_sync(0xffffffffu, best));
+    if ((threadIdx.x & 31) == 0) atomicMax(out, best);
+}
+
+template <class V>
+__device__ __forceinline__ void smem_vals4(const V *p, float (&v)[4]);
+template <>
+__device__ __forceinline__ void smem_vals4<float>(const float *p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void smem_vals4<__nv_bfloat16>(const __nv_bfloat16 *p, float (&v)[4]) {
+    const uint2 t = *reinterpret_cast<const uint2 *>(p);
+    const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.x));
+    const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.y));
+    v[0] = fa.x; v[1] = fa.y; v[2] = fb.x; v[3] = fb.y;
+}
+
+template <int EPI, int XM>
+struct StagedNeeds {
+    static constexpr bool xr = XM == 0 && EPI == EPI_JACOBI;                // x rows (Jacobi form)
+    static constexpr bool v = epi_reads_v<EPI>() || XM == 2;
+    static constexpr bool w = epi_reads_w<EPI>() || XM == 2;
+};
+
+template <class V, int EPI, int XM>
+__global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, EpiParams<float> e, StagedCfg cfg,
+                                                                   int *kflag) {
+    if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
+    constexpr int R = 4, S = 32 * R;
+    using Nd = StagedNeeds<EPI, XM>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int nst = cfg.nst;
+    unsigned char *wbase = smem + size_t(wib) * cfg.warp_bytes;
+    uint64_t *bar = reinterpret_cast<uint64_t *>(wbase);
+    int *desc = reinterpret_cast<int *>(wbase + 8 * kStagedMaxStages);
+    unsigned char *stage0 = wbase + cfg.hdr_bytes;
+    const V *vals = static_cast<const V *>(m.vals);
+    const int64_t ns = m.nslices;
+    const int64_t warp0 = int64_t(blockIdx.x) * kStagedWarps + wib;
+    const int64_t nwarps = int64_t(gridDim.x) * kStagedWarps;
+    const int cmax = int(m.ncols) - 1;
+    const unsigned full = 0xffffffffu;
+
+    if (lane == 0) {
+        for (int i = 0; i < nst; ++i) mbar_init(&bar[i], 1);
+        mbar_fence_init();
+    }
+    __syncwarp();
+
+    // per-slice metadata a lane needs to issue its copies: header and its slot's offset.
+    // Headers are loaded one slice before the offsets they point to, so neither load waits
+    // on the other inside an iteration.
+    struct Meta {
+        int64_t base;
+        int w;
+        int off;
+    };
+    auto load_hdr = [&](int64_t s) -> int4 {
+        return s < ns ? __ldg(reinterpret_cast<const int4 *>(m.hdr) + s) : make_int4(0, 0, 0, 0);
+    };
+    auto meta_of = [&](const int4 &q) -> Meta {
+        Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), q.z, 0};
+        if (lane < mt.w) mt.off = __ldg(m.offs + q.w + lane);
+        return mt;
+    };
+
+    // issue the copies of slice s into stage st (whole warp, converged)
+    auto issue = [&](int64_t s, int st, const Meta &mt) {
+        unsigned char *sg = stage0 + size_t(st) * cfg.stage_bytes;
+        int *d = desc + st * kStagedDesc;
+        const int w = mt.w;
+        const int r0 = int(s * S);
+        const int rows = int(min(int64_t(S), m.nrows - int64_t(r0)));
+        const int offk = mt.off;
+        const int prev = __shfl_up_sync(full, offk, 1);
+        const bool start = lane < w && (lane == 0 || offk - prev > kStagedGap);
+        const unsigned gmask = __ballot_sync(full, start);
+        // my group's last slot: one before the next group start, or w - 1
+        const unsigned after = lane == 31 ? 0u : (gmask & ~((2u << lane) - 1u));
+        const int last = after ? (__ffs(after) - 2) : (w - 1);
+        const int offl = __shfl_sync(full, offk, last & 31);
+        int len = 0, lo_r = 0;
+        if (start) {
+            // clamped columns of the group's gathers lie in [lo, hi]; the window covers it
+            // rounded out to 16 bytes (ncols is a multiple of 4, so it stays inside x)
+            const int lo = min(max(r0 + offk, 0), cmax);
+            const int hi = min(max(r0 + S - 1 + offl, 0), cmax);
+            lo_r = lo & ~3;
+            len = ((hi + 4) & ~3) - lo_r;
+        }
+        int incl = len;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(full, incl, o);
+            if (lane >= o) incl += t;
+        }
+        const int woff = incl - len;  // float offset of my window in the stage's window region
+        const int xtot = __shfl_sync(full, incl, 31);
+        const unsigned upto = lane == 31 ? gmask : (gmask & ((2u << lane) - 1u));
+        const int first = upto ? 31 - __clz(upto) : 0;
+        const int xb = __shfl_sync(full, woff - lo_r, first);
+        // the stage is free: every lane's reads of its previous slice are done
+        // interior slice: no gather of any row leaves [0, ncols), so slot k's reads for lane l
+        // and row 32 r + l sit at (r0 + off_k + xb_k) + l + 32 r without clamping
+        const int off_lo = __shfl_sync(full, offk, 0);
+        const int off_hi = __shfl_sync(full, offk, (w - 1) & 31);
+        const bool interior = w > 0 && r0 + off_lo >= 0 && r0 + S - 1 + off_hi <= cmax;
+        if (lane < w) {
+            d[2 + lane] = offk;
+            d[34 + lane] = interior ? r0 + offk + xb : xb;
+        }
+        if (lane == 0) {
+            d[0] = w;
+            d[1] = interior ? 1 : 0;
+        }
+        const uint32_t vbytes = uint32_t(w) * S * uint32_t(sizeof(V));
+        const uint32_t rbytes = uint32_t(rows) * 4u;
+        uint32_t total = vbytes + uint32_t(xtot) * 4u * (XM == 2 ? 2u : 1u);
+        if (Nd::xr) total += rbytes;
+        if (Nd::v) total += rbytes;
+        if (Nd::w) total += rbytes;
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect_tx(&bar[st], total);
+        __syncwarp();
+        if (lane == 0 && vbytes) bulk_g2s(sg, vals + mt.base, vbytes, &bar[st]);
+        if (start) {
+            if constexpr (XM == 2) {
+                bulk_g2s(sg + cfg.o_x + 4u * woff, e.w + lo_r, 4u * len, &bar[st]);
+                bulk_g2s(sg + cfg.o_x2 + 4u * woff, e.v + lo_r, 4u * len, &bar[st]);
+            } else {
+                bulk_g2s(sg + cfg.o_x + 4u * woff, e.x + lo_r, 4u * len, &bar[st]);
+            }
+        }
+        if (Nd::xr && lane == 1) bulk_g2s(sg + cfg.o_xr, e.x + r0, rbytes, &bar[st]);
+        if (Nd::v && lane == 2) bulk_g2s(sg + cfg.o_v, e.v + r0, rbytes, &bar[st]);
+        if (Nd::w && lane == 3) bulk_g2s(sg + cfg.o_w, e.w + r0, rbytes, &bar[st]);
+    };
+
+    // the product and epilogue of slice s from stage st
+    auto compute = [&](int64_t s, int st) {
+        const unsigned char *sg = stage0 + size_t(st) * cfg.stage_bytes;
+        const int *d = desc + st * kStagedDesc;
+        const int w = d[0];
+        const int r0 = int(s * S);
+        const V *sv = reinterpret_cast<const V *>(sg);
+        const float *sx = reinterpret_cast<const float *>(sg + cfg.o_x);
+        const float *sx2 = reinterpret_cast<const float *>(sg + cfg.o_x2);
+        float acc[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[r] = 0.f;
+        if (d[1]) {
+            const float *xl = sx + lane;
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const float *xp = xl + d[34 + k];
+                float v[R];
+                smem_vals4<V>(sv + k * S + lane * R, v);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float xv;
+                    if constexpr (XM == 2) xv = xp[32 * r] * xp[32 * r + (sx2 - sx)];
+                    else xv = xp[32 * r];
+                    acc[r] = fmaf(v[r], xv, acc[r]);
+                }
+            }
+        } else {
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const int off = d[2 + k];
+                const int xb = d[34 + k];
+                float v[R];
+                smem_vals4<V>(sv + k * S + lane * R, v);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int c = min(max(r0 + lane + 32 * r + off, 0), cmax) + xb;
+                    float xv;
+                    if constexpr (XM == 2) xv = sx[c] * sx2[c];
+                    else xv = sx[c];
+                    acc[r] = fmaf(v[r], xv, acc[r]);
+                }
+            }
+        }
+        const float *sxr = reinterpret_cast<const float *>(sg + cfg.o_xr);
+        const float *svv = reinterpret_cast<const float *>(sg + cfg.o_v);
+        const float *sww = reinterpret_cast<const float *>(sg + cfg.o_w);
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int rl = lane + 32 * r;
+            const int64_t row = int64_t(r0) + rl;
+            if (row < m.nrows) {
+                float vr = 0.f, wr = 0.f, xr = 0.f;
+                if constexpr (Nd::v) vr = svv[rl];
+                if constexpr (Nd::w) wr = sww[rl];
+                if constexpr (XM == 2) xr = wr * vr;
+                else if constexpr (Nd::xr) xr = sxr[rl];
+                e.y[row] = epi_row<float, EPI>(acc[r], xr, vr, wr);
+            }
+        }
+    };
+
+    // prologue: fill the ring
+    for (int i = 0; i < nst; ++i) {
+        const int64_t s = warp0 + int64_t(i) * nwarps;
+        if (s < ns) issue(s, i, meta_of(load_hdr(s)));
+    }
+    int4 hq = load_hdr(warp0 + int64_t(nst) * nwarps);
+    int it = 0;
+    bool ok = true;
+    for (int64_t s = warp0; s < ns; s += nwarps, ++it) {
+        const int st = it % nst;
+        const int64_t s_next = s + int64_t(nst) * nwarps;
+        const Meta mt = meta_of(hq);  // in flight while this slice is computed
+        hq = load_hdr(s_next + nwarps);
+        if (!mbar_wait_bounded(&bar[st], uint32_t(it / nst) & 1u)) {
+            ok = false;
+            break;
+        }
+        compute(s, st);
+        __syncwarp();
+        if (s_next < ns) issue(s_next, st, mt);
+    }
+    if (!ok) {
+        // record the failure and let the copies still in flight land before the CTA exits
+        if (lane == 0) atomicExch(kflag, 1);
+        for (int j = 0; j < nst; ++j) {
+            const int64_t s = warp0 + int64_t(it + j) * nwarps;
+            if (s < ns) mbar_wait_bounded(&bar[(it + j) % nst], uint32_t((it + j) / nst) & 1u);
+        }
+    }
+}
+
+
 // The loop is warp-uniform (each warp covers 32/G rows per step) so the shuffles
 // always see the full warp.
 template <class V, class T, int G, int EPI, int XM, bool DOT>
@@ -437,7 +875,7 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (row < nrows && sub == 0) {
             T xr = T(0);
-            if constexpr (XM != 0 || EPI == EPI_JACOBI || EPI == EPI_CHEB || DOT) xr = xin_at<T, XM>(e, beta, row);
+            if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row);
             if constexpr (XM == 1) e.pout[row] = xr;
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
@@ -478,6 +916,8 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.dot_counter = a.dot_counter;
     e.done = a.done;
     e.gate = a.gate;
+    auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    e.vec_ok = al(a.x) && al(a.p) && al(a.pout) && al(a.v) && al(a.w) && al(a.y) && al(a.dv);
     return e;
 }
 
@@ -494,7 +934,7 @@ void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
     SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
                s.offs.as<int32_t>(),
-               s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols};
+               s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols, s.interleaved ? 1 : 0};
     // one wave of resident CTAs (grid-stride over slices)
     static int per_sm = 0;
     if (per_sm == 0) {
@@ -506,6 +946,76 @@ void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * per_sm)));
     if constexpr (DOT) g = std::min(g, kSpmvDotGrid);
     k_sell_spmv<V, T, R, EPI, XM, DOT><<<g, kSpmvWarps * 32, 0, ctx.stream>>>(m, make_epi<T>(a));
+}
+
+#ifndef UGPU_SELL_STAGED
+#define UGPU_SELL_STAGED 1
+#endif
+
+inline uint32_t round128(uint32_t b) { return (b + 127u) & ~127u; }
+
+// Launches the staged kernel when the matrix and vectors allow it; false otherwise.
+template <class V, int EPI, int XM>
+bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
+    const Sell &s = *A.sell;
+    if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
+    const EpiParams<float> e = make_epi<float>(a);
+    if (!e.vec_ok) return false;
+    using Nd = StagedNeeds<EPI, XM>;
+    constexpr int S = 128;
+    StagedCfg c{};
+    const int wcap = std::max(1, s.max_width);
+    c.xcap = std::max(4, s.xwin_max);
+    const uint32_t vals_b = round128(uint32_t(wcap) * S * uint32_t(sizeof(V)));
+    const uint32_t x_b = round128(uint32_t(c.xcap) * 4u);
+    uint32_t o = vals_b;
+    c.o_x = o;
+    o += x_b;
+    c.o_x2 = o;
+    if (XM == 2) o += x_b;
+    c.o_xr = o;
+    if (Nd::xr) o += S * 4;
+    c.o_v = o;
+    if (Nd::v) o += S * 4;
+    c.o_w = o;
+    if (Nd::w) o += S * 4;
+    c.stage_bytes = round128(o);
+    c.hdr_bytes = round128(8u * kStagedMaxStages + 4u * kStagedDesc * kStagedMaxStages);
+    auto kern = k_sell_staged<V, EPI, XM>;
+    static bool attr = false;
+    if (!attr) {
+        UGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+        attr = true;
+    }
+    // Ring depth: the per-slice work is latency-bound instruction issue, so first as many
+    // resident warps as possible up to 16 per SM, then as many bytes in flight as possible
+    // (about 64 KB per SM covers the HBM latency-bandwidth product).
+    int best_nst = 0, best_per_sm = 0;
+    long long best_score = 0;
+    for (int nst = kStagedMaxStages; nst >= 2; --nst) {
+        const uint32_t cta = kStagedWarps * (c.hdr_bytes + uint32_t(nst) * c.stage_bytes);
+        if (cta > 227u * 1024u) continue;
+        int per_sm = 0;
+        UGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStagedWarps * 32, cta));
+        const long long warps = per_sm * kStagedWarps;
+        const long long inflight = warps * (nst - 1) * c.stage_bytes;
+        const long long score = std::min(warps, 16ll) * 1000000ll + std::min(inflight, 65536ll) * 8 + warps;
+        if (per_sm > 0 && score > best_score) {
+            best_score = score;
+            best_nst = nst;
+            best_per_sm = per_sm;
+        }
+    }
+    if (best_nst == 0) return false;
+    c.nst = best_nst;
+    c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
+    const uint32_t cta = kStagedWarps * c.warp_bytes;
+    SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
+               s.offs.as<int32_t>(), s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols, 1};
+    const int64_t want = (s.nslices + kStagedWarps - 1) / kStagedWarps;
+    const int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * best_per_sm)));
+    kern<<<g, kStagedWarps * 32, cta, ctx.stream>>>(m, e, c, ctx.d_kflags());
+    return true;
 }
 
 template <class V, class T, int EPI, int XM, bool DOT>
@@ -534,6 +1044,10 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
     } else {
         constexpr int R = std::is_same<V, double>::value ? 2 : 4;
         UGPU_CHECK(A.sell->R == R, UGPU_ERR_INTERNAL, "sliced-ELL rows-per-thread mismatch");
+        if constexpr (std::is_same<T, float>::value && !std::is_same<V, double>::value && !DOT &&
+                      (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0) {
+            if (staged_launch<V, EPI, XM>(ctx, A, a)) return;
+        }
         sell_launch<V, T, R, EPI, XM, DOT>(ctx, A, a);
     }
 }
@@ -624,6 +1138,8 @@ void build_sell(Mat &A) {
     }
     s->nstored = sptr[ns];
     s->ndiag_slices = ndiag;
+    s->interleaved = A.vdtype != UGPU_F64 && ndiag == ns && maxw <= kStagedMaxWidth && A.nrows % 4 == 0 &&
+                     A.ncols % 4 == 0;
     s->max_width = maxw;
     s->noffs = noffs;
     s->ncols_explicit = ncol;
@@ -651,7 +1167,8 @@ void build_sell(Mat &A) {
             k_sell_fill<V><<<gA, kAnalyzeThreads, 0, ctx.stream>>>(
                 A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), A.vals.as<V>(), A.nrows, A.ncols, S, ns,
                 s->slice_w.as<int32_t>(), s->slice_ptr.as<int64_t>(), s->slice_aux.as<int64_t>(),
-                offs_tmp.as<int32_t>(), s->offs.as<int32_t>(), s->cols.as<int32_t>(), s->vals.as<V>());
+                offs_tmp.as<int32_t>(), s->offs.as<int32_t>(), s->cols.as<int32_t>(), s->vals.as<V>(),
+                s->interleaved);
         };
         if (A.vdtype == UGPU_F64) fill(double{});
         else if (A.vdtype == UGPU_F32) fill(float{});
@@ -659,7 +1176,19 @@ void build_sell(Mat &A) {
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
     }
+    Buffer wmax;
+    int h_wmax = 0;
+    if (ns && s->interleaved) {
+        wmax.alloc(sizeof(int));
+        UGPU_CUDA(cudaMemsetAsync(wmax.ptr, 0, sizeof(int), ctx.stream));
+        k_sell_window_max<<<gA, kAnalyzeThreads, 0, ctx.stream>>>(s->hdr.as<int4>(), s->offs.as<int32_t>(), ns, S,
+                                                                  A.ncols, wmax.as<int>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+        UGPU_CUDA(cudaMemcpyAsync(&h_wmax, wmax.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+    }
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));  // host vectors above must outlive the copies
+    s->xwin_max = h_wmax;
     A.sell = std::move(s);
 }
 
@@ -936,6 +1465,15 @@ int ugpu_mat_sell_info(const ugpu_mat *A, int64_t *nslices, int64_t *nstored, in
     if (nstored) *nstored = s.nstored;
     if (ndiag_slices) *ndiag_slices = s.ndiag_slices;
     if (rows_per_slice) *rows_per_slice = s.S;
+    UGPU_ABI_END(nullptr)
+}
+
+int ugpu_mat_sell_layout(const ugpu_mat *A, int *interleaved) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(interleaved);
+    UGPU_CHECK(A->impl.sell != nullptr, UGPU_ERR_STATE, "matrix has no sliced-ELL layout");
+    *interleaved = A->impl.sell->interleaved ? 1 : 0;
     UGPU_ABI_END(nullptr)
 }
 
