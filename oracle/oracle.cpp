@@ -765,6 +765,8 @@ bool fcg(const Csr &A, const double *b, double *x, Precond &M, const Params &prm
     st.spmv_count++;
     M.apply(r.data(), z.data());
     p = z;
+    // (p, r) by the recurrence (p', r') = (z, r') + beta ((p, r) - alpha (p, q)) (r' = r - alpha q)
+    double pr = dot(n, z.data(), r.data());
     int64_t it = 0;
     double r_norm = 9e9;
     bool stop = false;
@@ -772,7 +774,7 @@ bool fcg(const Csr &A, const double *b, double *x, Precond &M, const Params &prm
         spmv(A, p.data(), q.data());
         st.spmv_count++;
         double pq = dot(n, p.data(), q.data());
-        double alpha = dot(n, p.data(), r.data()) / pq;
+        double alpha = pr / pq;
         if (std::isinf(alpha) || std::isnan(alpha)) {
             stop = check_convergence(prm, st, it, r_norm, 1, 1);
             if (!stop) st.reason = DIVERGED_NAN;
@@ -790,6 +792,7 @@ bool fcg(const Csr &A, const double *b, double *x, Precond &M, const Params &prm
         std::fill(z.begin(), z.end(), 0.0);
         M.apply(r.data(), z.data());
         double beta = -dot(n, z.data(), q.data()) / pq;
+        pr = dot(n, z.data(), r.data()) + beta * (pr - alpha * pq);
         for (int64_t i = 0; i < n; ++i) p[i] = z[i] + beta * p[i];
         stop = check_convergence(prm, st, it, r_norm, 1, 1);
         it++;

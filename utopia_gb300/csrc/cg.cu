@@ -3,7 +3,8 @@
 // Mirrors ConjugateGradient::preconditioned_solve / unpreconditioned_solve
 // (utopia/solvers/smoothers/utopia_ConjugateGradient_impl.hpp:90-294) and adds the
 // flexible form (Notay's FCG(1): alpha = (p,r)/(p,Ap), beta = -(z,Ap)/(p,Ap)) used as
-// the FP64 outer iteration of the mixed-precision multigrid preconditioner.
+// the FP64 outer iteration of the mixed-precision multigrid preconditioner; (p,r) follows
+// the scalar recurrence (p',r') = (z,r') + beta ((p,r) - alpha (p,Ap)) instead of a dot.
 //
 // The reference evaluates alpha, beta and the stopping test on the host after every
 // dot.  Here the dots finish in the last CTA of the kernel that produces them, the
@@ -49,6 +50,10 @@ namespace {
 
 enum CgMode : int { CG_PLAIN = 0, CG_JACOBI = 1, CG_GENERIC = 2 };
 
+__device__ __forceinline__ double2 ld2(const double *p, int64_t j) { return reinterpret_cast<const double2 *>(p)[j]; }
+__device__ __forceinline__ void st2(double *p, int64_t j, double2 v) { reinterpret_cast<double2 *>(p)[j] = v; }
+inline bool al16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 __device__ __forceinline__ void cg_stop(CgDev *d, int reason, int converged) {
     d->done = 1;
     d->reason = reason;
@@ -64,7 +69,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
                                                       const double *__restrict__ dinv, double *__restrict__ z,
                                                       float *__restrict__ r32, CgDev *dev, double *partials,
                                                       unsigned int *counter, double atol, long long max_it,
-                                                      int flexible) {
+                                                      int flexible, int vec) {
     if (dev->done) return;
     if (MODE == CG_PLAIN && dev->pAp == 0.0) {
         // `if (dot_pq == 0.) { converged = true; break; }`
@@ -84,7 +89,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
         return;
     }
     double a0 = 0.0, a1 = 0.0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    auto one = [&](int64_t i) {
         x[i] = x[i] + alpha * p[i];
         double ri = r[i] - alpha * Ap[i];
         r[i] = ri;
@@ -95,6 +100,32 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
             a1 = fma(zi, ri, a1);
         }
         if constexpr (R32) r32[i] = float(ri);
+    };
+    const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+    if (vec) {
+        // pairs of elements as 16-byte loads and stores
+        const int64_t n2 = n >> 1;
+#pragma unroll 2
+        for (int64_t j = tid; j < n2; j += nth) {
+            const double2 xv = ld2(x, j), pv = ld2(p, j), rv = ld2(r, j), qv = ld2(Ap, j);
+            const double r0 = rv.x - alpha * qv.x, r1 = rv.y - alpha * qv.y;
+            st2(x, j, make_double2(xv.x + alpha * pv.x, xv.y + alpha * pv.y));
+            st2(r, j, make_double2(r0, r1));
+            a0 = fma(r0, r0, a0);
+            a0 = fma(r1, r1, a0);
+            if constexpr (MODE == CG_JACOBI) {
+                const double2 dv = ld2(dinv, j);
+                const double z0 = dv.x * r0, z1 = dv.y * r1;
+                st2(z, j, make_double2(z0, z1));
+                a1 = fma(z0, r0, a1);
+                a1 = fma(z1, r1, a1);
+            }
+            if constexpr (R32) reinterpret_cast<float2 *>(r32)[j] = make_float2(float(r0), float(r1));
+        }
+        if ((n & 1) && tid == 0) one(n - 1);
+    } else {
+        for (int64_t i = tid; i < n; i += nth) one(i);
     }
     double acc[2] = {a0, a1};
     const int nd = (MODE == CG_JACOBI) ? 2 : 1;
@@ -138,13 +169,42 @@ template <class ZT>
 __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__restrict__ zin,
                                                      const double *__restrict__ r, const double *__restrict__ q,
                                                      CgDev *dev, double *partials, unsigned int *counter,
-                                                     long long max_it, int flexible) {
+                                                     long long max_it, int flexible, int vec) {
     if (dev->done) return;
     double a0 = 0.0, a1 = 0.0;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+    auto one = [&](int64_t i) {
         double zi = double(zin[i]);
         a0 = fma(zi, r[i], a0);
         if (flexible) a1 = fma(zi, q[i], a1);
+    };
+    if (vec) {
+        const int64_t n2 = n >> 1;
+#pragma unroll 2
+        for (int64_t j = tid; j < n2; j += nth) {
+            double z0, z1;
+            if constexpr (sizeof(ZT) == 4) {
+                const float2 t = reinterpret_cast<const float2 *>(zin)[j];
+                z0 = t.x;
+                z1 = t.y;
+            } else {
+                const double2 t = ld2(reinterpret_cast<const double *>(zin), j);
+                z0 = t.x;
+                z1 = t.y;
+            }
+            const double2 rv = ld2(r, j);
+            a0 = fma(z0, rv.x, a0);
+            a0 = fma(z1, rv.y, a0);
+            if (flexible) {
+                const double2 qv = ld2(q, j);
+                a1 = fma(z0, qv.x, a1);
+                a1 = fma(z1, qv.y, a1);
+            }
+        }
+        if ((n & 1) && tid == 0) one(n - 1);
+    } else {
+        for (int64_t i = tid; i < n; i += nth) one(i);
     }
     double acc[2] = {a0, a1};
     const int nd = flexible ? 2 : 1;
@@ -152,7 +212,11 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
     double sums[2];
     if (finish_last_block(nd, partials, gridDim.x, sums, counter) && threadIdx.x == 0) {
         if (flexible) {
-            dev->beta = -sums[1] / dev->pAp;
+            // (p_new, r) without a dot over p: p_new = z + beta p and, after r -= alpha Ap,
+            // (p, r) = (p, r)_old - alpha (p, Ap)
+            const double beta = -sums[1] / dev->pAp;
+            dev->beta = beta;
+            dev->pr = sums[0] + beta * (dev->pr - dev->alpha * dev->pAp);
         } else {
             dev->beta = sums[0] / dev->rz;
         }
@@ -165,17 +229,38 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
 // K0: p = z + beta p (z in FP64 or, for the mixed form, FP32)
 template <class ZT>
 __global__ void __launch_bounds__(kBlock) k_cg_pupdate(int64_t n, const ZT *__restrict__ z, double *__restrict__ p,
-                                                       const CgDev *dev) {
+                                                       const CgDev *dev, int vec) {
     if (dev->done) return;
     const double beta = dev->beta;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
-        p[i] = double(z[i]) + beta * p[i];
+    const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+    if (vec) {
+        const int64_t n2 = n >> 1;
+#pragma unroll 2
+        for (int64_t j = tid; j < n2; j += nth) {
+            double z0, z1;
+            if constexpr (sizeof(ZT) == 4) {
+                const float2 t = reinterpret_cast<const float2 *>(z)[j];
+                z0 = t.x;
+                z1 = t.y;
+            } else {
+                const double2 t = ld2(reinterpret_cast<const double *>(z), j);
+                z0 = t.x;
+                z1 = t.y;
+            }
+            const double2 pv = ld2(p, j);
+            st2(p, j, make_double2(z0 + beta * pv.x, z1 + beta * pv.y));
+        }
+        if ((n & 1) && tid == 0) p[n - 1] = double(z[n - 1]) + beta * p[n - 1];
+    } else {
+        for (int64_t i = tid; i < n; i += nth) p[i] = double(z[i]) + beta * p[i];
+    }
 }
 
 __global__ void k_cg_init(CgDev *dev, double rz, double rnorm, long long it0) {
     dev->rz = rz;
     dev->pAp = 0;
-    dev->pr = 0;
+    dev->pr = rz;  // flexible form: p = z at the start, so (p, r) = (z, r)
     dev->beta = 0;
     dev->rnorm = rnorm;
     dev->alpha = 0;
@@ -368,12 +453,14 @@ private:
         const int g = reduce_grid(n);
         const bool f32 = mode_ == CG_GENERIC && pc_->pc_dtype() == UGPU_F32;
         // K0: p = z + beta p   (plain CG: p = r + beta p)
+        // the solver's own vectors are cudaMalloc'd; only x may be caller memory
+        const int vec = al16(x) ? 1 : 0;
         if (f32)
-            k_cg_pupdate<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), p_.as<double>(), dev);
+            k_cg_pupdate<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), p_.as<double>(), dev, 1);
         else
             k_cg_pupdate<double><<<g, kBlock, 0, ctx->stream>>>(n, (mode_ == CG_PLAIN) ? r_.as<double>()
                                                                                        : z_.as<double>(),
-                                                                p_.as<double>(), dev);
+                                                                p_.as<double>(), dev, 1);
         ctx->launches++;
         // K1: Ap = A p ; (p, Ap) [, (p, r)]
         {
@@ -385,7 +472,6 @@ private:
             a.dot_partials = part;
             a.dot_out = &dev->pAp;
             a.dot_counter = cnt + 0;
-            if (flexible_) a.dv = r_.ptr;
             a.done = &dev->done;
             launch_spmv(*ctx, *op, a);
         }
@@ -397,7 +483,8 @@ private:
 #define UGPU_CG_UPD(M, R)                                                                                          \
     k_cg_update<M, R><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<double *>(x), p_.as<double>(), r_.as<double>(), \
                                                      Ap_.as<double>(), dinv, z_.as<double>(), r32_.as<float>(), dev,  \
-                                                     part + 2 * kSpmvDotGrid, cnt + 1, atol, max_it, int(flexible_))
+                                                     part + 2 * kSpmvDotGrid, cnt + 1, atol, max_it, int(flexible_), \
+                                                     vec)
             if (mode_ == CG_PLAIN) UGPU_CG_UPD(CG_PLAIN, false);
             else if (mode_ == CG_JACOBI) UGPU_CG_UPD(CG_JACOBI, false);
             else if (f32) UGPU_CG_UPD(CG_GENERIC, true);
@@ -413,11 +500,11 @@ private:
         if (f32)
             k_cg_zdots<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), r_.as<double>(), Ap_.as<double>(),
                                                              dev, part + 4 * kSpmvDotGrid, cnt + 2, max_it,
-                                                             int(flexible_));
+                                                             int(flexible_), 1);
         else
             k_cg_zdots<double><<<g, kBlock, 0, ctx->stream>>>(n, z_.as<double>(), r_.as<double>(), Ap_.as<double>(),
                                                               dev, part + 4 * kSpmvDotGrid, cnt + 2, max_it,
-                                                              int(flexible_));
+                                                              int(flexible_), 1);
         ctx->launches++;
         UGPU_LAUNCH_CHECK();
     }

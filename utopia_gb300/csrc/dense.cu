@@ -176,23 +176,52 @@ __global__ void k_zero(double *p, int64_t m) {
         p[i] = 0.0;
 }
 
-// x = Ainv * r (one warp per row); input/output dtypes converted on the fly
-template <class TI, class TO>
-__global__ void __launch_bounds__(256) k_gemv(const double *M, int64_t n, const TI *r, TO *x, const int *done) {
+// x = Ainv * r, one CTA per row (the coarse matrix has only a few thousand rows, so a warp
+// per row would leave each warp a long chain of dependent load rounds); the matrix and the
+// vectors share the type T (the FP64 inverse for FP64 vectors, its FP32 copy for FP32).
+// Rows are read as 16-byte vectors when n and the pointers allow it.
+constexpr int kGemvThreads = 256;
+template <class T>
+__global__ void __launch_bounds__(kGemvThreads) k_gemv(const T *M, int64_t n, const T *r, T *x, const int *done,
+                                                       int vec) {
     if (done && *done) return;
-    const int lane = threadIdx.x & 31;
-    const int64_t w0 = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
-    for (int64_t i = w0; i < n; i += nw) {
-        const double *row = M + i * n;
-        double s = 0.0;
-        for (int64_t c = lane; c < n; c += 32) s = fma(__ldg(row + c), cvt<double>(__ldg(r + c)), s);
+    constexpr int V = 16 / sizeof(T);  // elements per 16-byte vector
+    using Vec = typename std::conditional<sizeof(T) == 8, double2, float4>::type;
+    __shared__ T part[kGemvThreads / 32];
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const T *row = M + i * n;
+        T s = T(0);
+        if (vec) {
+            const Vec *rv = reinterpret_cast<const Vec *>(row);
+            const Vec *xv = reinterpret_cast<const Vec *>(r);
+            for (int64_t c = threadIdx.x; c < n / V; c += kGemvThreads) {
+                const Vec a = __ldg(rv + c), b = __ldg(xv + c);
+                const T *pa = reinterpret_cast<const T *>(&a);
+                const T *pb = reinterpret_cast<const T *>(&b);
+#pragma unroll
+                for (int q = 0; q < V; ++q) s = fma(pa[q], pb[q], s);
+            }
+        } else {
+            for (int64_t c = threadIdx.x; c < n; c += kGemvThreads) s = fma(__ldg(row + c), __ldg(r + c), s);
+        }
         s = warp_sum(s);
-        if (lane == 0) x[i] = cvt<TO>(s);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            T t = threadIdx.x < kGemvThreads / 32 ? part[threadIdx.x] : T(0);
+            t = warp_sum(t);
+            if (threadIdx.x == 0) x[i] = t;
+        }
+        __syncthreads();
     }
 }
 
 }  // namespace
+
+void DenseCholesky::make_fp32_inverse() {
+    Ainv32.alloc(sizeof(float) * std::max<int64_t>(n * n, 1));
+    if (n) launch_convert(*ctx, Ainv.ptr, UGPU_F64, Ainv32.ptr, UGPU_F32, n * n);
+}
 
 bool DenseCholesky::factor(const Mat &A) {
     UGPU_CHECK(A.nrows == A.ncols, UGPU_ERR_ARG, "coarse solver: square matrix required");
@@ -202,6 +231,7 @@ bool DenseCholesky::factor(const Mat &A) {
     UGPU_CHECK(n <= 16384, UGPU_ERR_UNSUPPORTED, "coarse solver: dense size limited to 16384");
     L.alloc(sizeof(double) * std::max<int64_t>(n * n, 1));
     Ainv.alloc(sizeof(double) * std::max<int64_t>(n * n, 1));
+    Ainv32.release();
     if (n == 0) return true;
     double *Lp = L.as<double>();
     double *Y = Ainv.as<double>();  // holds L^-1 first
@@ -276,14 +306,18 @@ void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int 
     Context &c = *ctx;
     if (n == 0) return;
     int g = int(std::min<int64_t>((n * 32 + 255) / 256, int64_t(c.sms) * 8));
-    const double *M = Ainv.as<double>();
-    if (rdt == UGPU_F64 && xdt == UGPU_F64)
-        k_gemv<double, double><<<g, 256, 0, c.stream>>>(M, n, static_cast<const double *>(rhs),
-                                                         static_cast<double *>(x), done);
-    else if (rdt == UGPU_F32 && xdt == UGPU_F32)
-        k_gemv<float, float><<<g, 256, 0, c.stream>>>(M, n, static_cast<const float *>(rhs), static_cast<float *>(x),
-                                                      done);
-    else
+    g = int(std::min<int64_t>(std::max<int64_t>(n, 1), int64_t(c.sms) * 8));
+    auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
+    if (rdt == UGPU_F64 && xdt == UGPU_F64) {
+        const int vec = (n % 2 == 0) && al(Ainv.ptr) && al(rhs);
+        k_gemv<double><<<g, kGemvThreads, 0, c.stream>>>(Ainv.as<double>(), n, static_cast<const double *>(rhs),
+                                                          static_cast<double *>(x), done, vec);
+    } else if (rdt == UGPU_F32 && xdt == UGPU_F32) {
+        UGPU_CHECK(Ainv32.ptr != nullptr, UGPU_ERR_STATE, "coarse solve: FP32 inverse not prepared");
+        const int vec = (n % 4 == 0) && al(Ainv32.ptr) && al(rhs);
+        k_gemv<float><<<g, kGemvThreads, 0, c.stream>>>(Ainv32.as<float>(), n, static_cast<const float *>(rhs),
+                                                         static_cast<float *>(x), done, vec);
+    } else
         throw Error(UGPU_ERR_UNSUPPORTED, "coarse solve: FP64 or FP32 vectors");
     c.launches++;
     UGPU_LAUNCH_CHECK();

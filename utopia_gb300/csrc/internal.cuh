@@ -286,8 +286,10 @@ struct DenseCholesky {
     int64_t n = 0;
     Buffer L;      // n*n FP64, row-major, lower triangle
     Buffer Ainv;   // n*n FP64 explicit inverse (L^-T L^-1), applied as one GEMV per coarse solve
+    Buffer Ainv32; // its FP32 copy for FP32 vectors (make_fp32_inverse; dropped by factor())
     Buffer tmp_d;  // FP64 rhs/solution staging
     bool factor(const Mat &A);           // returns false if not SPD
+    void make_fp32_inverse();            // FP32 copy of the inverse (coarse solves with FP32 vectors)
     void solve(const void *rhs, int rdt, void *x, int xdt, const int *done = nullptr);
 };
 

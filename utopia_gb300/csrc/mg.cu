@@ -219,6 +219,7 @@ public:
         for (int l = 1; l < L; ++l) setup_smoother(l, sm, rng);
         UGPU_CHECK(coarse_.factor(*levels_[0].A64), UGPU_ERR_NOT_SPD,
                    "coarse operator is not symmetric positive definite");
+        if (vdt_ == UGPU_F32) coarse_.make_fp32_inverse();
         const size_t vs = dtype_size(vdt_);
         for (auto &l : levels_) {
             size_t b = vs * std::max<int64_t>(l.n, 1);

@@ -1048,7 +1048,12 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
                       (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0) {
             if (staged_launch<V, EPI, XM>(ctx, A, a)) return;
         }
-        sell_launch<V, T, R, EPI, XM, DOT>(ctx, A, a);
+        // transfer-like operators (not all slices diagonal) with fewer slices than resident
+        // warps: in the register kernel one lane per row would serialize each long row's
+        // gathers, so the CSR kernel (several lanes per row) runs them
+        const bool few = A.sell->ndiag_slices < A.sell->nslices && A.sell->nslices < int64_t(ctx.sms) * kSpmvWarps;
+        if (few) csr_launch<V, T, EPI, XM, DOT>(ctx, A, a);
+        else sell_launch<V, T, R, EPI, XM, DOT>(ctx, A, a);
     }
 }
 
