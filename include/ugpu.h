@@ -167,11 +167,12 @@ UGPU_API int ugpu_mat_set_format(ugpu_mat *A, int format);
 /* sliced-ELL statistics: slices, stored slots (incl. padding), diagonal-keyed slices */
 UGPU_API int ugpu_mat_sell_info(const ugpu_mat *A, int64_t *nslices, int64_t *nstored, int64_t *ndiag_slices,
                                 int *rows_per_slice);
-/* sliced-ELL row layout: *interleaved = 1 when lane l of a slice's warp owns rows l + 32 r (FP32 / BF16
- * operators whose slices are all diagonal; their products run through the shared-memory staged kernel
- * when the vectors are 16-byte aligned), 0 when it owns R consecutive rows.  No counterpart in the
- * reference (a layout query of this backend). */
-UGPU_API int ugpu_mat_sell_layout(const ugpu_mat *A, int *interleaved);
+/* sliced-ELL layout: *interleaved = 1 when lane l of a slice's warp owns rows l + 32 r (FP32 / BF16
+ * operators whose slices are all keyed; their products run through the shared-memory staged kernel
+ * when the vectors are 16-byte aligned), 0 when it owns R consecutive rows; *anchored_slices = slices
+ * keyed by col - (first column of the row) (transfer operators).  Either pointer may be NULL.  No
+ * counterpart in the reference (a layout query of this backend). */
+UGPU_API int ugpu_mat_sell_layout(const ugpu_mat *A, int *interleaved, int64_t *anchored_slices);
 /* diag(A) (MatGetDiagonal, utopia/backend/petsc/utopia_petsc_Matrix.cpp:756) */
 UGPU_API int ugpu_diag(const ugpu_mat *A, ugpu_vec *d);
 /* explicit transpose (BLAS3Matrix::transpose, utopia_BLAS_Operands.hpp:135-171; used by IPRTransfer

@@ -107,28 +107,46 @@ def test_spmv_unaligned_wrapped_input(ctx, oracle):
     np.testing.assert_allclose(vy.numpy(), oracle.Matrix(A).matvec(x), rtol=1e-13, atol=1e-13)
 
 
+def torch_sms():
+    import torch
+
+    return torch.cuda.get_device_properties(0).multi_processor_count
+
+
 @pytest.mark.parametrize("dtype", [U.F32, U.BF16])
 def test_staged_kernel_matches_register_kernel(ctx, dtype):
-    """FP32 / BF16 operators whose slices are all diagonal get the lane-interleaved layout and
-    run through the shared-memory staged kernel when every vector is 16-byte aligned; a vector
-    4 bytes into its allocation sends the same call to the register kernel.  Both sum each row
-    over the same slots in the same order, so the product, residual, add and Jacobi forms agree
-    bit for bit, on the 7-point fine operator (24^3) and its 27-point Galerkin coarse operator."""
+    """FP32 / BF16 operators whose slices are all keyed (diagonal: col - row; anchored:
+    col - first column of the row) get the lane-interleaved layout and run through the
+    shared-memory staged kernel when every vector is 16-byte aligned; a vector 4 bytes into
+    its allocation sends the same call to the register kernel.  Both sum each row over the
+    same slots in the same order, so the product, residual, add and Jacobi forms agree bit
+    for bit: on the 7-point fine operator (24^3), its 27-point Galerkin coarse operator, the
+    trilinear interpolation P (anchored, x windows staged) and R = P^T (anchored, x gathered
+    through the caches).  The transfers are taken at 108^3 -> 54^3 so that both have more
+    slices than 8 per SM: smaller transfer operators go to the CSR kernel instead of the
+    register kernel, which sums in another order."""
     A = P.lognormal_diffusion_3d(24, 5)[0]
     M64 = U.SparseMatrix(ctx, A)
-    Pm = U.SparseMatrix(ctx, P.interpolation_3d(24))
+    P24 = U.SparseMatrix(ctx, P.interpolation_3d(24))
+    Pcsr = P.interpolation_3d(108)
+    Pm = U.SparseMatrix(ctx, Pcsr)
+    Rsp = Pcsr.to_scipy().T.tocsr()
+    Rsp.sort_indices()
+    Rm = U.SparseMatrix(ctx, P.CSR.from_scipy(Rsp))
+    assert Rm.sell_info()["nslices"] > 8 * torch_sms()
     rng = np.random.default_rng(11)
-    for M in (M64, M64.ptap(Pm)):
+    for M, square in ((M64, True), (M64.ptap(P24), True), (Pm, False), (Rm, False)):
         Mx = M.cast(dtype)
         assert Mx.sell_interleaved()
-        n = M.nrows
-        x, b, v = (rng.standard_normal(n).astype(np.float32) for _ in range(3))
+        n, m = M.nrows, M.ncols
+        x = rng.standard_normal(m).astype(np.float32)
+        b, v = (rng.standard_normal(n).astype(np.float32) for _ in range(2))
 
         def vec(a, aligned):
             if aligned:
                 return U.Vector(ctx, a, dtype=U.F32), None
             big = U.Vector(ctx, np.concatenate([[np.float32(3)], a]).astype(np.float32), dtype=U.F32)
-            return U.Vector.wrap_device(ctx, big.device_ptr + 4, n, U.F32), big
+            return U.Vector.wrap_device(ctx, big.device_ptr + 4, a.size, U.F32), big
 
         out = {}
         for aligned in (True, False):
@@ -136,19 +154,34 @@ def test_staged_kernel_matches_register_kernel(ctx, dtype):
             vb, vv = U.Vector(ctx, b, dtype=U.F32), U.Vector(ctx, v, dtype=U.F32)
             ys = [U.Vector(ctx, n=n, dtype=U.F32) for _ in range(4)]
             Mx.apply(vx, ys[0])
-            Mx.residual(vb, vx, ys[1])
             Mx.apply_add(vx, vv, ys[2])
-            Mx.jacobi_sweep(vb, vx, 0.8, ys[3])
+            if square:
+                Mx.residual(vb, vx, ys[1])
+                Mx.jacobi_sweep(vb, vx, 0.8, ys[3])
             out[aligned] = [y.numpy() for y in ys]
         for a, u in zip(out[True], out[False]):
             assert np.array_equal(a.view(np.uint32), u.view(np.uint32))
-        vals = np.asarray(Mx.csr()[2], np.float64)
-        r, c, _ = M.csr()
-        ref = P.CSR(n, n, r, c, vals).matvec(x.astype(np.float64))
-        bound = 1e-6 * (np.abs(P.CSR(n, n, r, c, vals).to_scipy()) @ np.abs(x.astype(np.float64)))
+        r, c, vals = Mx.csr()
+        ref = P.CSR(n, m, r, c, vals).matvec(x.astype(np.float64))
+        bound = 1e-6 * (np.abs(P.CSR(n, m, r, c, vals).to_scipy()) @ np.abs(x.astype(np.float64)))
         assert np.all(np.abs(out[True][0] - ref) <= 4 * bound + 1e-30)
-    # the transfers keep explicit-column slices and the consecutive-rows layout
-    assert not Pm.cast(dtype).sell_interleaved()
+
+
+def test_transfer_operators_use_anchored_slices(ctx):
+    """Rows of the trilinear interpolation and of its transpose share one shape relative to
+    their first column: every slice is keyed by col - anchor (no column indices stored), and
+    the FP64 products through those slices match scipy."""
+    Psp = P.interpolation_3d(24).to_scipy()
+    for M in (Psp, Psp.T.tocsr()):
+        M.sort_indices()
+        C = P.CSR.from_scipy(M)
+        Md = U.SparseMatrix(ctx, C)
+        info = Md.sell_info()
+        assert info["ndiag_slices"] == 0 and Md.sell_anchored_slices() == info["nslices"]
+        x = np.random.default_rng(5).standard_normal(C.ncols)
+        y = U.Vector(ctx, n=C.nrows)
+        Md.apply(U.Vector(ctx, x), y)
+        np.testing.assert_allclose(y.numpy(), M @ x, rtol=1e-14, atol=1e-14)
 
 
 def test_stencil_operators_use_diagonal_slices(ctx):

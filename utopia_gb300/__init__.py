@@ -218,8 +218,14 @@ class SparseMatrix:
     def sell_interleaved(self) -> bool:
         """True when the sliced-ELL rows are lane-interleaved (the staged kernel's layout)."""
         v = C.c_int()
-        self.ctx.check(self.ctx.lib.ugpu_mat_sell_layout(self.h, C.byref(v)))
+        self.ctx.check(self.ctx.lib.ugpu_mat_sell_layout(self.h, C.byref(v), None))
         return bool(v.value)
+
+    def sell_anchored_slices(self) -> int:
+        """Slices keyed by col - (first column of the row)."""
+        v = C.c_int64()
+        self.ctx.check(self.ctx.lib.ugpu_mat_sell_layout(self.h, None, C.byref(v)))
+        return v.value
 
     def update_values(self, values):
         v = np.ascontiguousarray(values, dtype=np.float64)

@@ -83,7 +83,7 @@ SIGNATURES = {
     "ugpu_mat_cast": [_vp, _int, _pp],
     "ugpu_mat_set_format": [_vp, _int],
     "ugpu_mat_sell_info": [_vp, C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_i64), C.POINTER(_int)],
-    "ugpu_mat_sell_layout": [_vp, C.POINTER(_int)],
+    "ugpu_mat_sell_layout": [_vp, C.POINTER(_int), C.POINTER(_i64)],
     "ugpu_diag": [_vp, _vp],
     "ugpu_transpose": [_vp, _pp],
     "ugpu_spgemm": [_vp, _vp, _pp],

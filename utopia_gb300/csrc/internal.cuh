@@ -164,11 +164,12 @@ struct Sell {
     int64_t nslices = 0;
     int64_t nstored = 0;   // stored value slots (incl. padding)
     int64_t ndiag_slices = 0;
+    int64_t nanch_slices = 0;  // slices keyed by col - (first column of the row)
     int max_width = 0;
-    Buffer hdr;         // int4[nslices] packed {value offset lo, hi, width, aux} read by the kernels
+    Buffer hdr;         // int4[nslices] packed {value offset lo, hi, width word, aux} read by the kernels
     Buffer slice_ptr;   // int64[nslices+1] value offset of slice (elements)
-    Buffer slice_w;     // int32[nslices]   width (slots); negative: explicit-column slice
-    Buffer slice_aux;   // int64[nslices]   diagonal slices: index into offs; explicit: index into cols
+    Buffer slice_w;     // int32[nslices]   width word: w (diagonal), kAnchoredTag + w (anchored), -w (explicit)
+    Buffer slice_aux;   // int64[nslices]   diagonal slices: index into offs; anchored / explicit: index into cols
     Buffer offs;        // int32 per diagonal slot
     Buffer cols;        // int32 per explicit slot entry
     Buffer vals;        // value storage (dtype of the matrix)

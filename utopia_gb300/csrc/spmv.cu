@@ -60,8 +60,48 @@ __global__ void k_diag(const int32_t *rp, const int32_t *ci, const V *v, int64_t
 // ------------------------------------------------------------------------------------
 constexpr int kAnalyzeThreads = 128;
 
-// per slice: width and kind.  Diagonal slices collect the sorted distinct offsets
-// (col - row) by repeated min-extraction over the slice's entries.
+// Slice kinds, as encoded in the width word of a slice header:
+//   diagonal  0 <= w < kAnchoredTag   entries keyed by col - row (one int32 key per slot)
+//   anchored  w - kAnchoredTag        entries keyed by col - anchor(row), anchor = the row's
+//                                     first column (one key per slot + one anchor per row)
+//   explicit  -w                      one column index per stored entry
+// Anchored keying fits transfer operators: every row of an interpolation (or of its
+// transpose) has the same shape relative to its first column, so a slice needs as many
+// slots as that shape has entries.
+constexpr int kAnchoredTag = 1 << 16;
+
+// Sorted distinct keys of a slice by repeated min-extraction; returns the count, or -1 if
+// more than kMaxDiagSlots (or a key outside int32).  ANCH: key = col - first column.
+template <bool ANCH>
+__device__ int slice_keys(const int32_t *rp, const int32_t *ci, int64_t r0, int64_t r1, int32_t *out,
+                          long long *s_min) {
+    int nd = 0;
+    long long prev = LLONG_MIN;
+    while (true) {
+        if (threadIdx.x == 0) *s_min = LLONG_MAX;
+        __syncthreads();
+        long long m = LLONG_MAX;
+        for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+            const int32_t k0 = rp[r], k1 = rp[r + 1];
+            const long long base = ANCH ? (k1 > k0 ? (long long)ci[k0] : 0ll) : r;
+            for (int32_t k = k0; k < k1; ++k) {
+                long long off = (long long)ci[k] - base;
+                if (off > prev && off < m) m = off;
+            }
+        }
+        atomicMin(s_min, m);
+        __syncthreads();
+        long long mm = *s_min;
+        __syncthreads();
+        if (mm == LLONG_MAX) return nd;
+        if (nd >= kMaxDiagSlots || mm > INT_MAX || mm < INT_MIN) return -1;
+        if (threadIdx.x == 0) out[nd] = int32_t(mm);
+        nd++;
+        prev = mm;
+    }
+}
+
+// per slice: kind and width (the cheapest of the three layouts in bytes)
 __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_analyze(const int32_t *rp, const int32_t *ci, int64_t n,
                                                                    int S, int64_t nslices, int sval,
                                                                    int32_t *width, int32_t *offs_tmp) {
@@ -75,39 +115,20 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_analyze(const int32_t 
         for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) mr = max(mr, rp[r + 1] - rp[r]);
         atomicMax(&s_maxrow, mr);
         __syncthreads();
-        int maxrow = s_maxrow;
+        const int maxrow = s_maxrow;
         __syncthreads();
-        int nd = 0;
-        bool diag_ok = maxrow <= kMaxDiagSlots;
-        long long prev = LLONG_MIN;
-        while (diag_ok) {
-            if (threadIdx.x == 0) s_min = LLONG_MAX;
-            __syncthreads();
-            long long m = LLONG_MAX;
-            for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-                for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
-                    long long off = (long long)ci[k] - r;
-                    if (off > prev && off < m) m = off;
-                }
-            atomicMin(&s_min, m);
-            __syncthreads();
-            long long mm = s_min;
-            __syncthreads();
-            if (mm == LLONG_MAX) break;
-            if (nd >= kMaxDiagSlots || mm > INT_MAX || mm < INT_MIN) {
-                diag_ok = false;
-                break;
-            }
-            if (threadIdx.x == 0) offs_tmp[s * kMaxDiagSlots + nd] = int32_t(mm);
-            nd++;
-            prev = mm;
+        // bytes: diagonal nd*S*sval + 4nd; anchored na*S*sval + 4na + 4S + 8; explicit maxrow*S*(sval+4)
+        const long long expl = (long long)maxrow * S * (sval + 4);
+        int32_t *keys = offs_tmp + s * kMaxDiagSlots;
+        const int nd = maxrow <= kMaxDiagSlots ? slice_keys<false>(rp, ci, r0, r1, keys, &s_min) : -1;
+        int kind_w = -maxrow;
+        if (nd >= 0 && (long long)nd * S * sval + 4ll * nd <= expl) {
+            kind_w = nd;
+        } else if (maxrow <= kMaxDiagSlots) {
+            const int na = slice_keys<true>(rp, ci, r0, r1, keys, &s_min);
+            if (na >= 0 && (long long)na * S * sval + 4ll * na + 4ll * S + 8 < expl) kind_w = kAnchoredTag + na;
         }
-        // bytes: diagonal = nd*S*sval (+4*nd), explicit = maxrow*S*(sval+4)
-        if (diag_ok && (long long)nd * S * sval + 4ll * nd <= (long long)maxrow * S * (sval + 4)) {
-            if (threadIdx.x == 0) width[s] = nd;
-        } else {
-            if (threadIdx.x == 0) width[s] = -maxrow;
-        }
+        if (threadIdx.x == 0) width[s] = kind_w;
         __syncthreads();
     }
 }
@@ -125,11 +146,12 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp
                                                                 const int64_t *aux, const int32_t *offs_tmp,
                                                                 int32_t *offs, int32_t *cols, V *vals, bool il) {
     __shared__ int32_t s_off[kMaxDiagSlots];
+    __shared__ int s_amin, s_amax;
     for (int64_t s = blockIdx.x; s < nslices; s += gridDim.x) {
         int w = width[s];
         int64_t base = sptr[s];
         int64_t r0 = s * S;
-        if (w >= 0) {
+        if (w >= 0 && w < kAnchoredTag) {
             for (int k = threadIdx.x; k < w; k += blockDim.x) {
                 s_off[k] = offs_tmp[s * kMaxDiagSlots + k];
                 offs[aux[s] + k] = s_off[k];
@@ -145,6 +167,50 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_fill(const int32_t *rp
                     int32_t off = int32_t((long long)ci[k] - r);
                     while (slot < w && s_off[slot] < off) ++slot;
                     if (slot < w && s_off[slot] == off) vals[base + int64_t(slot) * S + sell_pos(rl, S, il)] = cv[k];
+                }
+            }
+            __syncthreads();
+        } else if (w >= kAnchoredTag) {
+            // anchors at cols[cb, cb + S) in slot-position order, keys at cols[cb + S, cb + S + wa),
+            // then the slice's smallest and largest anchor (the x range its gathers can touch)
+            const int wa = w - kAnchoredTag;
+            const int64_t cb = aux[s];
+            for (int k = threadIdx.x; k < wa; k += blockDim.x) {
+                s_off[k] = offs_tmp[s * kMaxDiagSlots + k];
+                cols[cb + S + k] = s_off[k];
+            }
+            if (threadIdx.x == 0) {
+                s_amin = INT_MAX;
+                s_amax = INT_MIN;
+            }
+            __syncthreads();
+            for (int rl = threadIdx.x; rl < S; rl += blockDim.x) {
+                const int64_t r = r0 + rl;
+                if (r < n && rp[r + 1] > rp[r]) {
+                    atomicMin(&s_amin, ci[rp[r]]);
+                    atomicMax(&s_amax, ci[rp[r]]);
+                }
+            }
+            for (int64_t e = threadIdx.x; e < int64_t(wa) * S; e += blockDim.x) vals[base + e] = cvt<V>(0.0);
+            __syncthreads();
+            const int amin = s_amin == INT_MAX ? 0 : s_amin;
+            const int amax = s_amin == INT_MAX ? 0 : s_amax;
+            if (threadIdx.x == 0) {
+                cols[cb + S + wa] = amin;
+                cols[cb + S + wa + 1] = amax;
+            }
+            for (int rl = threadIdx.x; rl < S; rl += blockDim.x) {
+                const int64_t r = r0 + rl;
+                const bool has = r < n && rp[r + 1] > rp[r];
+                const int32_t a = has ? ci[rp[r]] : amin;  // empty and padding rows: any anchor in range
+                const int p = sell_pos(rl, S, il);
+                cols[cb + p] = a;
+                if (!has) continue;
+                int slot = 0;
+                for (int32_t k = rp[r]; k < rp[r + 1]; ++k) {
+                    const int32_t key = ci[k] - a;
+                    while (slot < wa && s_off[slot] < key) ++slot;
+                    if (slot < wa && s_off[slot] == key) vals[base + int64_t(slot) * S + p] = cv[k];
                 }
             }
             __syncthreads();
@@ -389,9 +455,12 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
         return h;
     };
     auto load_offs = [&](const SliceHdr &h, int64_t s, int32_t &lo, int32_t &hi) {
-        const bool diag = s < ns && h.w >= 0;
-        lo = (diag && lane < h.w) ? __ldg(m.offs + h.aux + lane) : 0;
-        hi = (diag && lane + 32 < h.w) ? __ldg(m.offs + h.aux + 32 + lane) : 0;
+        const bool keyed = s < ns && h.w >= 0;  // diagonal or anchored
+        const bool anch = h.w >= kAnchoredTag;
+        const int wk = anch ? h.w - kAnchoredTag : h.w;
+        const int32_t *kp = anch ? m.cols + h.aux + S : m.offs + h.aux;
+        lo = (keyed && lane < wk) ? __ldg(kp + lane) : 0;
+        hi = (keyed && lane + 32 < wk) ? __ldg(kp + 32 + lane) : 0;
     };
     SliceHdr h_cur = load_hdr(warp0), h_nxt = load_hdr(warp0 + nwarps);
     int32_t o_lo, o_hi;
@@ -415,18 +484,28 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = T(0);
         if (w >= 0) {
-            // the slice's offsets were read once (coalesced) and are broadcast by shuffle, so
-            // the gathers of a slot depend on no load but the value stream's
-            const int r0i = int(row0);  // nrows, ncols < 2^31
+            // the slice's keys were read once (coalesced) and are broadcast by shuffle, so
+            // the gathers of a slot depend on no load but the value stream's; row r gathers
+            // at gb[r] + key: gb = the row (diagonal) or the row's first column (anchored,
+            // stored at the row's slot position lane R + r)
+            const bool anch = w >= kAnchoredTag;
+            const int wk = anch ? w - kAnchoredTag : w;
             const int cmax = int(m.ncols) - 1;
+            int gb[R];
+            if (anch) {
+                load_cols<R>(m.cols + aux + lane * R, gb);
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) gb[r] = int(row0) + r * rs;  // nrows, ncols < 2^31
+            }
             UGPU_PRAGMA_UNROLL(UGPU_SELL_UNROLL)
-            for (int k = 0; k < w; ++k) {
+            for (int k = 0; k < wk; ++k) {
                 const int32_t off = __shfl_sync(0xffffffffu, k < 32 ? off_lo : off_hi, k & 31);
                 LV v[R];
                 VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    int c = r0i + r * rs + off;
+                    int c = gb[r] + off;
                     c = c < 0 ? 0 : (c > cmax ? cmax : c);
                     acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
                 }
@@ -531,6 +610,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
 constexpr int kStagedWarps = 4;      // warps per CTA
 constexpr int kStagedMaxStages = 4;
 constexpr int kStagedGap = 16;       // offsets at most this far apart share one x window
+constexpr int kStagedXBudget = 2048; // most x-window floats per slice that are staged
 constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[32], xb[32]
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
 
@@ -539,8 +619,9 @@ struct StagedCfg {
     uint32_t warp_bytes;   // shared bytes per warp (barriers + descriptors + stages)
     uint32_t hdr_bytes;    // barriers + descriptors
     uint32_t stage_bytes;
-    uint32_t o_x, o_x2, o_xr, o_v, o_w;  // byte offsets inside a stage
+    uint32_t o_x, o_x2, o_xr, o_v, o_w, o_a;  // byte offsets inside a stage (o_a: anchors)
     int xcap;              // floats of one window region
+    int xglobal;           // x is gathered from global memory (windows too wide to stage)
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -592,25 +673,32 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // Floats of x that the staged kernel copies for slice s (offsets off[0..w) ascending): one
 // window per group of offsets at most kStagedGap apart, each covering the group's clamped
 // gathers rounded out to 16 bytes.  Same arithmetic as the kernel's issue step.
-__device__ __forceinline__ int staged_window_floats(const int32_t *off, int w, int r0, int S, int cmax) {
+__device__ __forceinline__ int staged_window_floats(const int32_t *off, int w, int gmin, int gmax, int cmax) {
     int total = 0;
     for (int a = 0; a < w;) {
         int b = a;
         while (b + 1 < w && off[b + 1] - off[b] <= kStagedGap) ++b;
-        const int lo = min(max(r0 + off[a], 0), cmax);
-        const int hi = min(max(r0 + S - 1 + off[b], 0), cmax);
+        const int lo = min(max(gmin + off[a], 0), cmax);
+        const int hi = min(max(gmax + off[b], 0), cmax);
         total += ((hi + 4) & ~3) - (lo & ~3);
         a = b + 1;
     }
     return total;
 }
 
-__global__ void k_sell_window_max(const int4 *hdr, const int32_t *offs, int64_t ns, int S, int64_t ncols,
-                                  int *out) {
+__global__ void k_sell_window_max(const int4 *hdr, const int32_t *offs, const int32_t *cols, int64_t ns, int S,
+                                  int64_t ncols, int *out) {
     int best = 0;
     for (int64_t s = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; s < ns; s += int64_t(gridDim.x) * blockDim.x) {
         const int4 q = hdr[s];
-        if (q.z > 0) best = max(best, staged_window_floats(offs + q.w, q.z, int(s * S), S, int(ncols) - 1));
+        const int r0 = int(s * S);
+        if (q.z >= kAnchoredTag) {
+            const int w = q.z - kAnchoredTag;
+            const int32_t *kp = cols + q.w + S;
+            if (w > 0) best = max(best, staged_window_floats(kp, w, kp[w], kp[w + 1], int(ncols) - 1));
+        } else if (q.z > 0) {
+            best = max(best, staged_window_floats(offs + q.w, q.z, r0, r0 + S - 1, int(ncols) - 1));
+        }
     }
     best = max(best, __reduce_max_sync(0xffffffffu, best));
     if ((threadIdx.x & 31) == 0) atomicMax(out, best);
@@ -629,6 +717,12 @@ __device__ __forceinline__ void smem_vals4<__nv_bfloat16>(const __nv_bfloat16 *p
     const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.x));
     const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.y));
     v[0] = fa.x; v[1] = fa.y; v[2] = fb.x; v[3] = fb.y;
+}
+
+// a lane's four anchors in a staged slice: rows l + 32 r sit at slot positions 4 l + r
+__device__ __forceinline__ void stage_anchors(const int *sa, int lane, int (&a)[4]) {
+    const int4 q = *reinterpret_cast<const int4 *>(sa + 4 * lane);
+    a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
 }
 
 template <int EPI, int XM>
@@ -670,15 +764,24 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
     // on the other inside an iteration.
     struct Meta {
         int64_t base;
-        int w;
-        int off;
+        int w;      // slots
+        int off;    // this lane's key
+        int aux;
+        int anch;   // anchored slice
+        int amin, amax;
     };
     auto load_hdr = [&](int64_t s) -> int4 {
         return s < ns ? __ldg(reinterpret_cast<const int4 *>(m.hdr) + s) : make_int4(0, 0, 0, 0);
     };
     auto meta_of = [&](const int4 &q) -> Meta {
-        Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), q.z, 0};
-        if (lane < mt.w) mt.off = __ldg(m.offs + q.w + lane);
+        const int anch = q.z >= kAnchoredTag;
+        Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), anch ? q.z - kAnchoredTag : q.z, 0, q.w, anch, 0, 0};
+        const int32_t *kp = anch ? m.cols + q.w + S : m.offs + q.w;
+        if (lane < mt.w) mt.off = __ldg(kp + lane);
+        if (anch) {
+            mt.amin = __ldg(kp + mt.w);
+            mt.amax = __ldg(kp + mt.w + 1);
+        }
         return mt;
     };
 
@@ -691,18 +794,22 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const int rows = int(min(int64_t(S), m.nrows - int64_t(r0)));
         const int offk = mt.off;
         const int prev = __shfl_up_sync(full, offk, 1);
-        const bool start = lane < w && (lane == 0 || offk - prev > kStagedGap);
+        const bool start = !cfg.xglobal && lane < w && (lane == 0 || offk - prev > kStagedGap);
         const unsigned gmask = __ballot_sync(full, start);
         // my group's last slot: one before the next group start, or w - 1
         const unsigned after = lane == 31 ? 0u : (gmask & ~((2u << lane) - 1u));
         const int last = after ? (__ffs(after) - 2) : (w - 1);
         const int offl = __shfl_sync(full, offk, last & 31);
+        // gathers of row i at slot k: gbase(i) + key_k, gbase = the row (diagonal slice) or its
+        // anchor (anchored slice), gbase in [gmin, gmax]
+        const int gmin = mt.anch ? mt.amin : r0;
+        const int gmax = mt.anch ? mt.amax : r0 + S - 1;
         int len = 0, lo_r = 0;
         if (start) {
             // clamped columns of the group's gathers lie in [lo, hi]; the window covers it
             // rounded out to 16 bytes (ncols is a multiple of 4, so it stays inside x)
-            const int lo = min(max(r0 + offk, 0), cmax);
-            const int hi = min(max(r0 + S - 1 + offl, 0), cmax);
+            const int lo = min(max(gmin + offk, 0), cmax);
+            const int hi = min(max(gmax + offl, 0), cmax);
             lo_r = lo & ~3;
             len = ((hi + 4) & ~3) - lo_r;
         }
@@ -718,18 +825,19 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const int first = upto ? 31 - __clz(upto) : 0;
         const int xb = __shfl_sync(full, woff - lo_r, first);
         // the stage is free: every lane's reads of its previous slice are done
-        // interior slice: no gather of any row leaves [0, ncols), so slot k's reads for lane l
-        // and row 32 r + l sit at (r0 + off_k + xb_k) + l + 32 r without clamping
+        // interior slice: no gather of any row leaves [0, ncols), so slot k's read for row i
+        // sits at gbase(i) + (key_k + xb_k) without clamping (diagonal: (r0 + key_k + xb_k)
+        // + l + 32 r for lane l, row 32 r + l)
         const int off_lo = __shfl_sync(full, offk, 0);
         const int off_hi = __shfl_sync(full, offk, (w - 1) & 31);
-        const bool interior = w > 0 && r0 + off_lo >= 0 && r0 + S - 1 + off_hi <= cmax;
+        const bool interior = w > 0 && gmin + off_lo >= 0 && gmax + off_hi <= cmax;
         if (lane < w) {
             d[2 + lane] = offk;
-            d[34 + lane] = interior ? r0 + offk + xb : xb;
+            d[34 + lane] = interior ? (mt.anch ? 0 : r0) + offk + xb : xb;
         }
         if (lane == 0) {
             d[0] = w;
-            d[1] = interior ? 1 : 0;
+            d[1] = (interior ? 1 : 0) | (mt.anch ? 2 : 0);
         }
         const uint32_t vbytes = uint32_t(w) * S * uint32_t(sizeof(V));
         const uint32_t rbytes = uint32_t(rows) * 4u;
@@ -737,6 +845,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (Nd::xr) total += rbytes;
         if (Nd::v) total += rbytes;
         if (Nd::w) total += rbytes;
+        if (mt.anch) total += S * 4u;
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive_expect_tx(&bar[st], total);
@@ -753,6 +862,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (Nd::xr && lane == 1) bulk_g2s(sg + cfg.o_xr, e.x + r0, rbytes, &bar[st]);
         if (Nd::v && lane == 2) bulk_g2s(sg + cfg.o_v, e.v + r0, rbytes, &bar[st]);
         if (Nd::w && lane == 3) bulk_g2s(sg + cfg.o_w, e.w + r0, rbytes, &bar[st]);
+        if (mt.anch && lane == 4) bulk_g2s(sg + cfg.o_a, m.cols + mt.aux, S * 4u, &bar[st]);
     };
 
     // the product and epilogue of slice s from stage st
@@ -767,7 +877,53 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         float acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = 0.f;
-        if (d[1]) {
+        const int flags = d[1];
+        const int *sa = reinterpret_cast<const int *>(sg + cfg.o_a);
+        if (cfg.xglobal) {
+            // values (and anchors) staged, x gathered through L1 / L2
+            int gb[R];
+            if (flags & 2) {
+                stage_anchors(sa, lane, gb);
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) gb[r] = r0 + lane + 32 * r;
+            }
+            const bool inner = flags & 1;
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const int off = d[2 + k];
+                float v[R];
+                smem_vals4<V>(sv + k * S + lane * R, v);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    int c = gb[r] + off;
+                    if (!inner) c = min(max(c, 0), cmax);
+                    float xv;
+                    if constexpr (XM == 2) xv = __ldg(e.w + c) * __ldg(e.v + c);
+                    else xv = __ldg(e.x + c);
+                    acc[r] = fmaf(v[r], xv, acc[r]);
+                }
+            }
+        } else if (flags == 3) {
+            // anchored, interior
+            int a[R];
+            stage_anchors(sa, lane, a);
+#pragma unroll 4
+            for (int k = 0; k < w; ++k) {
+                const int dk = d[34 + k];
+                float v[R];
+                smem_vals4<V>(sv + k * S + lane * R, v);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    const int c = a[r] + dk;
+                    float xv;
+                    if constexpr (XM == 2) xv = sx[c] * sx2[c];
+                    else xv = sx[c];
+                    acc[r] = fmaf(v[r], xv, acc[r]);
+                }
+            }
+        } else if (flags == 1) {
+            // diagonal, interior
             const float *xl = sx + lane;
 #pragma unroll 4
             for (int k = 0; k < w; ++k) {
@@ -783,6 +939,14 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 }
             }
         } else {
+            // boundary slice: clamp every gather
+            int gb[R];
+            if (flags & 2) {
+                stage_anchors(sa, lane, gb);
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) gb[r] = r0 + lane + 32 * r;
+            }
 #pragma unroll 4
             for (int k = 0; k < w; ++k) {
                 const int off = d[2 + k];
@@ -791,7 +955,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int c = min(max(r0 + lane + 32 * r + off, 0), cmax) + xb;
+                    const int c = min(max(gb[r] + off, 0), cmax) + xb;
                     float xv;
                     if constexpr (XM == 2) xv = sx[c] * sx2[c];
                     else xv = sx[c];
@@ -965,7 +1129,10 @@ bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     constexpr int S = 128;
     StagedCfg c{};
     const int wcap = std::max(1, s.max_width);
-    c.xcap = std::max(4, s.xwin_max);
+    // x windows wider than the budget (restrictions: anchors two fine points apart under nine
+    // key groups) are not staged; such operators gather x through the caches
+    c.xglobal = s.xwin_max > kStagedXBudget ? 1 : 0;
+    c.xcap = c.xglobal ? 0 : std::max(4, s.xwin_max);
     const uint32_t vals_b = round128(uint32_t(wcap) * S * uint32_t(sizeof(V)));
     const uint32_t x_b = round128(uint32_t(c.xcap) * 4u);
     uint32_t o = vals_b;
@@ -979,6 +1146,8 @@ bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (Nd::v) o += S * 4;
     c.o_w = o;
     if (Nd::w) o += S * 4;
+    c.o_a = o;
+    if (s.nanch_slices) o += S * 4;
     c.stage_bytes = round128(o);
     c.hdr_bytes = round128(8u * kStagedMaxStages + 4u * kStagedDesc * kStagedMaxStages);
     auto kern = k_sell_staged<V, EPI, XM>;
@@ -1125,14 +1294,19 @@ void build_sell(Mat &A) {
     if (ns) UGPU_CUDA(cudaMemcpyAsync(hw.data(), width.ptr, sizeof(int32_t) * ns, cudaMemcpyDeviceToHost, ctx.stream));
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
     std::vector<int64_t> sptr(ns + 1, 0), aux(ns, 0);
-    int64_t noffs = 0, ncol = 0, ndiag = 0;
+    int64_t noffs = 0, ncol = 0, ndiag = 0, nanch = 0;
     int maxw = 0;
     for (int64_t i = 0; i < ns; ++i) {
-        int w = hw[i];
-        int wd = w >= 0 ? w : -w;
+        const int w = hw[i];
+        const bool anch = w >= kAnchoredTag;
+        const int wd = anch ? w - kAnchoredTag : (w >= 0 ? w : -w);
         maxw = std::max(maxw, wd);
         sptr[i + 1] = sptr[i] + int64_t(wd) * S;
-        if (w >= 0) {
+        if (anch) {
+            aux[i] = ncol;  // anchors, keys, smallest and largest anchor; 16-byte aligned
+            ncol += (int64_t(S) + wd + 2 + 3) & ~int64_t(3);
+            nanch++;
+        } else if (w >= 0) {
             aux[i] = noffs;
             noffs += w;
             ndiag++;
@@ -1143,7 +1317,8 @@ void build_sell(Mat &A) {
     }
     s->nstored = sptr[ns];
     s->ndiag_slices = ndiag;
-    s->interleaved = A.vdtype != UGPU_F64 && ndiag == ns && maxw <= kStagedMaxWidth && A.nrows % 4 == 0 &&
+    s->nanch_slices = nanch;
+    s->interleaved = A.vdtype != UGPU_F64 && ndiag + nanch == ns && maxw <= kStagedMaxWidth && A.nrows % 4 == 0 &&
                      A.ncols % 4 == 0;
     s->max_width = maxw;
     s->noffs = noffs;
@@ -1186,8 +1361,9 @@ void build_sell(Mat &A) {
     if (ns && s->interleaved) {
         wmax.alloc(sizeof(int));
         UGPU_CUDA(cudaMemsetAsync(wmax.ptr, 0, sizeof(int), ctx.stream));
-        k_sell_window_max<<<gA, kAnalyzeThreads, 0, ctx.stream>>>(s->hdr.as<int4>(), s->offs.as<int32_t>(), ns, S,
-                                                                  A.ncols, wmax.as<int>());
+        k_sell_window_max<<<gA, kAnalyzeThreads, 0, ctx.stream>>>(s->hdr.as<int4>(), s->offs.as<int32_t>(),
+                                                                  s->cols.as<int32_t>(), ns, S, A.ncols,
+                                                                  wmax.as<int>());
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
         UGPU_CUDA(cudaMemcpyAsync(&h_wmax, wmax.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
@@ -1473,12 +1649,12 @@ int ugpu_mat_sell_info(const ugpu_mat *A, int64_t *nslices, int64_t *nstored, in
     UGPU_ABI_END(nullptr)
 }
 
-int ugpu_mat_sell_layout(const ugpu_mat *A, int *interleaved) {
+int ugpu_mat_sell_layout(const ugpu_mat *A, int *interleaved, int64_t *anchored_slices) {
     UGPU_ABI_BEGIN
     UGPU_REQUIRE(A);
-    UGPU_REQUIRE(interleaved);
     UGPU_CHECK(A->impl.sell != nullptr, UGPU_ERR_STATE, "matrix has no sliced-ELL layout");
-    *interleaved = A->impl.sell->interleaved ? 1 : 0;
+    if (interleaved) *interleaved = A->impl.sell->interleaved ? 1 : 0;
+    if (anchored_slices) *anchored_slices = A->impl.sell->nanch_slices;
     UGPU_ABI_END(nullptr)
 }
 
