@@ -121,8 +121,9 @@ def test_staged_kernel_matches_register_kernel(ctx, dtype):
     its allocation sends the same call to the register kernel.  Both sum each row over the
     same slots in the same order, so the product, residual, add and Jacobi forms agree bit
     for bit: on the 7-point fine operator (24^3), its 27-point Galerkin coarse operator, the
-    trilinear interpolation P (anchored, x windows staged) and R = P^T (anchored, x gathered
-    through the caches).  The transfers are taken at 108^3 -> 54^3 so that both have more
+    trilinear interpolation P (anchored, x windows staged) and R = P^T (anchored; its x
+    windows are too wide to stage, so both calls take the register kernel).  The transfers are
+    taken at 108^3 -> 54^3 so that both have more
     slices than 8 per SM: smaller transfer operators go to the CSR kernel instead of the
     register kernel, which sums in another order."""
     A = P.lognormal_diffusion_3d(24, 5)[0]

@@ -611,6 +611,7 @@ constexpr int kStagedWarps = 4;      // warps per CTA
 constexpr int kStagedMaxStages = 4;
 constexpr int kStagedGap = 16;       // offsets at most this far apart share one x window
 constexpr int kStagedXBudget = 2048; // most x-window floats per slice that are staged
+constexpr bool kStagedGlobalX = false;  // run operators with wider windows here (x through the caches)
 constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[32], xb[32]
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
 
@@ -1130,8 +1131,11 @@ bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     StagedCfg c{};
     const int wcap = std::max(1, s.max_width);
     // x windows wider than the budget (restrictions: anchors two fine points apart under nine
-    // key groups) are not staged; such operators gather x through the caches
+    // key groups) are not staged.  Gathering their x through the caches from this kernel
+    // (xglobal) was measured slower than the register kernel, whose 64 warps per SM hide the
+    // gather latency better, so such operators go there.
     c.xglobal = s.xwin_max > kStagedXBudget ? 1 : 0;
+    if (c.xglobal && !kStagedGlobalX) return false;
     c.xcap = c.xglobal ? 0 : std::max(4, s.xwin_max);
     const uint32_t vals_b = round128(uint32_t(wcap) * S * uint32_t(sizeof(V)));
     const uint32_t x_b = round128(uint32_t(c.xcap) * 4u);
