@@ -348,7 +348,7 @@ def main():
     t16 = time_kernel(lambda: A16.apply(x16, y16))
     s16 = A16.sell_info()
     b16 = s16["nstored"] * 2 + 2 * n * 4
-    roofline_bf16 = {"kernel": "k_sell_spmv<bf16,float,4,EPI_STORE>", "us": t16 * 1e6,
+    roofline_bf16 = {"kernel": "k_sell_staged<bf16,EPI_STORE> (shared-memory staged sliced ELL)", "us": t16 * 1e6,
                      "format_bytes": b16, "achieved": b16 / t16 / 1e9, "peak": hbm, "unit": "GB/s",
                      "frac": b16 / t16 / 1e9 / hbm, "csr_model_gbs": (nnz * 6 + 4 * (n + 1) + 2 * n * 4) / t16 / 1e9}
     del A16

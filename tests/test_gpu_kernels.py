@@ -63,6 +63,34 @@ def test_vector_roundtrip_and_blas1(ctx):
     np.testing.assert_array_equal(v32.numpy(), a.astype(np.float32))
 
 
+def test_fp64_fp32_conversions_match_ieee(ctx):
+    """The device converts FP64 <-> FP32 with integer bit operations (round to nearest even);
+    results equal numpy's IEEE conversions bit for bit, on ties, the overflow boundary, the
+    smallest normals, subnormals, signed zeros, infinities, NaNs and random magnitudes."""
+    rng = np.random.default_rng(7)
+    one = 1.0
+    edge = [0.0, -0.0, one, -one, one + 2.0**-24, one + 3 * 2.0**-24, one + 2.0**-24 + 2.0**-52,
+            np.float32(3.4028235e38).astype(np.float64), 3.4028235677973366e38, 3.4028235677973362e38, 1e39,
+            -1e39, 2.0**-126, 2.0**-126 * (1 - 2.0**-25), 2.0**-127, 1e-45, 1e-300, np.inf, -np.inf,
+            np.nan, 0.1, 1 / 3]
+    rnd = rng.standard_normal(20000) * 10.0 ** rng.integers(-40, 40, 20000)
+    d = np.array(edge + list(rnd), dtype=np.float64)
+    v64, v32 = U.Vector(ctx, d), U.Vector(ctx, n=d.size, dtype=U.F32)
+    v64.copy_to(v32)
+    with np.errstate(over="ignore"):
+        ref = d.astype(np.float32)
+    got = v32.numpy()
+    ok = (got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))
+    assert ok.all(), d[~ok][:5]
+    f = np.concatenate([ref, np.array([1e-40, -1e-44, 1.17549435e-38], np.float32),
+                        (rng.standard_normal(20000) * 10.0 ** rng.integers(-44, 38, 20000)).astype(np.float32)])
+    w32, w64 = U.Vector(ctx, f, dtype=U.F32), U.Vector(ctx, n=f.size)
+    w32.copy_to(w64)
+    got64, ref64 = w64.numpy(), f.astype(np.float64)
+    ok = (got64.view(np.uint64) == ref64.view(np.uint64)) | (np.isnan(got64) & np.isnan(ref64))
+    assert ok.all(), f[~ok][:5]
+
+
 def test_empty_vector_dot(ctx):
     v = U.Vector(ctx, n=0)
     assert v.dot(v) == 0.0

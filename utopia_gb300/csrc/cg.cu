@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
             z[i] = zi;
             a1 = fma(zi, ri, a1);
         }
-        if constexpr (R32) r32[i] = float(ri);
+        if constexpr (R32) r32[i] = d2f_bits(ri);
     };
     const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     const int64_t nth = int64_t(gridDim.x) * blockDim.x;
@@ -121,7 +121,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
                 a1 = fma(z0, r0, a1);
                 a1 = fma(z1, r1, a1);
             }
-            if constexpr (R32) reinterpret_cast<float2 *>(r32)[j] = make_float2(float(r0), float(r1));
+            if constexpr (R32) reinterpret_cast<float2 *>(r32)[j] = make_float2(d2f_bits(r0), d2f_bits(r1));
         }
         if ((n & 1) && tid == 0) one(n - 1);
     } else {
@@ -175,7 +175,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
     const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     const int64_t nth = int64_t(gridDim.x) * blockDim.x;
     auto one = [&](int64_t i) {
-        double zi = double(zin[i]);
+        double zi = cvt<double>(zin[i]);
         a0 = fma(zi, r[i], a0);
         if (flexible) a1 = fma(zi, q[i], a1);
     };
@@ -186,8 +186,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
             double z0, z1;
             if constexpr (sizeof(ZT) == 4) {
                 const float2 t = reinterpret_cast<const float2 *>(zin)[j];
-                z0 = t.x;
-                z1 = t.y;
+                z0 = f2d_bits(t.x);
+                z1 = f2d_bits(t.y);
             } else {
                 const double2 t = ld2(reinterpret_cast<const double *>(zin), j);
                 z0 = t.x;
@@ -241,8 +241,8 @@ __global__ void __launch_bounds__(kBlock) k_cg_pupdate(int64_t n, const ZT *__re
             double z0, z1;
             if constexpr (sizeof(ZT) == 4) {
                 const float2 t = reinterpret_cast<const float2 *>(z)[j];
-                z0 = t.x;
-                z1 = t.y;
+                z0 = f2d_bits(t.x);
+                z1 = f2d_bits(t.y);
             } else {
                 const double2 t = ld2(reinterpret_cast<const double *>(z), j);
                 z0 = t.x;
@@ -251,9 +251,9 @@ __global__ void __launch_bounds__(kBlock) k_cg_pupdate(int64_t n, const ZT *__re
             const double2 pv = ld2(p, j);
             st2(p, j, make_double2(z0 + beta * pv.x, z1 + beta * pv.y));
         }
-        if ((n & 1) && tid == 0) p[n - 1] = double(z[n - 1]) + beta * p[n - 1];
+        if ((n & 1) && tid == 0) p[n - 1] = cvt<double>(z[n - 1]) + beta * p[n - 1];
     } else {
-        for (int64_t i = tid; i < n; i += nth) p[i] = double(z[i]) + beta * p[i];
+        for (int64_t i = tid; i < n; i += nth) p[i] = cvt<double>(z[i]) + beta * p[i];
     }
 }
 

@@ -17,12 +17,40 @@ __device__ __forceinline__ D cvt(__nv_bfloat16 v);
 
 template <>
 __device__ __forceinline__ double cvt<double>(double v) { return v; }
+// Exact IEEE-754 binary32 -> binary64 and round-to-nearest-even binary64 -> binary32 by bit
+// manipulation on the integer pipe.  On GB300 the FP64 pipe (about two operations per clock
+// per SM) also executes the hardware conversions, and it bounds the FP64 vector kernels of
+// the mixed solver; zeros, subnormals, infinities and NaNs take the hardware conversion.
+__device__ __forceinline__ double f2d_bits(float f) {
+    const uint32_t u = __float_as_uint(f);
+    const uint32_t e = (u >> 23) & 0xffu;
+    if (e - 1u < 254u) {  // normal: rebias the exponent (1023 - 127), widen the mantissa
+        const uint64_t b = (uint64_t(u & 0x80000000u) << 32) | (uint64_t(e + 896u) << 52) |
+                           (uint64_t(u & 0x7fffffu) << 29);
+        return __longlong_as_double((long long)b);
+    }
+    return double(f);
+}
+__device__ __forceinline__ float d2f_bits(double d) {
+    const uint64_t b = (uint64_t)__double_as_longlong(d);
+    const uint32_t e = uint32_t(b >> 52) & 0x7ffu;
+    if (e - 897u < 254u) {  // the result's exponent is a normal float exponent (1..254)
+        const uint64_t m = b & 0xfffffffffffffull;
+        uint32_t r = ((e - 896u) << 23) | uint32_t(m >> 29);  // truncated exponent and mantissa
+        const uint64_t rem = m & 0x1fffffffull;               // the 29 dropped bits
+        const uint64_t half = 0x10000000ull;
+        r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;  // a carry may raise the exponent (to inf)
+        return __uint_as_float((uint32_t(b >> 32) & 0x80000000u) | r);
+    }
+    return float(d);
+}
+
 template <>
-__device__ __forceinline__ float cvt<float>(double v) { return float(v); }
+__device__ __forceinline__ float cvt<float>(double v) { return d2f_bits(v); }
 template <>
 __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(double v) { return __float2bfloat16(float(v)); }
 template <>
-__device__ __forceinline__ double cvt<double>(float v) { return double(v); }
+__device__ __forceinline__ double cvt<double>(float v) { return f2d_bits(v); }
 template <>
 __device__ __forceinline__ float cvt<float>(float v) { return v; }
 template <>

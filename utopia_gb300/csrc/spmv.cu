@@ -483,21 +483,30 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
         T acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = T(0);
-        if (w >= 0) {
-            // the slice's keys were read once (coalesced) and are broadcast by shuffle, so
-            // the gathers of a slot depend on no load but the value stream's; row r gathers
-            // at gb[r] + key: gb = the row (diagonal) or the row's first column (anchored,
-            // stored at the row's slot position lane R + r)
-            const bool anch = w >= kAnchoredTag;
-            const int wk = anch ? w - kAnchoredTag : w;
+        if (w >= 0 && w < kAnchoredTag) {
+            // the slice's offsets were read once (coalesced) and are broadcast by shuffle, so
+            // the gathers of a slot depend on no load but the value stream's
+            const int r0i = int(row0);  // nrows, ncols < 2^31
+            const int cmax = int(m.ncols) - 1;
+            UGPU_PRAGMA_UNROLL(UGPU_SELL_UNROLL)
+            for (int k = 0; k < w; ++k) {
+                const int32_t off = __shfl_sync(0xffffffffu, k < 32 ? off_lo : off_hi, k & 31);
+                LV v[R];
+                VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    int c = r0i + r * rs + off;
+                    c = c < 0 ? 0 : (c > cmax ? cmax : c);
+                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
+                }
+            }
+        } else if (w >= kAnchoredTag) {
+            // anchored: row r gathers at gb[r] + key, gb = the row's first column (stored at
+            // the row's slot position lane R + r); keys broadcast by shuffle as above
+            const int wk = w - kAnchoredTag;
             const int cmax = int(m.ncols) - 1;
             int gb[R];
-            if (anch) {
-                load_cols<R>(m.cols + aux + lane * R, gb);
-            } else {
-#pragma unroll
-                for (int r = 0; r < R; ++r) gb[r] = int(row0) + r * rs;  // nrows, ncols < 2^31
-            }
+            load_cols<R>(m.cols + aux + lane * R, gb);
             UGPU_PRAGMA_UNROLL(UGPU_SELL_UNROLL)
             for (int k = 0; k < wk; ++k) {
                 const int32_t off = __shfl_sync(0xffffffffu, k < 32 ? off_lo : off_hi, k & 31);
@@ -733,7 +742,8 @@ struct StagedNeeds {
     static constexpr bool w = epi_reads_w<EPI>() || XM == 2;
 };
 
-template <class V, int EPI, int XM>
+// ANCH: the operator has anchored slices (transfers); false compiles the diagonal-only kernel
+template <class V, int EPI, int XM, bool ANCH>
 __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, EpiParams<float> e, StagedCfg cfg,
                                                                    int *kflag) {
     if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
@@ -775,7 +785,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         return s < ns ? __ldg(reinterpret_cast<const int4 *>(m.hdr) + s) : make_int4(0, 0, 0, 0);
     };
     auto meta_of = [&](const int4 &q) -> Meta {
-        const int anch = q.z >= kAnchoredTag;
+        const int anch = ANCH && q.z >= kAnchoredTag;
         Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), anch ? q.z - kAnchoredTag : q.z, 0, q.w, anch, 0, 0};
         const int32_t *kp = anch ? m.cols + q.w + S : m.offs + q.w;
         if (lane < mt.w) mt.off = __ldg(kp + lane);
@@ -846,7 +856,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (Nd::xr) total += rbytes;
         if (Nd::v) total += rbytes;
         if (Nd::w) total += rbytes;
-        if (mt.anch) total += S * 4u;
+        if (ANCH && mt.anch) total += S * 4u;
         fence_proxy_async_smem();
         __syncwarp();
         if (lane == 0) mbar_arrive_expect_tx(&bar[st], total);
@@ -863,7 +873,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (Nd::xr && lane == 1) bulk_g2s(sg + cfg.o_xr, e.x + r0, rbytes, &bar[st]);
         if (Nd::v && lane == 2) bulk_g2s(sg + cfg.o_v, e.v + r0, rbytes, &bar[st]);
         if (Nd::w && lane == 3) bulk_g2s(sg + cfg.o_w, e.w + r0, rbytes, &bar[st]);
-        if (mt.anch && lane == 4) bulk_g2s(sg + cfg.o_a, m.cols + mt.aux, S * 4u, &bar[st]);
+        if (ANCH && mt.anch && lane == 4) bulk_g2s(sg + cfg.o_a, m.cols + mt.aux, S * 4u, &bar[st]);
     };
 
     // the product and epilogue of slice s from stage st
@@ -878,9 +888,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         float acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = 0.f;
-        const int flags = d[1];
+        const int flags = ANCH ? d[1] : (d[1] & 1);
         const int *sa = reinterpret_cast<const int *>(sg + cfg.o_a);
-        if (cfg.xglobal) {
+        if (ANCH && cfg.xglobal) {
             // values (and anchors) staged, x gathered through L1 / L2
             int gb[R];
             if (flags & 2) {
@@ -905,7 +915,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                     acc[r] = fmaf(v[r], xv, acc[r]);
                 }
             }
-        } else if (flags == 3) {
+        } else if (ANCH && flags == 3) {
             // anchored, interior
             int a[R];
             stage_anchors(sa, lane, a);
@@ -942,7 +952,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         } else {
             // boundary slice: clamp every gather
             int gb[R];
-            if (flags & 2) {
+            if (ANCH && (flags & 2)) {
                 stage_anchors(sa, lane, gb);
             } else {
 #pragma unroll
@@ -1088,7 +1098,9 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
 
 int spmv_grid(const Context &ctx, int64_t units_per_cta_work, int64_t total) {
     int64_t g = (total + units_per_cta_work - 1) / units_per_cta_work;
-    int64_t cap = int64_t(ctx.sms) * 8;
+    // up to four waves of resident CTAs: a warp's rows are a serial chain of dependent loads,
+    // so few rows per warp keep more of them in flight
+    int64_t cap = int64_t(ctx.sms) * 32;
     if (g > cap) g = cap;
     if (g < 1) g = 1;
     return int(g);
@@ -1119,11 +1131,9 @@ void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
 
 inline uint32_t round128(uint32_t b) { return (b + 127u) & ~127u; }
 
-// Launches the staged kernel when the matrix and vectors allow it; false otherwise.
-template <class V, int EPI, int XM>
-bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
+template <class V, int EPI, int XM, bool ANCH>
+bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
-    if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
     const EpiParams<float> e = make_epi<float>(a);
     if (!e.vec_ok) return false;
     using Nd = StagedNeeds<EPI, XM>;
@@ -1154,7 +1164,7 @@ bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (s.nanch_slices) o += S * 4;
     c.stage_bytes = round128(o);
     c.hdr_bytes = round128(8u * kStagedMaxStages + 4u * kStagedDesc * kStagedMaxStages);
-    auto kern = k_sell_staged<V, EPI, XM>;
+    auto kern = k_sell_staged<V, EPI, XM, ANCH>;
     static bool attr = false;
     if (!attr) {
         UGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -1189,6 +1199,18 @@ bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * best_per_sm)));
     kern<<<g, kStagedWarps * 32, cta, ctx.stream>>>(m, e, c, ctx.d_kflags());
     return true;
+}
+
+// Launches the staged kernel when the matrix and vectors allow it; false otherwise.  Operators
+// with anchored slices (interpolations) take the anchored variant, built for the product and
+// the prolongation's add form only.
+template <class V, int EPI, int XM>
+bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
+    const Sell &s = *A.sell;
+    if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
+    if (s.nanch_slices == 0) return staged_launch_t<V, EPI, XM, false>(ctx, A, a);
+    if constexpr ((EPI == EPI_ADD || EPI == EPI_STORE) && XM == 0) return staged_launch_t<V, EPI, XM, true>(ctx, A, a);
+    return false;
 }
 
 template <class V, class T, int EPI, int XM, bool DOT>
