@@ -195,6 +195,24 @@ def run_spmv_only(args):
     print(json.dumps({"spmv_only": True, "n": A.nrows, "nnz": A.nnz}))
 
 
+def run_cg_jacobi(args):
+    """Profiling case: FP64 CG with the Jacobi preconditioner on the lognormal operator, four
+    iterations, every kernel launched individually (FP64 SpMV + (p, Ap), the CG vector kernels)."""
+    import utopia_gb300 as U
+    from utopia_gb300 import problems as P
+
+    A = P.lognormal_diffusion_3d(args.size, 2)[0]
+    ctx = U.Context(0)
+    M = U.SparseMatrix(ctx, A)
+    b = U.Vector(ctx, np.random.default_rng(0).uniform(-1, 1, A.nrows))
+    x = U.Vector(ctx, n=A.nrows)
+    cg = U.ConjugateGradient(ctx, atol=0.0, max_it=4, use_graphs=0)
+    cg.set_preconditioner(U.InvDiagPreconditioner(ctx))
+    cg.solve(M, b, x)
+    ctx.synchronize()
+    print(json.dumps({"cg_jacobi": True, "n": A.nrows, "iterations": cg.solution_status()["iterates"]}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -207,6 +225,8 @@ def main():
     ap.add_argument("--eager", action="store_true",
                     help="launch every kernel individually instead of one graph per solve (ncu does not "
                          "profile kernels inside conditional graph bodies)")
+    ap.add_argument("--cg-jacobi", action="store_true",
+                    help="profiling case: four eager iterations of FP64 Jacobi-preconditioned CG, nothing else")
     ap.add_argument("--spmv-only", action="store_true",
                     help="profiling case: FP64 and FP32 products and a BF16 Jacobi sweep of the fine operator, "
                          "two launches each, nothing else")
@@ -216,6 +236,9 @@ def main():
         return
     if args.spmv_only:
         run_spmv_only(args)
+        return
+    if args.cg_jacobi:
+        run_cg_jacobi(args)
         return
 
     import torch
