@@ -1,5 +1,6 @@
 """CPU checks of the C-ABI library: it builds, loads without a GPU, exports every entry
-point declared in include/ugpu.h, and reports a missing device as an error code."""
+point declared in include/ugpu.h and include/isolver_lsolve.h, and reports a missing device
+as an error code."""
 import ctypes
 import os
 import subprocess
@@ -57,3 +58,25 @@ def test_null_handles_are_rejected(lib):
     assert lib.ugpu_spmv(None, None, None) == -2
     assert lib.ugpu_solver_apply(None, None, None) == -2
     assert lib.ugpu_vec_destroy(None) == 0
+
+
+def test_isolver_plugin_is_exported(lib):
+    """The ten isolver_lsolve_* entry points of utopia's isolver plugin are served by libugpu."""
+    syms = _abi.isolver_symbols()
+    assert len(syms) == 10 and set(syms) == set(_abi.ISOLVER_SIGNATURES)
+    out = subprocess.run(["nm", "-D", "--defined-only", _abi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
+    assert not [s for s in syms if s not in exported]
+
+
+def test_isolver_plugin_errors_without_state(lib):
+    import torch
+
+    assert lib.isolver_lsolve_init(None) == -2
+    info = _abi.IsolverLsolve()
+    x = (ctypes.c_double * 4)()
+    assert lib.isolver_lsolve_apply(ctypes.byref(info), x, x) == -5  # no solver in private_data
+    assert lib.isolver_lsolve_set_atol(ctypes.byref(info), 1e-9) == -5
+    assert lib.isolver_lsolve_destroy(ctypes.byref(info)) == 0
+    if not torch.cuda.is_available():
+        assert lib.isolver_lsolve_init(ctypes.byref(info)) < 0 and not info.private_data

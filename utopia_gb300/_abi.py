@@ -117,6 +117,39 @@ SIGNATURES = {
 }
 
 
+ISOLVER_HEADER = os.path.join(os.path.dirname(HEADER), "isolver_lsolve.h")
+
+
+class IsolverLsolve(C.Structure):
+    """isolver_lsolve_t: communicator slot and the solver's private data."""
+
+    _fields_ = [("comm", C.c_void_p), ("private_data", C.c_void_p)]
+
+
+_ip = C.POINTER(C.c_int)
+_dp = C.POINTER(C.c_double)
+_info = C.POINTER(IsolverLsolve)
+ISOLVER_SIGNATURES = {
+    "isolver_lsolve_init": [_info],
+    "isolver_lsolve_update_crs": [_info, C.c_ssize_t, C.c_ssize_t, _ip, _ip, _dp],
+    "isolver_lsolve_update_with_preconditioner_crs": [_info, C.c_ssize_t, C.c_ssize_t, _ip, _ip, _dp, _ip, _ip,
+                                                      _dp],
+    "isolver_lsolve_apply": [_info, _dp, _dp],
+    "isolver_lsolve_set_max_iterations": [_info, C.c_int],
+    "isolver_lsolve_set_atol": [_info, C.c_double],
+    "isolver_lsolve_set_stol": [_info, C.c_double],
+    "isolver_lsolve_set_rtol": [_info, C.c_double],
+    "isolver_lsolve_set_verbosity": [_info, C.c_int],
+    "isolver_lsolve_destroy": [_info],
+}
+
+
+def isolver_symbols(path: str = ISOLVER_HEADER):
+    """Function names declared with ISOLVER_EXPORT in include/isolver_lsolve.h."""
+    txt = open(path).read()
+    return sorted(set(re.findall(r"ISOLVER_EXPORT\s+(isolver_\w+)\s*\(", txt)))
+
+
 def header_symbols(path: str = HEADER):
     """Function names declared with UGPU_API in include/ugpu.h."""
     txt = open(path).read()
@@ -135,6 +168,10 @@ def load(path: str = LIB_PATH):
                 f = getattr(L, name)
                 f.argtypes = args
                 f.restype = C.c_char_p if name == "ugpu_last_error" else C.c_int
+            for name, args in ISOLVER_SIGNATURES.items():
+                f = getattr(L, name)
+                f.argtypes = args
+                f.restype = C.c_int
             _lib = L
     return _lib
 
