@@ -59,6 +59,7 @@ extern "C" {
 #define UGPU_SOLVER_MPRGP 4       /* utopia::MPRGP */
 #define UGPU_SOLVER_PGS 5         /* utopia::ProjectedGaussSeidel */
 #define UGPU_SOLVER_CHOLESKY 6    /* dense coarse-level direct solver (utopia::Factorization) */
+#define UGPU_SOLVER_AMG 7         /* utopia::AlgebraicMultigrid with utopia::Agglomerate */
 
 /* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
 #define UGPU_CONVERGED_FNORM_ABS 2
@@ -246,6 +247,13 @@ UGPU_API int ugpu_solver_status(const ugpu_solver *s, ugpu_solution_status *out)
  * order; red-black (x + y) mod 2 on the 5-point grid).  The reference sweeps rows
  * lexicographically (utopia_ProjectedGaussSeidel.hpp:213-254); colour may be NULL. */
 UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *ncolours);
+/* Aggregation of level `level` of an algebraic multigrid (0 = the fine operator's): parent[i] = the
+ * aggregate of row i, -2 for excluded Dirichlet rows (Agglomerate::create_transfer_matrix,
+ * utopia/solvers/multilevel/agglomerate/utopia_Agglomerate.hpp:51-186); *n rows, *n_coarse aggregates.
+ * The algebraic multigrid (UGPU_SOLVER_AMG, utopia/solvers/multilevel/utopia_AlgebraicMultigrid.hpp:16-177)
+ * takes the keys n_levels (reference default 2; 0 = coarsen until at most max_coarse_rows rows), bmax,
+ * weight, use_additive_correction and every multigrid key; the ugpu_mg_* queries accept it. */
+UGPU_API int ugpu_amg_parent(const ugpu_solver *amg, int level, int32_t *parent, int64_t *n, int64_t *n_coarse);
 
 /* ---------------------------------------------------------------- differentiable solve ---- */
 /* No reference counterpart (utopia/differentiable/ is symbolic autodiff of expressions, not an

@@ -86,6 +86,7 @@ def lib():
                 "or_projected_gradient_norm": (_d, [_vp, _vp, _vp, _vp, _vp]),
                 "or_edge_grad": (None, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
                 "or_pattern_grad": (None, [_vp, _vp, _vp, _vp]),
+                "or_agglomerate": (_vp, [_vp, _i64, _d, C.c_int, _vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -282,3 +283,26 @@ def pattern_grad(A: Matrix, lam, x):
     g = np.empty(A.nnz)
     lib().or_pattern_grad(A.h, _p(lam), _p(x), _p(g))
     return g
+
+
+def agglomerate(A: Matrix, bmax=3, weight=1.0 / 3, use_additive_correction=False):
+    """Agglomerate::create_transfer_matrix: (parent per row, prolongator as an oracle Matrix)."""
+    parent = np.empty(A.nrows, np.int32)
+    h = lib().or_agglomerate(A.h, int(bmax), float(weight), int(use_additive_correction), _p(parent))
+    return parent, Matrix(_handle=h)
+
+
+def amg_hierarchy(A: Matrix, n_levels=2, bmax=3, weight=1.0 / 3, max_coarse_rows=4096):
+    """AlgebraicMultigridBuilder::build: prolongators ordered coarse -> fine (n_levels 0: coarsen
+    until at most max_coarse_rows rows) and the aggregation parents, finest first."""
+    Ps, parents, cur = [], [], A
+    level = 0
+    while (n_levels == 0 and cur.nrows > max_coarse_rows) or (n_levels and level < n_levels - 1):
+        parent, P = agglomerate(cur, bmax, weight)
+        if n_levels == 0 and P.ncols == cur.nrows:
+            break
+        Ps.append(P)
+        parents.append(parent)
+        cur = Matrix(_handle=lib().or_ptap(cur.h, P.h))
+        level += 1
+    return Ps[::-1], parents

@@ -1184,6 +1184,66 @@ int or_pgs_solve(const void *hA, const double *b, const double *lb, const double
 
 int or_colouring(const void *hA, int32_t *colour) { return greedy_colouring(*static_cast<const Csr *>(hA), colour); }
 
+// Agglomerate::create_transfer_matrix (utopia/solvers/multilevel/agglomerate/utopia_Agglomerate.hpp:51-186),
+// one process.  Restated from the reference: Dirichlet rows (one stored value) excluded (parent -2) unless
+// use_additive_correction (:70-77); a_max_i = max_{j != i} |a_ij| (:88-92); greedy aggregation in row order
+// with at most bmax neighbours j, |a_ij| > weight a_max_i, parent_j == -1 (:95-141); leftovers become
+// singletons (:143-147); prolongator P(i, parent_i) = (a_max_i != 0) (:162-176).  Returns P and fills parent.
+void *or_agglomerate(const void *hA, int64_t bmax, double weight, int use_additive_correction, int32_t *parent_out) {
+    const Csr &A = *static_cast<const Csr *>(hA);
+    const int64_t n = A.n;
+    std::vector<int32_t> parent(n, -1);
+    std::vector<double> a_max(n, 0.0);
+    int64_t nc = 0;
+    if (!use_additive_correction)
+        for (int64_t i = 0; i < n; ++i)
+            if (A.rp[i + 1] - A.rp[i] == 1) parent[i] = -2;
+    for (int64_t i = 0; i < n; ++i)
+        for (int32_t k = A.rp[i]; k < A.rp[i + 1]; ++k)
+            if (A.ci[k] != i) a_max[i] = std::max(a_max[i], std::abs(A.v[k]));
+    for (int64_t i = 0; i < n; ++i) {
+        if (parent[i] != -1) continue;
+        parent[i] = int32_t(nc);
+        int64_t count = 0;
+        for (int32_t k = A.rp[i]; k < A.rp[i + 1]; ++k) {
+            const int32_t j = A.ci[k];
+            if (weight * a_max[i] < std::abs(A.v[k]) && parent[j] == -1) {
+                parent[j] = int32_t(nc);
+                ++count;
+            }
+            if (count >= bmax) break;
+        }
+        if (count == 0) {
+            parent[i] = -1;
+            double best = 0;
+            int64_t arg = -1;
+            for (int32_t k = A.rp[i]; k < A.rp[i + 1]; ++k)
+                if (std::abs(A.v[k]) > best) {
+                    best = std::abs(A.v[k]);
+                    arg = A.ci[k];
+                }
+            if (arg != -1) parent[i] = parent[arg];
+        } else {
+            ++nc;
+        }
+    }
+    for (int64_t i = 0; i < n; ++i)
+        if (parent[i] == -1) parent[i] = int32_t(nc++);
+    auto *P = new Csr();
+    P->n = n;
+    P->m = nc;
+    P->rp.assign(n + 1, 0);
+    for (int64_t i = 0; i < n; ++i) {
+        if (parent[i] >= 0) {
+            P->ci.push_back(parent[i]);
+            P->v.push_back(a_max[i] != 0 ? 1.0 : 0.0);
+        }
+        P->rp[i + 1] = int32_t(P->ci.size());
+    }
+    std::copy(parent.begin(), parent.end(), parent_out);
+    return P;
+}
+
 // Projected-gradient norm || P(x - g) - x ||, g = A x - b (reported for the QP runs)
 double or_projected_gradient_norm(const void *hA, const double *b, const double *lb, const double *ub,
                                   const double *x) {

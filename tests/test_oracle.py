@@ -144,3 +144,68 @@ def test_oracle_adjoint_gradient_matches_central_differences(oracle):
         Lm = np.sum((solve(theta - h * v, b) - x_t) ** 2)
         fd = (Lp - Lm) / (2 * h)
         assert abs(g @ v - fd) <= 1e-6 * abs(fd)
+
+
+def _agglomerate_py(A, bmax=3, weight=1.0 / 3):
+    """Independent pure-Python restatement of Agglomerate::create_transfer_matrix
+    (utopia/solvers/multilevel/agglomerate/utopia_Agglomerate.hpp:51-186), for small matrices."""
+    n, rp, ci, v = A.nrows, A.rowptr, A.colidx, A.values
+    parent = [-1] * n
+    for i in range(n):
+        if rp[i + 1] - rp[i] == 1:
+            parent[i] = -2
+    amax = [max([abs(v[k]) for k in range(rp[i], rp[i + 1]) if ci[k] != i], default=0.0) for i in range(n)]
+    nc = 0
+    for i in range(n):
+        if parent[i] != -1:
+            continue
+        parent[i] = nc
+        count = 0
+        for k in range(rp[i], rp[i + 1]):
+            j = ci[k]
+            if weight * amax[i] < abs(v[k]) and parent[j] == -1:
+                parent[j] = nc
+                count += 1
+            if count >= bmax:
+                break
+        if count == 0:
+            parent[i] = -1
+            best, arg = 0.0, -1
+            for k in range(rp[i], rp[i + 1]):
+                if abs(v[k]) > best:
+                    best, arg = abs(v[k]), ci[k]
+            if arg != -1:
+                parent[i] = parent[arg]
+        else:
+            nc += 1
+    for i in range(n):
+        if parent[i] == -1:
+            parent[i] = nc
+            nc += 1
+    return np.array(parent, np.int32), nc
+
+
+def test_agglomerate_matches_python_restatement(oracle):
+    for A in (P.laplacian_1d_dirichlet(100), P.lognormal_diffusion_3d(8, 3)[0], P.random_spd_graph(600, 3, 2)):
+        parent, Pm = oracle.agglomerate(oracle.Matrix(A))
+        ref, nc = _agglomerate_py(A)
+        np.testing.assert_array_equal(parent, ref)
+        assert Pm.ncols == nc and Pm.nrows == A.nrows
+        rp, ci, v = Pm.arrays()
+        assert np.array_equal(ci, ref[ref >= 0])
+
+
+def test_reference_amg_1d_case(oracle):
+    """The reference's AMGTest (utopia/tests/utopia_AMGTest.cpp:36-110): 1D Laplacian with identity
+    boundary rows, 100 dofs, b = 2 (0 on the boundary), 6 levels, atol 1e-6; pass if ||b - A x||_1 < 1e-5.
+    The reference smooths with ILU (exact on a tridiagonal matrix), which this build does not have; with
+    Chebyshev3level smoothing the hierarchy preconditions CG instead of iterating alone."""
+    A = P.laplacian_1d_dirichlet(100)
+    Am = oracle.Matrix(A)
+    b = np.full(100, 2.0)
+    b[0] = b[-1] = 0.0
+    Ps, parents = oracle.amg_hierarchy(Am, n_levels=6)
+    assert [p.nrows for p in Ps[::-1]] == [100, 49, 25, 13, 7]
+    mg = oracle.Multigrid(Am, Ps, smoother="chebyshev", pre=3, post=3)
+    x, st = oracle.cg_solve(Am, b, precond="mg", mg=mg, atol=1e-6, max_it=100)
+    assert st["converged"] and np.abs(b - A.matvec(x)).sum() < 1e-5

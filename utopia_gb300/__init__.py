@@ -379,6 +379,25 @@ class Multigrid(_Solver):
         self.ctx.check(self.ctx.lib.ugpu_mg_vcycle(self.h, r.h, z.h))
 
 
+class AlgebraicMultigrid(Multigrid):
+    """utopia::AlgebraicMultigrid with utopia::Agglomerate: the hierarchy is built from the
+    operator by greedy aggregation (keys n_levels, bmax, weight, use_additive_correction;
+    n_levels=0 coarsens until at most max_coarse_rows rows), then runs as the multigrid."""
+
+    KIND = _abi.SOLVER_AMG
+
+    def set_transfer_operators(self, interpolations):
+        raise TypeError("the algebraic multigrid builds its own transfer operators")
+
+    def parent(self, level: int):
+        """Aggregate of every row of level `level` (0 = the fine operator); -2 = excluded row."""
+        n, nc = C.c_int64(), C.c_int64()
+        self.ctx.check(self.ctx.lib.ugpu_amg_parent(self.h, int(level), None, C.byref(n), C.byref(nc)))
+        out = np.empty(n.value, np.int32)
+        self.ctx.check(self.ctx.lib.ugpu_amg_parent(self.h, int(level), _ptr(out), None, None))
+        return out, nc.value
+
+
 class _QPSolver(_Solver):
     def set_box_constraints(self, lb: Vector | None, ub: Vector | None):
         self._box = (lb, ub)

@@ -19,6 +19,7 @@ HEADER = os.path.join(ROOT, "include", "ugpu.h")
 F64, F32, BF16 = 0, 1, 2
 FORMAT_CSR, FORMAT_SELL = 0, 1
 SOLVER_CG, SOLVER_MULTIGRID, SOLVER_INVDIAG, SOLVER_MPRGP, SOLVER_PGS, SOLVER_CHOLESKY = 1, 2, 3, 4, 5, 6
+SOLVER_AMG = 7
 
 _lock = threading.Lock()
 _lib = None
@@ -109,6 +110,7 @@ SIGNATURES = {
     "ugpu_solver_status": [_vp, C.POINTER(SolutionStatus)],
     "ugpu_project": [_vp, _vp, _vp],
     "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
+    "ugpu_amg_parent": [_vp, _int, _vp, C.POINTER(_i64), C.POINTER(_i64)],
     "ugpu_graph_create": [_vp, _i64, _i64, _vp, _vp, _i64, _vp, _vp, _pp],
     "ugpu_graph_destroy": [_vp],
     "ugpu_graph_assemble": [_vp, _vp, _vp],

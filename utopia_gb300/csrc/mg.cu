@@ -596,20 +596,20 @@ private:
 std::unique_ptr<Solver> make_multigrid(Context *c) { return std::make_unique<Multigrid>(c); }
 
 int mg_n_levels(const Solver *s) {
-    auto m = dynamic_cast<const Multigrid *>(s);
+    auto m = dynamic_cast<const Multigrid *>(amg_multigrid(s));
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     return m->n_levels();
 }
 
 std::unique_ptr<Mat> mg_level_matrix(const Solver *s, int l) {
-    auto m = dynamic_cast<const Multigrid *>(s);
+    auto m = dynamic_cast<const Multigrid *>(amg_multigrid(s));
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     UGPU_CHECK(l >= 0 && l < m->n_levels(), UGPU_ERR_ARG, "level out of range");
     return cast_matrix(*m->level(l).A64, UGPU_F64);
 }
 
 void mg_eigs(const Solver *s, int l, double *emax, double *emin) {
-    auto m = dynamic_cast<const Multigrid *>(s);
+    auto m = dynamic_cast<const Multigrid *>(amg_multigrid(s));
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     UGPU_CHECK(l >= 0 && l < m->n_levels(), UGPU_ERR_ARG, "level out of range");
     m->eigs(l, emax, emin);

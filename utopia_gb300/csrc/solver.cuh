@@ -107,6 +107,9 @@ std::unique_ptr<Solver> make_invdiag(Context *c);
 std::unique_ptr<Solver> make_cholesky(Context *c);
 std::unique_ptr<Solver> make_mprgp(Context *c);
 std::unique_ptr<Solver> make_pgs(Context *c);
+std::unique_ptr<Solver> make_amg(Context *c);
+// the multigrid inside an algebraic multigrid solver (any other solver: itself)
+const Solver *amg_multigrid(const Solver *s);
 
 // multigrid introspection for the ABI
 int mg_n_levels(const Solver *s);

@@ -51,6 +51,7 @@ int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out) {
         case UGPU_SOLVER_MPRGP: s->impl = make_mprgp(c); break;
         case UGPU_SOLVER_PGS: s->impl = make_pgs(c); break;
         case UGPU_SOLVER_CHOLESKY: s->impl = make_cholesky(c); break;
+        case UGPU_SOLVER_AMG: s->impl = make_amg(c); break;
         default: throw Error(UGPU_ERR_ARG, "unknown solver kind");
     }
     *out = s.release();

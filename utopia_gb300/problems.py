@@ -361,3 +361,29 @@ def graph_adjoint(N: int = 128, seed: int = 4, seed_target: int = 5):
     b[(c * N + c) * N + c] += 1.0
     theta_t = np.random.default_rng(seed_target).normal(0.0, 0.5, G.E).astype(np.float32)
     return G, theta, b, theta_t
+
+
+def laplacian_1d_dirichlet(n: int) -> CSR:
+    """assemble_laplacian_1D(A, bc=true) (utopia/tests/test_problems/utopia_assemble_laplacian_1D.hpp:11-40):
+    rows 0 and n-1 are the identity, interior rows (-1, 2, -1) including the columns of the boundary."""
+    rows, cols, vals = [0, n - 1], [0, n - 1], [1.0, 1.0]
+    for i in range(1, n - 1):
+        rows += [i, i, i]
+        cols += [i - 1, i, i + 1]
+        vals += [-1.0, 2.0, -1.0]
+    return CSR.from_scipy(_sp.csr_matrix((vals, (rows, cols)), shape=(n, n)))
+
+
+def random_spd_graph(n: int, degree: int, seed: int) -> CSR:
+    """Weighted graph Laplacian of a random graph plus a small diagonal shift (SPD, unstructured)."""
+    rng = np.random.default_rng(seed)
+    i = np.repeat(np.arange(n), degree)
+    j = rng.integers(0, n, n * degree)
+    keep = i != j
+    w = rng.uniform(0.1, 2.0, keep.sum())
+    W = _sp.coo_matrix((w, (i[keep], j[keep])), shape=(n, n)).tocsr()
+    W = W + W.T
+    L = _sp.diags(np.asarray(W.sum(axis=1)).ravel() + 1e-3) - W
+    L = L.tocsr()
+    L.sort_indices()
+    return CSR.from_scipy(L)
