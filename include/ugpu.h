@@ -251,7 +251,8 @@ UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *nc
  * aggregate of row i, -2 for excluded Dirichlet rows (Agglomerate::create_transfer_matrix,
  * utopia/solvers/multilevel/agglomerate/utopia_Agglomerate.hpp:51-186); *n rows, *n_coarse aggregates.
  * The algebraic multigrid (UGPU_SOLVER_AMG, utopia/solvers/multilevel/utopia_AlgebraicMultigrid.hpp:16-177)
- * takes the keys n_levels (reference default 2; 0 = coarsen until at most max_coarse_rows rows), bmax,
+ * takes the keys n_levels (reference default 2; 0 = coarsen until at most max_coarse_rows rows or until a
+ * level shrinks by less than 4:3), bmax,
  * weight, use_additive_correction and every multigrid key; the ugpu_mg_* queries accept it. */
 UGPU_API int ugpu_amg_parent(const ugpu_solver *amg, int level, int32_t *parent, int64_t *n, int64_t *n_coarse);
 

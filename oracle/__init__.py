@@ -299,7 +299,7 @@ def amg_hierarchy(A: Matrix, n_levels=2, bmax=3, weight=1.0 / 3, max_coarse_rows
     level = 0
     while (n_levels == 0 and cur.nrows > max_coarse_rows) or (n_levels and level < n_levels - 1):
         parent, P = agglomerate(cur, bmax, weight)
-        if n_levels == 0 and P.ncols == cur.nrows:
+        if n_levels == 0 and 4 * P.ncols > 3 * cur.nrows:  # coarsening stalled
             break
         Ps.append(P)
         parents.append(parent)

@@ -301,6 +301,30 @@ def test_spgemm_long_rows_use_the_cta_path(ctx, oracle):
               "close")
 
 
+def test_spgemm_wide_rows_use_the_window_path(ctx, oracle):
+    """Rows with more than 4096 intermediate products (here up to ~60,000, spread over ~30,000
+    columns, i.e. several 8192-column windows) go through the windowed dense-accumulator path:
+    identical structure to the oracle's product and values to rounding, and identical bits on a
+    second run (the accumulation order is fixed)."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(21)
+    A = sp.random(400, 3000, density=0.002, random_state=rng, format="lil")
+    for r in (0, 7, 399):
+        cols = rng.choice(3000, 2500, replace=False)
+        A[r, cols] = rng.standard_normal(cols.size)
+    A = A.tocsr()
+    A.sort_indices()
+    B = sp.random(3000, 30000, density=0.0008, random_state=rng, format="csr")
+    B.sort_indices()
+    Ac, Bc = P.CSR.from_scipy(A), P.CSR.from_scipy(B)
+    assert (A.astype(bool).astype(int) @ np.diff(B.indptr)).max() > 4096
+    Ag, Bg = U.SparseMatrix(ctx, Ac), U.SparseMatrix(ctx, Bc)
+    C1 = Ag.matmul(Bg)
+    _same_csr(C1, oracle.Matrix(Ac).matmul(oracle.Matrix(Bc)), "close")
+    np.testing.assert_array_equal(C1.csr()[2], Ag.matmul(Bg).csr()[2])
+
+
 def test_ptap_structure_bit_exact_fixture(ctx, oracle, laplace_hierarchy):
     A, Is, _ = laplace_hierarchy
     _same_csr(U.SparseMatrix(ctx, A).ptap(U.SparseMatrix(ctx, Is[2])), oracle.Matrix(A).ptap(oracle.Matrix(Is[2])),

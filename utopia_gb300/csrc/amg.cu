@@ -134,7 +134,7 @@ public:
         prm["bmax"] = 3;                // utopia_Agglomerate.hpp:43
         prm["weight"] = 1.0 / 3;        // utopia_Agglomerate.hpp:45
         prm["use_additive_correction"] = 0;
-        prm["max_coarse_rows"] = 4096;  // n_levels = 0: coarsen until the coarsest level is this small
+        prm["max_coarse_rows"] = 4096;  // n_levels = 0: coarsen until at most this many rows (or a stall)
     }
 
     void set(const std::string &k, double v) override {
@@ -166,7 +166,9 @@ public:
             agglomerate_host(cur->nrows, rp.data(), ci.data(), v.data(), int64_t(get("bmax")), get("weight"),
                              get("use_additive_correction") != 0, parent, amax, nc);
             UGPU_CHECK(nc > 0, UGPU_ERR_ARG, "algebraic multigrid: empty coarse level");
-            if (want_levels == 0 && nc == cur->nrows) break;  // no coarsening left
+            // automatic depth: stop once a level shrinks by less than 4:3 (the Galerkin operators
+            // of stalled levels grow dense and would dominate the cycle)
+            if (want_levels == 0 && 4 * nc > 3 * cur->nrows) break;
             auto P = prolongator(*ctx, cur->nrows, nc, parent, amax);
             parents_.push_back(parent);
             auto next = ptap(*cur, *P);  // IPRTransfer::restrict(M): P^T M P

@@ -281,8 +281,108 @@ __global__ void __launch_bounds__(kCtaThreads) k_spgemm_cta(const int *big_rows,
     __shared__ int s_count;
     for (int b = blockIdx.x; b < n_big; b += gridDim.x) {
         const int64_t i = big_rows[b];
+        if (ub[i] > kCtaRowsUb) continue;  // wide row: k_spgemm_wide
         row_product<V, NUMERIC, true>(i, threadIdx.x, blockDim.x, table_size(ub[i], kCtaTable), keys, vals, lkeys,
                                       lvals, &s_count, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    }
+}
+
+// Rows with more than kCtaRowsUb intermediate products (wide Galerkin rows of deep algebraic-
+// multigrid levels): one CTA per row walks the row's column range in windows of kWideWindow
+// columns, with a dense shared-memory accumulator per window.  Products are added in A-row order
+// (one B row at a time, each column owned by one thread, a barrier between B rows), so the sums
+// are deterministic; a block-wide scan of the window's occupancy flags writes the entries in
+// column order.  NUMERIC = false counts the row's distinct columns.
+constexpr int kWideWindow = 8192;
+constexpr int kWideThreads = 256;
+constexpr size_t kWideSmem = (sizeof(double) + sizeof(int)) * kWideWindow;
+
+template <bool NUMERIC>
+__global__ void __launch_bounds__(kWideThreads) k_spgemm_wide(const int *big_rows, int n_big, const int64_t *ub,
+                                                              const int32_t *arp, const int32_t *aci,
+                                                              const double *acv, const int32_t *brp,
+                                                              const int32_t *bci, const double *bcv, int64_t *cnt,
+                                                              const int32_t *crp, int32_t *cci, double *ccv) {
+    extern __shared__ unsigned char smem[];
+    double *acc = reinterpret_cast<double *>(smem);
+    int *flag = reinterpret_cast<int *>(acc + kWideWindow);
+    __shared__ int s_min, s_max, s_base, s_warp[kWideThreads / 32];
+    const int tid = threadIdx.x;
+    for (int b = blockIdx.x; b < n_big; b += gridDim.x) {
+        const int64_t i = big_rows[b];
+        if (ub[i] <= kCtaRowsUb) continue;  // a shared-memory hash row
+        // column range of the row's products
+        int lo = INT_MAX, hi = -1;
+        for (int32_t ka = arp[i]; ka < arp[i + 1]; ++ka) {
+            const int32_t j = aci[ka];
+            for (int32_t kb = brp[j] + tid; kb < brp[j + 1]; kb += kWideThreads) {
+                lo = min(lo, bci[kb]);
+                hi = max(hi, bci[kb]);
+            }
+        }
+        if (tid == 0) {
+            s_min = INT_MAX;
+            s_max = -1;
+            s_base = 0;
+        }
+        __syncthreads();
+        atomicMin(&s_min, lo);
+        atomicMax(&s_max, hi);
+        __syncthreads();
+        const int cmin = s_min, cmax = s_max;
+        int64_t written = 0;
+        for (int64_t c0 = cmin; c0 <= cmax; c0 += kWideWindow) {
+            for (int s = tid; s < kWideWindow; s += kWideThreads) {
+                acc[s] = 0.0;
+                flag[s] = 0;
+            }
+            __syncthreads();
+            for (int32_t ka = arp[i]; ka < arp[i + 1]; ++ka) {
+                const int32_t j = aci[ka];
+                const double a = NUMERIC ? acv[ka] : 0.0;
+                for (int32_t kb = brp[j] + tid; kb < brp[j + 1]; kb += kWideThreads) {
+                    const int64_t c = bci[kb] - c0;
+                    if (c >= 0 && c < kWideWindow) {
+                        flag[c] = 1;
+                        if (NUMERIC) acc[c] = fma(a, bcv[kb], acc[c]);
+                    }
+                }
+                __syncthreads();  // every product of this B row lands before the next row's
+            }
+            // block-wide exclusive scan of the flags: thread t owns kWideWindow / kWideThreads
+            // consecutive columns
+            constexpr int per = kWideWindow / kWideThreads;
+            int mine = 0;
+            for (int q = 0; q < per; ++q) mine += flag[tid * per + q];
+            int incl = mine;
+            const int lane = tid & 31, warp = tid >> 5;
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            if (lane == 31) s_warp[warp] = incl;
+            __syncthreads();
+            int wofs = 0;
+            for (int w = 0; w < warp; ++w) wofs += s_warp[w];
+            int pos = wofs + incl - mine;
+            if (NUMERIC) {
+                const int64_t base = int64_t(crp[i]) + written;
+                for (int q = 0; q < per; ++q) {
+                    const int s = tid * per + q;
+                    if (flag[s]) {
+                        cci[base + pos] = int32_t(c0 + s);
+                        ccv[base + pos] = acc[s];
+                        ++pos;
+                    }
+                }
+            }
+            int total = 0;
+            for (int w = 0; w < kWideThreads / 32; ++w) total += s_warp[w];
+            written += total;
+            __syncthreads();  // the window's arrays are reused
+        }
+        if (!NUMERIC && tid == 0) cnt[i] = written;
+        __syncthreads();
     }
 }
 
@@ -386,6 +486,10 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
                                        int(cta_smem)));
         UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(cta_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_wide<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kWideSmem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_wide<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(kWideSmem)));
         attr_done = true;
     }
     const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
@@ -406,8 +510,7 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
         }
         for (auto v : h) max_ub = std::max(max_ub, v);
     }
-    UGPU_CHECK(max_ub <= kCtaRowsUb, UGPU_ERR_UNSUPPORTED,
-               "spgemm: a row has more than 4096 intermediate products (shared-memory hash table limit)");
+    const bool wide = max_ub > kCtaRowsUb;  // rows beyond the shared-memory hash tables
     const int gw = int(std::min<int64_t>((m + kWarpsPerCta - 1) / kWarpsPerCta, int64_t(ctx.sms) * 16));
     // symbolic
     if (m) {
@@ -426,6 +529,13 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
             nullptr, nullptr);
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
+        if (wide) {
+            k_spgemm_wide<false><<<std::min(h_nbig, ctx.sms * 2), kWideThreads, kWideSmem, ctx.stream>>>(
+                big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr,
+                nullptr, nullptr);
+            ctx.launches++;
+            UGPU_LAUNCH_CHECK();
+        }
     }
     int64_t nnz = device_exclusive_scan(ctx, cnt.as<int64_t>(), crp64.as<int64_t>(), m);
     UGPU_CHECK(nnz < (1ll << 31), UGPU_ERR_UNSUPPORTED, "spgemm: product has more than 2^31 entries");
@@ -448,6 +558,13 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
             C->colidx.as<int32_t>(), C->vals.as<double>());
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
+        if (wide) {
+            k_spgemm_wide<true><<<std::min(h_nbig, ctx.sms * 2), kWideThreads, kWideSmem, ctx.stream>>>(
+                big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr,
+                C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
+            ctx.launches++;
+            UGPU_LAUNCH_CHECK();
+        }
     }
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
     finalize_matrix(*C);
