@@ -256,6 +256,23 @@ UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *nc
  * weight, use_additive_correction and every multigrid key; the ugpu_mg_* queries accept it. */
 UGPU_API int ugpu_amg_parent(const ugpu_solver *amg, int level, int32_t *parent, int64_t *n, int64_t *n_coarse);
 
+/* ---------------------------------------------------------------- files ---- */
+/* PETSc binary matrices and vectors (utopia::read / write over MatLoad / VecLoad, used for the
+ * reference's inputs in utopia/data and by utopia/apps/ls_solve/utopia_ls_solve.cpp:117-133).  Layout
+ * (big endian, 32-bit indices): Mat = classid 1211216, M, N, nnz, row lengths, column indices,
+ * float64 values; Vec = classid 1211214, N, float64 values.  Rows must have ascending columns. */
+UGPU_API int ugpu_petsc_read_mat(ugpu_ctx *ctx, const char *path, ugpu_mat **out);
+UGPU_API int ugpu_petsc_read_vec(ugpu_ctx *ctx, const char *path, ugpu_vec **out);
+UGPU_API int ugpu_petsc_write_mat(const ugpu_mat *A, const char *path);
+UGPU_API int ugpu_petsc_write_vec(const ugpu_vec *x, const char *path);
+/* Raw CRS directory (rowptr.raw, colidx.raw, values.raw; native endianness) as read by the reference's
+ * qp_solve inputs (utopia/data/test/qpsolve.yaml:13-35): index_bytes 4 or 8, value_bytes 8 or 4,
+ * ncols 0 = square.  Raw vectors: one native array of value_bytes elements (written as float64). */
+UGPU_API int ugpu_raw_crs_read(ugpu_ctx *ctx, const char *dir, int index_bytes, int value_bytes, int64_t ncols,
+                               ugpu_mat **out);
+UGPU_API int ugpu_raw_vec_read(ugpu_ctx *ctx, const char *path, int value_bytes, ugpu_vec **out);
+UGPU_API int ugpu_raw_vec_write(const ugpu_vec *x, const char *path);
+
 /* ---------------------------------------------------------------- differentiable solve ---- */
 /* No reference counterpart (utopia/differentiable/ is symbolic autodiff of expressions, not an
  * adjoint solver).  A graph with per-edge log-conductances theta:

@@ -297,7 +297,7 @@ def amg_hierarchy(A: Matrix, n_levels=2, bmax=3, weight=1.0 / 3, max_coarse_rows
     until at most max_coarse_rows rows) and the aggregation parents, finest first."""
     Ps, parents, cur = [], [], A
     level = 0
-    while (n_levels == 0 and cur.nrows > max_coarse_rows) or (n_levels and level < n_levels - 1):
+    while (n_levels == 0 and (level == 0 or cur.nrows > max_coarse_rows)) or (n_levels and level < n_levels - 1):
         parent, P = agglomerate(cur, bmax, weight)
         if n_levels == 0 and 4 * P.ncols > 3 * cur.nrows:  # coarsening stalled
             break

@@ -120,6 +120,12 @@ class Vector:
         self.ctx.check(self.ctx.lib.ugpu_vec_download(self.h, _ptr(out)))
         return out
 
+    def write_petsc(self, path: str):
+        self.ctx.check(self.ctx.lib.ugpu_petsc_write_vec(self.h, str(path).encode()))
+
+    def write_raw(self, path: str):
+        self.ctx.check(self.ctx.lib.ugpu_raw_vec_write(self.h, str(path).encode()))
+
     def upload_from(self, host_ptr: int):
         """Copy n elements from host memory at host_ptr (e.g. pinned) into the vector."""
         self.ctx.check(self.ctx.lib.ugpu_vec_upload(self.h, C.c_void_p(host_ptr)))
@@ -215,6 +221,9 @@ class SparseMatrix:
         self.ctx.check(self.ctx.lib.ugpu_mat_sell_info(self.h, C.byref(a), C.byref(b), C.byref(c), C.byref(d)))
         return {"nslices": a.value, "nstored": b.value, "ndiag_slices": c.value, "rows_per_slice": d.value}
 
+    def write_petsc(self, path: str):
+        self.ctx.check(self.ctx.lib.ugpu_petsc_write_mat(self.h, str(path).encode()))
+
     def sell_interleaved(self) -> bool:
         """True when the sliced-ELL rows are lane-interleaved (the staged kernel's layout)."""
         v = C.c_int()
@@ -262,6 +271,33 @@ class SparseMatrix:
 
     def jacobi_sweep(self, b: Vector, x: Vector, omega: float, x_out: Vector):
         self.ctx.check(self.ctx.lib.ugpu_jacobi_sweep(self.h, b.h, x.h, float(omega), x_out.h))
+
+
+def read_petsc_matrix(ctx: "Context", path: str) -> "SparseMatrix":
+    """A PETSc binary matrix file (FP64 CSR on the device)."""
+    h = C.c_void_p()
+    ctx.check(ctx.lib.ugpu_petsc_read_mat(ctx.h, str(path).encode(), C.byref(h)))
+    return SparseMatrix(ctx, _handle=h)
+
+
+def read_petsc_vector(ctx: "Context", path: str) -> "Vector":
+    h = C.c_void_p()
+    ctx.check(ctx.lib.ugpu_petsc_read_vec(ctx.h, str(path).encode(), C.byref(h)))
+    return Vector(ctx, _handle=h)
+
+
+def read_raw_crs(ctx: "Context", directory: str, index_bytes=4, value_bytes=8, ncols=0) -> "SparseMatrix":
+    """rowptr.raw, colidx.raw and values.raw of one directory."""
+    h = C.c_void_p()
+    ctx.check(ctx.lib.ugpu_raw_crs_read(ctx.h, str(directory).encode(), int(index_bytes), int(value_bytes),
+                                        int(ncols), C.byref(h)))
+    return SparseMatrix(ctx, _handle=h)
+
+
+def read_raw_vector(ctx: "Context", path: str, value_bytes=8) -> "Vector":
+    h = C.c_void_p()
+    ctx.check(ctx.lib.ugpu_raw_vec_read(ctx.h, str(path).encode(), int(value_bytes), C.byref(h)))
+    return Vector(ctx, _handle=h)
 
 
 class _Solver:

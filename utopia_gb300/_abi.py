@@ -111,6 +111,13 @@ SIGNATURES = {
     "ugpu_project": [_vp, _vp, _vp],
     "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
     "ugpu_amg_parent": [_vp, _int, _vp, C.POINTER(_i64), C.POINTER(_i64)],
+    "ugpu_petsc_read_mat": [_vp, C.c_char_p, _pp],
+    "ugpu_petsc_read_vec": [_vp, C.c_char_p, _pp],
+    "ugpu_petsc_write_mat": [_vp, C.c_char_p],
+    "ugpu_petsc_write_vec": [_vp, C.c_char_p],
+    "ugpu_raw_crs_read": [_vp, C.c_char_p, _int, _int, _i64, _pp],
+    "ugpu_raw_vec_read": [_vp, C.c_char_p, _int, _pp],
+    "ugpu_raw_vec_write": [_vp, C.c_char_p],
     "ugpu_graph_create": [_vp, _i64, _i64, _vp, _vp, _i64, _vp, _vp, _pp],
     "ugpu_graph_destroy": [_vp],
     "ugpu_graph_assemble": [_vp, _vp, _vp],

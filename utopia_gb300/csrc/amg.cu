@@ -160,7 +160,7 @@ public:
         std::vector<int32_t> rp, ci, parent;
         std::vector<double> v, amax;
         for (int64_t l = 0; want_levels == 0 || l < want_levels - 1; ++l) {
-            if (want_levels == 0 && cur->nrows <= max_coarse) break;
+            if (want_levels == 0 && l > 0 && cur->nrows <= max_coarse) break;  // at least one coarse level
             download_csr(*cur, rp, ci, v);
             int64_t nc = 0;
             agglomerate_host(cur->nrows, rp.data(), ci.data(), v.data(), int64_t(get("bmax")), get("weight"),
