@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
     if (vec) {
         // pairs of elements as 16-byte loads and stores
         const int64_t n2 = n >> 1;
-#pragma unroll 2
+#pragma unroll 4
         for (int64_t j = tid; j < n2; j += nth) {
             const double2 xv = ld2(x, j), pv = ld2(p, j), rv = ld2(r, j), qv = ld2(Ap, j);
             const double r0 = rv.x - alpha * qv.x, r1 = rv.y - alpha * qv.y;
@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
     };
     if (vec) {
         const int64_t n2 = n >> 1;
-#pragma unroll 2
+#pragma unroll 4
         for (int64_t j = tid; j < n2; j += nth) {
             double z0, z1;
             if constexpr (sizeof(ZT) == 4) {
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(kBlock) k_cg_pupdate(int64_t n, const ZT *__re
     const int64_t nth = int64_t(gridDim.x) * blockDim.x;
     if (vec) {
         const int64_t n2 = n >> 1;
-#pragma unroll 2
+#pragma unroll 4
         for (int64_t j = tid; j < n2; j += nth) {
             double z0, z1;
             if constexpr (sizeof(ZT) == 4) {
@@ -455,10 +455,13 @@ private:
         // K0: p = z + beta p   (plain CG: p = r + beta p)
         // the solver's own vectors are cudaMalloc'd; only x may be caller memory
         const int vec = al16(x) ? 1 : 0;
+        // K0 reduces nothing, so it is not tied to the reductions' fixed grid: full occupancy
+        const int gp = int(std::max<int64_t>(1, std::min<int64_t>((n / 2 + kBlock - 1) / kBlock,
+                                                                  int64_t(ctx->sms) * 8)));
         if (f32)
-            k_cg_pupdate<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), p_.as<double>(), dev, 1);
+            k_cg_pupdate<float><<<gp, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), p_.as<double>(), dev, 1);
         else
-            k_cg_pupdate<double><<<g, kBlock, 0, ctx->stream>>>(n, (mode_ == CG_PLAIN) ? r_.as<double>()
+            k_cg_pupdate<double><<<gp, kBlock, 0, ctx->stream>>>(n, (mode_ == CG_PLAIN) ? r_.as<double>()
                                                                                        : z_.as<double>(),
                                                                 p_.as<double>(), dev, 1);
         ctx->launches++;
