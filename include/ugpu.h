@@ -60,6 +60,8 @@ extern "C" {
 #define UGPU_SOLVER_PGS 5         /* utopia::ProjectedGaussSeidel */
 #define UGPU_SOLVER_CHOLESKY 6    /* dense coarse-level direct solver (utopia::Factorization) */
 #define UGPU_SOLVER_AMG 7         /* utopia::AlgebraicMultigrid with utopia::Agglomerate */
+#define UGPU_SOLVER_BICGSTAB 8    /* utopia::BiCGStab (utopia/solvers/smoothers/utopia_BiCGStab_impl.hpp:44-250); an
+                                   * FP64 preconditioner is applied from a zero initial guess */
 
 /* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
 #define UGPU_CONVERGED_FNORM_ABS 2

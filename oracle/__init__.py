@@ -87,6 +87,7 @@ def lib():
                 "or_edge_grad": (None, [_i64, _vp, _vp, _vp, _vp, _vp, _vp]),
                 "or_pattern_grad": (None, [_vp, _vp, _vp, _vp]),
                 "or_agglomerate": (_vp, [_vp, _i64, _d, C.c_int, _vp]),
+                "or_bicgstab_solve": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _d, _i64, _vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -306,3 +307,13 @@ def amg_hierarchy(A: Matrix, n_levels=2, bmax=3, weight=1.0 / 3, max_coarse_rows
         cur = Matrix(_handle=lib().or_ptap(cur.h, P.h))
         level += 1
     return Ps[::-1], parents
+
+
+def bicgstab_solve(A: Matrix, b, x0=None, precond="none", mg=None, atol=1e-9, max_it=1000):
+    """BiCGStab (utopia_BiCGStab_impl.hpp:44-250); precond "none", "invdiag" or "mg"."""
+    b = _f64(b)
+    x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+    st = Status()
+    kind = {"none": 0, "invdiag": 1, "mg": 2}[precond]
+    lib().or_bicgstab_solve(A.h, _p(b), _p(x), kind, mg.h if mg is not None else None, atol, max_it, C.byref(st))
+    return x, st.as_dict()

@@ -802,6 +802,103 @@ bool fcg(const Csr &A, const double *b, double *x, Precond &M, const Params &prm
     return st.converged;
 }
 
+// BiCGStab, utopia/solvers/smoothers/utopia_BiCGStab_impl.hpp:44-250 (preconditioned :44-155 when M is given,
+// unpreconditioned :157-250 otherwise).  Preconditioner applications start from zero.  When the preconditioned
+// form stops on ||s|| it returns h = x + alpha y (the reference leaves x one half-step behind there).
+bool bicgstab(const Csr &A, const double *b, double *x, Precond *M, const Params &prm, or_status &st) {
+    const int64_t n = A.n;
+    std::vector<double> r(n), r0(n), p(n, 0.0), v(n, 0.0), h(n), y(n), s(n, 0.0), t(n), z(n), kt(n);
+    st = or_status{};
+    double rho = 1, rho_old = 1, alpha = 1, omega = 1, beta = 1;
+    residual(A, b, x, r.data());
+    st.spmv_count++;
+    r0 = r;
+    int64_t it = 0;
+    bool converged = false;
+    double r_norm = 1e10;
+    auto pc = [&](const std::vector<double> &in, std::vector<double> &out) {
+        std::fill(out.begin(), out.end(), 0.0);
+        M->apply(in.data(), out.data());
+    };
+    while (!converged) {
+        rho = dot(n, r0.data(), r.data());
+        if (!M && rho == 0.) {
+            converged = true;
+            break;
+        }
+        beta = (rho / rho_old) * (alpha / omega);
+        for (int64_t i = 0; i < n; ++i) p[i] = r[i] + beta * (p[i] - omega * v[i]);
+        const std::vector<double> *q = &p;
+        if (M) {
+            pc(p, y);
+            q = &y;
+        }
+        spmv(A, q->data(), v.data());
+        st.spmv_count++;
+        const double r0v = dot(n, r0.data(), v.data());
+        if (M && r0v == 0.0) {
+            residual(A, b, x, r.data());
+            st.spmv_count++;
+            r_norm = norm2(n, s.data());
+            converged = check_convergence(prm, st, it, r_norm, 1, 1);
+            break;
+        }
+        alpha = rho / r0v;
+        for (int64_t i = 0; i < n; ++i) {
+            h[i] = x[i] + alpha * (*q)[i];
+            s[i] = r[i] - alpha * v[i];
+        }
+        if (M) {
+            r_norm = norm2(n, s.data());
+            converged = check_convergence(prm, st, it, r_norm, 1, 1);
+            if (converged) {
+                std::copy(h.begin(), h.end(), x);
+                break;
+            }
+        }
+        const std::vector<double> *zz = &s;
+        if (M) {
+            pc(s, z);
+            zz = &z;
+        }
+        spmv(A, zz->data(), t.data());
+        st.spmv_count++;
+        double num, den;
+        if (M) {
+            pc(t, kt);
+            num = dot(n, z.data(), kt.data());
+            den = dot(n, kt.data(), kt.data());
+        } else {
+            num = dot(n, t.data(), s.data());
+            den = dot(n, t.data(), t.data());
+        }
+        omega = num / den;
+        if (std::isnan(omega) || (!M && std::isinf(omega))) {
+            if (!M) {
+                r_norm = norm2(n, s.data());
+                converged = check_convergence(prm, st, it, r_norm, 1, 1);
+            }
+            break;
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] = h[i] + omega * (*zz)[i];
+            r[i] = s[i] - omega * t[i];
+        }
+        rho_old = rho;
+        r_norm = norm2(n, r.data());
+        converged = check_convergence(prm, st, it, r_norm, 1, 1);
+        it++;
+    }
+    if (st.reason == 0) {
+        st.iterates = it;
+        st.gradient_norm = r_norm;
+        if (converged) st.reason = CONVERGED_FNORM_ABS;
+        else if (std::isnan(omega)) st.reason = DIVERGED_NAN;
+    }
+    st.converged = st.reason > 0;
+    return st.converged;
+}
+
 // ------------------------------------------------------------------------------------
 // Box-constrained QP
 // ------------------------------------------------------------------------------------
@@ -1104,6 +1201,20 @@ int or_cg_solve(const void *hA, const double *b, double *x, int precond, void *m
     }
     auto *h = static_cast<MgHandle *>(mg);
     return flexible ? fcg(A, b, x, *h->pc(), p, *st) : pcg(A, b, x, *h->pc(), p, *st);
+}
+
+int or_bicgstab_solve(const void *hA, const double *b, double *x, int precond, void *mg, double atol, int64_t max_it,
+                      or_status *st) {
+    const Csr &A = *static_cast<const Csr *>(hA);
+    Params p;
+    p.atol = atol;
+    p.max_it = max_it;
+    if (precond == 0) return bicgstab(A, b, x, nullptr, p, *st);
+    if (precond == 1) {
+        InvDiag M(A);
+        return bicgstab(A, b, x, &M, p, *st);
+    }
+    return bicgstab(A, b, x, static_cast<MgHandle *>(mg)->pc(), p, *st);
 }
 
 // Multigrid hierarchy: P[] ordered coarse -> fine.  precision: 0 fp64, 1 fp32, 2 bf16 storage.

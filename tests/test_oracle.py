@@ -209,3 +209,20 @@ def test_reference_amg_1d_case(oracle):
     mg = oracle.Multigrid(Am, Ps, smoother="chebyshev", pre=3, post=3)
     x, st = oracle.cg_solve(Am, b, precond="mg", mg=mg, atol=1e-6, max_it=100)
     assert st["converged"] and np.abs(b - A.matvec(x)).sum() < 1e-5
+
+
+def test_oracle_bicgstab_solves_nonsymmetric_systems(oracle):
+    """BiCGStab restatement (utopia_BiCGStab_impl.hpp:44-250) on an upwind convection-diffusion
+    operator, without and with the Jacobi preconditioner: the stop is ||r|| <= atol and the
+    solution matches a direct solve."""
+    import scipy.sparse.linalg as spla
+
+    A = P.convection_diffusion_2d(48, 20.0)
+    b = np.random.default_rng(4).uniform(-1, 1, A.nrows)
+    xd = spla.spsolve(A.to_scipy().tocsc(), b)
+    atol = 1e-10 * np.linalg.norm(b)
+    for pc in ("none", "invdiag"):
+        x, st = oracle.bicgstab_solve(oracle.Matrix(A), b, precond=pc, atol=atol, max_it=2000)
+        assert st["converged"], (pc, st)
+        assert np.linalg.norm(b - A.matvec(x)) <= atol * 1.0001
+        assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)

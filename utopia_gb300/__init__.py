@@ -434,6 +434,16 @@ class AlgebraicMultigrid(Multigrid):
         return out, nc.value
 
 
+class BiCGStab(_Solver):
+    """utopia::BiCGStab; preconditioned when a (FP64) preconditioner is set."""
+
+    KIND = _abi.SOLVER_BICGSTAB
+
+    def set_preconditioner(self, prec):
+        self._prec = prec
+        self.ctx.check(self.ctx.lib.ugpu_solver_set_preconditioner(self.h, prec.h))
+
+
 class _QPSolver(_Solver):
     def set_box_constraints(self, lb: Vector | None, ub: Vector | None):
         self._box = (lb, ub)

@@ -52,6 +52,7 @@ int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out) {
         case UGPU_SOLVER_PGS: s->impl = make_pgs(c); break;
         case UGPU_SOLVER_CHOLESKY: s->impl = make_cholesky(c); break;
         case UGPU_SOLVER_AMG: s->impl = make_amg(c); break;
+        case UGPU_SOLVER_BICGSTAB: s->impl = make_bicgstab(c); break;
         default: throw Error(UGPU_ERR_ARG, "unknown solver kind");
     }
     *out = s.release();

@@ -387,3 +387,17 @@ def random_spd_graph(n: int, degree: int, seed: int) -> CSR:
     L = L.tocsr()
     L.sort_indices()
     return CSR.from_scipy(L)
+
+
+def convection_diffusion_2d(n: int, peclet: float = 20.0) -> CSR:
+    """-Laplace(u) + c . grad(u) on n x n interior nodes, 5-point diffusion and first-order upwind
+    convection with c = (peclet, peclet / 2): a nonsymmetric M-matrix (BiCGStab test operator)."""
+    h = 1.0 / (n + 1)
+    cx, cy = peclet, peclet / 2
+    main = 4.0 / h**2 + (cx + cy) / h
+    T = _sp.diags([-1.0 / h**2 - cx / h, 0.0, -1.0 / h**2], [-1, 0, 1], shape=(n, n))
+    Ty = _sp.diags([-1.0 / h**2 - cy / h, 0.0, -1.0 / h**2], [-1, 0, 1], shape=(n, n))
+    I = _sp.identity(n)
+    A = (_sp.kron(I, T) + _sp.kron(Ty, I) + main * _sp.identity(n * n)).tocsr()
+    A.sort_indices()
+    return CSR.from_scipy(A)
