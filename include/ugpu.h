@@ -62,6 +62,10 @@ extern "C" {
 #define UGPU_SOLVER_AMG 7         /* utopia::AlgebraicMultigrid with utopia::Agglomerate */
 #define UGPU_SOLVER_BICGSTAB 8    /* utopia::BiCGStab (utopia/solvers/smoothers/utopia_BiCGStab_impl.hpp:44-250); an
                                    * FP64 preconditioner is applied from a zero initial guess */
+#define UGPU_SOLVER_SSNEWTON 9    /* utopia::SemismoothNewton (quadratic_programming/utopia_SemismoothNewton_impl.hpp:
+                                   * 74-207); box constraints by ugpu_qp_set_box_constraints; the inner linear solver
+                                   * is BiCGStab + Jacobi to linear_rtol * ||residual|| unless one is set through
+                                   * ugpu_solver_set_preconditioner */
 
 /* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
 #define UGPU_CONVERGED_FNORM_ABS 2

@@ -88,6 +88,7 @@ def lib():
                 "or_pattern_grad": (None, [_vp, _vp, _vp, _vp]),
                 "or_agglomerate": (_vp, [_vp, _i64, _d, C.c_int, _vp]),
                 "or_bicgstab_solve": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _d, _i64, _vp]),
+                "or_ssn_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _d, _i64, _d, _vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -316,4 +317,19 @@ def bicgstab_solve(A: Matrix, b, x0=None, precond="none", mg=None, atol=1e-9, ma
     st = Status()
     kind = {"none": 0, "invdiag": 1, "mg": 2}[precond]
     lib().or_bicgstab_solve(A.h, _p(b), _p(x), kind, mg.h if mg is not None else None, atol, max_it, C.byref(st))
+    return x, st.as_dict()
+
+
+def ssn_solve(A: Matrix, b, lb=None, ub=None, x0=None, stol=1e-11, max_it=1000, linear_rtol=1e-12):
+    """SemismoothNewton (utopia_SemismoothNewton_impl.hpp:74-207) with BiCGStab + InvDiag inner solves;
+    returns x, status, and the final active set."""
+    b = _f64(b)
+    x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+    lbp = _p(_f64(lb)) if lb is not None else None
+    ubp = _p(_f64(ub)) if ub is not None else None
+    keep = (_f64(lb) if lb is not None else None, _f64(ub) if ub is not None else None)
+    lbp = _p(keep[0]) if keep[0] is not None else None
+    ubp = _p(keep[1]) if keep[1] is not None else None
+    st = Status()
+    lib().or_ssn_solve(A.h, _p(b), lbp, ubp, _p(x), stol, max_it, linear_rtol, C.byref(st))
     return x, st.as_dict()

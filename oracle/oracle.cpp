@@ -1203,6 +1203,67 @@ int or_cg_solve(const void *hA, const double *b, double *x, int precond, void *m
     return flexible ? fcg(A, b, x, *h->pc(), p, *st) : pcg(A, b, x, *h->pc(), p, *st);
 }
 
+// SemismoothNewton, utopia/solvers/nonlinear/constrained/quadratic_programming/utopia_SemismoothNewton_impl.hpp:74-207.
+// Inner solves: BiCGStab + InvDiag of the active-row-replaced matrix to linear_rtol * ||residual||.
+int or_ssn_solve(const void *hA, const double *b, const double *lb_in, const double *ub_in, double *x, double stol,
+                 int64_t max_it, double linear_rtol, or_status *st) {
+    const Csr &A = *static_cast<const Csr *>(hA);
+    const int64_t n = A.n;
+    std::vector<double> lb(n), ub(n), res(n), lam(n, 0.0), active(n, 0.0), c(n);
+    for (int64_t i = 0; i < n; ++i) {
+        lb[i] = lb_in ? lb_in[i] : -std::numeric_limits<double>::max();
+        ub[i] = ub_in ? ub_in[i] : std::numeric_limits<double>::max();
+    }
+    Params p;
+    p.stol = stol;
+    p.max_it = max_it;
+    *st = or_status{};
+    residual(A, b, x, res.data());
+    Csr mat = A;
+    int64_t it = 0, lin_its = 0;
+    bool converged = false;
+    while (!converged) {
+        int64_t changed = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const bool prev = active[i] != 0.0;
+            const double d_lb = x[i] + lam[i] - lb[i];
+            const double d_ub = x[i] + lam[i] - ub[i];
+            const bool alb = d_lb <= 0.0, aub = d_ub >= 0.0;
+            const bool act = alb || aub;
+            res[i] = alb ? (lb[i] - x[i]) : (aub ? (ub[i] - x[i]) : res[i]);
+            active[i] = act ? 1.0 : 0.0;
+            changed += (prev != act);
+        }
+        for (int64_t i = 0; i < n; ++i)
+            for (int32_t k = A.rp[i]; k < A.rp[i + 1]; ++k)
+                mat.v[k] = active[i] != 0.0 ? (A.ci[k] == i ? 1.0 : 0.0) : A.v[k];
+        std::fill(c.begin(), c.end(), 0.0);
+        Params lp;
+        lp.atol = linear_rtol * norm2(n, res.data());
+        lp.max_it = 10000;
+        InvDiag M(mat);
+        or_status lst{};
+        if (!bicgstab(mat, res.data(), c.data(), &M, lp, lst)) return 0;
+        lin_its += lst.iterates;
+        for (int64_t i = 0; i < n; ++i) x[i] += c[i];
+        const double norm_c = norm2(n, c.data());
+        ++it;
+        if (it > 1 && !changed) {
+            converged = true;
+            st->iterates = it;
+            st->step_norm = norm_c;
+            st->reason = CONVERGED_SNORM_RELATIVE;
+        } else {
+            converged = check_convergence(p, *st, it, 1, 1, norm_c);
+        }
+        residual(A, b, x, res.data());
+        for (int64_t i = 0; i < n; ++i) lam[i] = active[i] * res[i];
+    }
+    st->converged = st->reason > 0;
+    st->spmv_count = lin_its;
+    return st->converged;
+}
+
 int or_bicgstab_solve(const void *hA, const double *b, double *x, int precond, void *mg, double atol, int64_t max_it,
                       or_status *st) {
     const Csr &A = *static_cast<const Csr *>(hA);

@@ -100,3 +100,27 @@ def test_pgs_and_mprgp_agree_on_the_active_set(ctx, oracle):
     assert oracle.projected_gradient_norm(Am, b, lb, ub, xg) <= 1e-9
     # same contact set away from the free boundary's rounding band
     assert (np.abs(xg - lb) < 1e-12).sum() == pytest.approx((np.abs(xm - lb) < 1e-12).sum(), abs=2)
+
+
+def test_semismooth_newton_matches_oracle(ctx, oracle):
+    """SemismoothNewton (utopia_SemismoothNewton_impl.hpp:74-207) through the C ABI on the scaled
+    obstacle QP (128^2): same Newton iterations, same final active set and the same minimiser as
+    the oracle's restatement, and the MPRGP minimiser."""
+    N = 128
+    h = 1.0 / (N + 1)
+    A, b, lb, ub = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    s = U.SemismoothNewton(ctx, stol=1e-13, max_it=100)
+    lbv = U.Vector(ctx, lb)
+    s.set_box_constraints(lbv, None)
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    st = s.solution_status()
+    xg = x.numpy()
+    Am = oracle.Matrix(A)
+    xr, ost = oracle.ssn_solve(Am, b, lb=lb, stol=1e-13, max_it=100)
+    assert st["converged"] and ost["converged"]
+    assert st["iterates"] == ost["iterates"]
+    np.testing.assert_array_equal(xg <= lb + 1e-12, xr <= lb + 1e-12)
+    assert np.linalg.norm(xg - xr) <= 1e-9 * np.linalg.norm(xr)
+    xm, _ = oracle.mprgp_solve(Am, b, lb, ub, atol=1e-12, max_it=50000)
+    assert np.linalg.norm(xg - xm) <= 1e-6 * np.linalg.norm(xm)

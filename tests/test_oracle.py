@@ -226,3 +226,18 @@ def test_oracle_bicgstab_solves_nonsymmetric_systems(oracle):
         assert st["converged"], (pc, st)
         assert np.linalg.norm(b - A.matvec(x)) <= atol * 1.0001
         assert np.linalg.norm(x - xd) <= 1e-8 * np.linalg.norm(xd)
+
+
+def test_oracle_semismooth_newton_matches_mprgp(oracle):
+    """SemismoothNewton restatement (utopia_SemismoothNewton_impl.hpp:74-207) and the MPRGP
+    restatement reach the same minimiser of the scaled obstacle QP (unique: A is SPD)."""
+    N = 40
+    h = 1.0 / (N + 1)
+    A, b, lb, ub = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    Am = oracle.Matrix(A)
+    x, st = oracle.ssn_solve(Am, b, lb=lb, ub=None, stol=1e-13, max_it=100)
+    assert st["converged"] and st["iterates"] < 30
+    xm, stm = oracle.mprgp_solve(Am, b, lb, ub, atol=1e-12, max_it=20000)
+    assert stm["converged"]
+    assert np.linalg.norm(x - xm) <= 1e-6 * np.linalg.norm(xm)
+    assert np.all(x >= lb - 1e-12)

@@ -451,6 +451,17 @@ class _QPSolver(_Solver):
                                                                 ub.h if ub is not None else None))
 
 
+class SemismoothNewton(_QPSolver):
+    """utopia::SemismoothNewton (primal-dual active set); set_linear_solver replaces the default
+    inner BiCGStab + Jacobi."""
+
+    KIND = _abi.SOLVER_SSNEWTON
+
+    def set_linear_solver(self, solver):
+        self._linear = solver
+        self.ctx.check(self.ctx.lib.ugpu_solver_set_preconditioner(self.h, solver.h))
+
+
 class MPRGP(_QPSolver):
     KIND = _abi.SOLVER_MPRGP
 

@@ -21,6 +21,7 @@ FORMAT_CSR, FORMAT_SELL = 0, 1
 SOLVER_CG, SOLVER_MULTIGRID, SOLVER_INVDIAG, SOLVER_MPRGP, SOLVER_PGS, SOLVER_CHOLESKY = 1, 2, 3, 4, 5, 6
 SOLVER_AMG = 7
 SOLVER_BICGSTAB = 8
+SOLVER_SSNEWTON = 9
 
 _lock = threading.Lock()
 _lib = None

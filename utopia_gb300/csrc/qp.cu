@@ -757,6 +757,171 @@ private:
     }
 };
 
+// ======================================================================================
+// SemismoothNewton (utopia/solvers/nonlinear/constrained/quadratic_programming/
+// utopia_SemismoothNewton_impl.hpp:74-207): primal-dual active-set Newton for
+// min 1/2 x'Ax - b'x, lb <= x <= ub.  Per iteration: d_lb = x + lambda - lb, d_ub = x + lambda - ub;
+// i is active at the lower (upper) bound when d_lb <= 0 (d_ub >= 0), its residual entry becomes
+// lb_i - x_i (ub_i - x_i) and its row of A the identity row (set_zero_rows(mat, active, 1));
+// solve mat c = residual, x += c; stop when the active set repeats (after the first
+// iteration) or on ||c|| <= stol / max_it; residual = b - A x, lambda = active .* residual.
+// The inner solver defaults to BiCGStab + Jacobi (the active rows make mat nonsymmetric), run
+// to ||r|| <= linear_rtol * ||residual||; a caller-set solver (set_preconditioner slot) replaces it.
+namespace {
+
+__global__ void k_ssn_active(int64_t n, const double *__restrict__ x, const double *__restrict__ lam,
+                             const double *__restrict__ lb, const double *__restrict__ ub, double *__restrict__ res,
+                             double *__restrict__ active, int *changed) {
+    int cnt = 0;
+    QP_LOOP(i, n) {
+        const bool prev = active[i] != 0.0;
+        const double d_lb = x[i] + lam[i] - lb[i];
+        const double d_ub = x[i] + lam[i] - ub[i];
+        const bool alb = d_lb <= 0.0, aub = d_ub >= 0.0;
+        const bool act = alb || aub;
+        res[i] = alb ? (lb[i] - x[i]) : (aub ? (ub[i] - x[i]) : res[i]);
+        active[i] = act ? 1.0 : 0.0;
+        cnt += (prev != act);
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(changed, cnt);
+}
+
+__global__ void k_ssn_rows(int64_t n, const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                           const double *__restrict__ a, const double *__restrict__ active, double *__restrict__ out) {
+    QP_LOOP(i, n) {
+        const bool act = active[i] != 0.0;
+        for (int32_t k = rp[i]; k < rp[i + 1]; ++k) out[k] = act ? (ci[k] == i ? 1.0 : 0.0) : a[k];
+    }
+}
+
+__global__ void k_ssn_lambda(int64_t n, const double *__restrict__ active, const double *__restrict__ res,
+                             double *__restrict__ lam) {
+    QP_LOOP(i, n) lam[i] = active[i] * res[i];
+}
+
+}  // namespace
+
+class SemismoothNewton final : public QpBase {
+public:
+    explicit SemismoothNewton(Context *c) : QpBase(c, UGPU_SOLVER_SSNEWTON) {
+        prm["linear_rtol"] = 1e-12;
+        prm["linear_max_it"] = 10000;
+    }
+
+    void set_preconditioner(Solver *s) override { user_linear_ = s; }
+
+    void update(const Mat *A) override {
+        UGPU_CHECK(A && A->nrows == A->ncols && A->vdtype == UGPU_F64, UGPU_ERR_ARG,
+                   "SemismoothNewton: square FP64 operator required");
+        op = A;
+        mat_ = cast_matrix(*A, UGPU_F64);  // details_->mat = *op
+        const size_t b = sizeof(double) * size_t(std::max<int64_t>(A->nrows, 1));
+        for (Buffer *w : {&res_, &lam_, &active_, &corr_}) w->alloc(b);
+        changed_.alloc(sizeof(int));
+        if (!user_linear_ && !linear_) {
+            linear_ = make_bicgstab(ctx);
+            jacobi_ = make_invdiag(ctx);
+            linear_->set_preconditioner(jacobi_.get());
+        }
+    }
+
+    void apply(const Vec &bv, Vec &xv) override {
+        UGPU_CHECK(op, UGPU_ERR_STATE, "SemismoothNewton: update() first");
+        const int64_t n = op->nrows;
+        UGPU_CHECK(bv.n == n && xv.n == n && bv.dtype == UGPU_F64 && xv.dtype == UGPU_F64, UGPU_ERR_ARG,
+                   "SemismoothNewton: FP64 vectors of the operator's size required");
+        const double t0 = now_s();
+        const int64_t l0 = ctx->launches;
+        st = ugpu_solution_status{};
+        const double *lb, *ub;
+        bounds(n, &lb, &ub);
+        double *x = xv.as<double>(), *res = res_.as<double>(), *lam = lam_.as<double>();
+        double *act = active_.as<double>(), *c = corr_.as<double>();
+        Solver *lin = user_linear_ ? user_linear_ : linear_.get();
+        const int g = stream_grid(*ctx, n);
+        auto residual = [&]() {  // res = b - A x
+            SpmvArgs a;
+            a.x = x;
+            a.v = bv.data();
+            a.y = res;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_RESIDUAL;
+            launch_spmv(*ctx, *op, a);
+        };
+        auto norm = [&](const double *v) {
+            DotArgs d{};
+            d.a[0] = d.b[0] = v;
+            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
+            d.nd = 1;
+            double o = 0;
+            host_dots(*ctx, n, d, &o);
+            return std::sqrt(o);
+        };
+        enq_set(*ctx, UGPU_F64, n, 0.0, lam, nullptr);
+        enq_set(*ctx, UGPU_F64, n, 0.0, act, nullptr);  // Details::init: active zeroed
+        residual();
+        int64_t it = 0, lin_its = 0;
+        bool converged = false;
+        double norm_c = 0;
+        Vec rv, cv;
+        rv.ctx = cv.ctx = ctx;
+        rv.n = cv.n = n;
+        rv.dtype = cv.dtype = UGPU_F64;
+        rv.buf.borrow(res, sizeof(double) * size_t(n));
+        cv.buf.borrow(c, sizeof(double) * size_t(n));
+        while (!converged) {
+            UGPU_CUDA(cudaMemsetAsync(changed_.ptr, 0, sizeof(int), ctx->stream));
+            k_ssn_active<<<g, kBlock, 0, ctx->stream>>>(n, x, lam, lb, ub, res, act, changed_.as<int>());
+            k_ssn_rows<<<g, kBlock, 0, ctx->stream>>>(n, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
+                                                      op->vals.as<double>(), act, mat_->vals.as<double>());
+            ctx->launches += 2;
+            UGPU_LAUNCH_CHECK();
+            int changed = 0;
+            UGPU_CUDA(cudaMemcpyAsync(&changed, changed_.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+            mat_->has_diag = false;
+            finalize_matrix(*mat_);  // new values: refresh the sliced-ELL copy
+            enq_set(*ctx, UGPU_F64, n, 0.0, c, nullptr);
+            if (!user_linear_) {
+                lin->set("atol", get("linear_rtol") * norm(res));
+                lin->set("max_it", get("linear_max_it"));
+            }
+            lin->update(mat_.get());
+            lin->apply(rv, cv);
+            lin_its += lin->st.iterates;
+            UGPU_CHECK(lin->st.converged, UGPU_ERR_INTERNAL,
+                       "SemismoothNewton: unable to solve the linear system for the subgradient");
+            enq_axpy(*ctx, UGPU_F64, n, 1.0, c, x, nullptr);  // x += correction
+            norm_c = norm(c);
+            ++it;
+            if (it > 1 && !changed) {
+                converged = true;
+                st.iterates = it;
+                st.step_norm = norm_c;
+                st.reason = UGPU_CONVERGED_SNORM_RELATIVE;
+            } else {
+                converged = check_convergence(it, 1, 1, norm_c);
+            }
+            residual();
+            k_ssn_lambda<<<g, kBlock, 0, ctx->stream>>>(n, act, res, lam);
+            ctx->launches++;
+        }
+        UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        st.converged = st.reason > 0 ? 1 : 0;
+        st.spmv_count = lin_its;  // inner iterations
+        st.execution_time = now_s() - t0;
+        st.kernel_launches = ctx->launches - l0;
+    }
+
+private:
+    std::unique_ptr<Mat> mat_;
+    Buffer res_, lam_, active_, corr_, changed_;
+    Solver *user_linear_ = nullptr;
+    std::unique_ptr<Solver> linear_, jacobi_;
+};
+
+std::unique_ptr<Solver> make_ssnewton(Context *c) { return std::make_unique<SemismoothNewton>(c); }
+
 std::unique_ptr<Solver> make_mprgp(Context *c) { return std::make_unique<Mprgp>(c); }
 std::unique_ptr<Solver> make_pgs(Context *c) { return std::make_unique<Pgs>(c); }
 

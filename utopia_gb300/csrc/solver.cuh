@@ -109,6 +109,7 @@ std::unique_ptr<Solver> make_mprgp(Context *c);
 std::unique_ptr<Solver> make_pgs(Context *c);
 std::unique_ptr<Solver> make_amg(Context *c);
 std::unique_ptr<Solver> make_bicgstab(Context *c);
+std::unique_ptr<Solver> make_ssnewton(Context *c);
 // the multigrid inside an algebraic multigrid solver (any other solver: itself)
 const Solver *amg_multigrid(const Solver *s);
 

@@ -53,6 +53,7 @@ int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out) {
         case UGPU_SOLVER_CHOLESKY: s->impl = make_cholesky(c); break;
         case UGPU_SOLVER_AMG: s->impl = make_amg(c); break;
         case UGPU_SOLVER_BICGSTAB: s->impl = make_bicgstab(c); break;
+        case UGPU_SOLVER_SSNEWTON: s->impl = make_ssnewton(c); break;
         default: throw Error(UGPU_ERR_ARG, "unknown solver kind");
     }
     *out = s.release();
