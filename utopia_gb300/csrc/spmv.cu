@@ -620,6 +620,7 @@ constexpr int kStagedWarps = 4;      // warps per CTA
 constexpr int kStagedMaxStages = 4;
 constexpr int kStagedGap = 16;       // offsets at most this far apart share one x window
 constexpr int kStagedXBudget = 2048; // most x-window floats per slice that are staged
+constexpr int kStagedMinWarps = 8;   // fewest resident warps per SM the staged kernel runs with
 constexpr bool kStagedGlobalX = false;  // run operators with wider windows here (x through the caches)
 constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[32], xb[32]
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
@@ -1189,7 +1190,11 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
             best_per_sm = per_sm;
         }
     }
+    // a large operator with too few resident warps to hide the per-slice latency chain: the
+    // register kernel (up to 64 warps per SM) does better; small operators keep the deep
+    // prefetch of the ring
     if (best_nst == 0) return false;
+    if (best_per_sm * kStagedWarps < kStagedMinWarps && s.nslices >= 16 * int64_t(ctx.sms)) return false;
     c.nst = best_nst;
     c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
     const uint32_t cta = kStagedWarps * c.warp_bytes;
@@ -1243,10 +1248,10 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
                       (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0) {
             if (staged_launch<V, EPI, XM>(ctx, A, a)) return;
         }
-        // transfer-like operators (not all slices diagonal) with fewer slices than resident
-        // warps: in the register kernel one lane per row would serialize each long row's
-        // gathers, so the CSR kernel (several lanes per row) runs them
-        const bool few = A.sell->ndiag_slices < A.sell->nslices && A.sell->nslices < int64_t(ctx.sms) * kSpmvWarps;
+        // transfer-like operators (not all slices diagonal) with fewer than two slices per SM: in
+        // the register kernel one lane per row would serialize each long row's gathers over too
+        // few warps, so the CSR kernel (several lanes per row) runs them
+        const bool few = A.sell->ndiag_slices < A.sell->nslices && A.sell->nslices < int64_t(ctx.sms) * 2;
         if (few) csr_launch<V, T, EPI, XM, DOT>(ctx, A, a);
         else sell_launch<V, T, R, EPI, XM, DOT>(ctx, A, a);
     }
