@@ -89,6 +89,9 @@ def lib():
                 "or_agglomerate": (_vp, [_vp, _i64, _d, C.c_int, _vp]),
                 "or_bicgstab_solve": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _d, _i64, _vp]),
                 "or_ssn_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _d, _i64, _d, _vp]),
+                "or_mmg_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int,
+                                           C.c_int, C.c_int, C.c_int, _d, _d, C.c_int, _d, _d, _d, _i64, _vp,
+                                           _vp, _vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -333,3 +336,34 @@ def ssn_solve(A: Matrix, b, lb=None, ub=None, x0=None, stol=1e-11, max_it=1000, 
     st = Status()
     lib().or_ssn_solve(A.h, _p(b), lbp, ubp, _p(x), stol, max_it, linear_rtol, C.byref(st))
     return x, st.as_dict()
+
+
+def monotone_mg_solve(A: Matrix, b, lb, ub, P_coarse_to_fine, x0=None, colour=None, pre=3, post=3,
+                      n_local_sweeps=3, symmetric=True, smoother="chebyshev", omega=1.0, active_tol=0.0,
+                      coarse_space_it=1, atol=1e-9, rtol=1e-9, stol=1e-11, max_it=1000):
+    """MonotoneMultigrid (utopia_MonotoneMultigrid.hpp:135-319): PGS smoothing on the fine level
+    (in the sweep order of `colour`, lexicographic when None), the interpolation of the last
+    transfer truncated on the active set, a linear multigrid (fix_semidefinite, no masks) on the
+    truncated Galerkin operator.  Returns x, status, the final active set and the last coarse
+    operator."""
+    b = _f64(b)
+    x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+    keep = (_f64(lb) if lb is not None else None, _f64(ub) if ub is not None else None)
+    lbp = _p(keep[0]) if keep[0] is not None else None
+    ubp = _p(keep[1]) if keep[1] is not None else None
+    Ps = [p if isinstance(p, Matrix) else Matrix(p) for p in P_coarse_to_fine]
+    arr = (C.c_void_p * len(Ps))(*[p.h for p in Ps])
+    if colour is not None:
+        colour = np.ascontiguousarray(colour, dtype=np.int32)
+        nc, cp = int(colour.max()) + 1, _p(colour)
+    else:
+        nc, cp = 0, None
+    st = Status()
+    active = np.zeros(b.size, np.int32)
+    coarse = C.c_void_p()
+    rc = lib().or_mmg_solve(A.h, _p(b), lbp, ubp, _p(x), len(Ps), C.cast(arr, C.c_void_p), cp, nc, pre, post,
+                            n_local_sweeps, int(symmetric), SMOOTHERS[smoother], omega, active_tol,
+                            coarse_space_it, atol, rtol, stol, max_it, C.byref(st), _p(active), C.byref(coarse))
+    if rc < 0:
+        raise RuntimeError("oracle monotone multigrid: coarse operator not SPD")
+    return x, st.as_dict(), active, Matrix(_handle=coarse.value)

@@ -1264,6 +1264,126 @@ int or_ssn_solve(const void *hA, const double *b, const double *lb_in, const dou
     return st->converged;
 }
 
+// MonotoneMultigrid::update/apply/step (utopia/solvers/multilevel/utopia_MonotoneMultigrid.hpp:135-319):
+// pre_smoothing_steps projected Gauss-Seidel steps on the fine level, the active set of
+// ActiveSet::determine (utopia/solvers/nonlinear/constrained/utopia_ActiveSet.hpp:47-84:
+// x_i <= lb_i + tol or x_i >= ub_i - tol), on a change IPTruncatedTransfer::truncate_interpolation
+// (utopia/solvers/multilevel/transfer/utopia_IPTruncatedTransfer.hpp:203-223: the fine transfer
+// with the active rows zeroed, structure kept) and galerkin_assembly (:212-227: P_t^T A P_t,
+// fix_semidefinite_operator, the linear multigrid rebuilt below it), the coarse correction
+// x += P_t MG(P_t^T (b - A x)) with coarse_space_it cycles of the linear multigrid (or the
+// direct solve when there is only the fine transfer), then post_smoothing_steps PGS steps.
+// Stop test check_convergence(it, ||P(x - g) - x||, 1, ||x - x_old||) for it = 1 .. max_it-1
+// (criticality_measure_inf, :348-364; ||g|| when a bound is missing).
+// P: interpolations coarse -> fine, the last one the fine-level (truncated) transfer.
+// colour/ncolours: the PGS sweep order (nullptr = lexicographic).  active_out: the final
+// active set; coarse_out (optional): a copy of the last truncated coarse operator.
+int or_mmg_solve(const void *hA, const double *b, const double *lb_in, const double *ub_in, double *x, int nP,
+                 const void *const *hP, const int32_t *colour, int ncolours, int pre, int post, int n_local_sweeps,
+                 int symmetric, int smoother, double omega, double active_tol, int coarse_space_it, double atol,
+                 double rtol, double stol, int64_t max_it, or_status *st, int32_t *active_out, void **coarse_out) {
+    const Csr &A = *static_cast<const Csr *>(hA);
+    const int64_t n = A.n;
+    if (nP < 1) return -1;
+    const Csr &I = *static_cast<const Csr *>(hP[nP - 1]);
+    std::vector<Csr> rest;
+    for (int i = 0; i + 1 < nP; ++i) rest.push_back(*static_cast<const Csr *>(hP[i]));
+    const bool both = lb_in && ub_in;
+    std::vector<double> lb(n), ub(n);
+    for (int64_t i = 0; i < n; ++i) {
+        lb[i] = lb_in ? lb_in[i] : -std::numeric_limits<double>::max();
+        ub[i] = ub_in ? ub_in[i] : std::numeric_limits<double>::max();
+    }
+    std::vector<double> dinv = diag(A), r(n), c(n), ubl(n), lbl(n), xold(x, x + n), help(n);
+    for (auto &v : dinv) v = 1. / v;
+    std::vector<int32_t> active(n, 0);
+    Csr It = I;  // truncated transfer (I itself until the first change of the active set)
+    Csr AH;
+    Cholesky chol;
+    std::unique_ptr<Mg<double, double>> mg;
+    MgOptions mo;
+    mo.smoother = smoother;
+    mo.pre = pre;
+    mo.post = post;
+    mo.omega = omega;
+    mo.fix_semidefinite = 1;  // MonotoneMultigrid(): algo_.fix_semidefinite_operators(true)
+    mo.masks = 0;             // algo_.must_generate_masks(false)
+    auto galerkin = [&]() -> bool {
+        AH = ptap(A, It);
+        Mg<double, double>::fix_semidefinite(AH);
+        if (rest.empty()) return chol.factor(AH);
+        mg.reset(new Mg<double, double>);
+        return mg->build(AH, rest, mo);
+    };
+    if (!galerkin()) return -2;
+    const int64_t nc = I.m;
+    std::vector<double> rc(nc), cc(nc);
+    Params p;
+    p.atol = atol;
+    p.rtol = rtol;
+    p.stol = stol;
+    p.max_it = max_it;
+    *st = or_status{};
+    auto smooth = [&](int sweeps) {
+        for (int s = 0; s < sweeps; ++s)
+            pgs_step(A, b, lb.data(), ub.data(), x, dinv.data(), n_local_sweeps, symmetric != 0, colour, ncolours, r,
+                     c, ubl, lbl);
+    };
+    auto measure = [&]() {  // r = b - A x = -g; ||P(x - g) - x|| or ||g||
+        residual(A, b, x, r.data());
+        if (!both) return norm2(n, r.data());
+        for (int64_t i = 0; i < n; ++i) help[i] = proj(lb[i], ub[i], x[i] + r[i]) - x[i];
+        return norm2(n, help.data());
+    };
+    double g_norm = measure();
+    bool converged = false;
+    int64_t it = 1;
+    for (; it < max_it && !converged; ++it) {
+        smooth(pre);
+        int64_t changed = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            const int a = (x[i] <= lb[i] + active_tol || x[i] >= ub[i] - active_tol) ? 1 : 0;
+            changed += (a != active[i]);
+            active[i] = a;
+        }
+        if (changed) {
+            for (int64_t i = 0; i < n; ++i)
+                for (int32_t k = I.rp[i]; k < I.rp[i + 1]; ++k) It.v[k] = active[i] ? 0.0 : I.v[k];
+            if (!galerkin()) return -2;
+        }
+        residual(A, b, x, r.data());
+        Csr Rt = transpose(It);
+        spmv(Rt, r.data(), rc.data());
+        std::fill(cc.begin(), cc.end(), 0.0);
+        if (rest.empty()) {
+            chol.solve(rc.data(), cc.data());
+        } else {
+            Params cp;  // algo_.max_it(coarse_space_it); algo_.apply(r_coarse, c_coarse)
+            cp.max_it = coarse_space_it;
+            or_status cst{};
+            mg->solve(rc.data(), cc.data(), cp, cst);
+        }
+        std::vector<double> corr(n);
+        spmv(It, cc.data(), corr.data());
+        for (int64_t i = 0; i < n; ++i) x[i] += corr[i];
+        smooth(post);
+        for (int64_t i = 0; i < n; ++i) help[i] = x[i] - xold[i];
+        const double x_diff = norm2(n, help.data());
+        g_norm = measure();
+        converged = check_convergence(p, *st, it, g_norm, 1, x_diff);
+        if (!converged) std::copy(x, x + n, xold.begin());
+    }
+    if (!converged) {  // the loop ran out at it == max_it without a test that says so
+        st->iterates = max_it - 1;
+        st->gradient_norm = g_norm;
+        st->reason = DIVERGED_MAX_IT;
+    }
+    st->converged = st->reason > 0;
+    if (active_out) std::copy(active.begin(), active.end(), active_out);
+    if (coarse_out) *coarse_out = new Csr(AH);
+    return st->converged;
+}
+
 int or_bicgstab_solve(const void *hA, const double *b, double *x, int precond, void *mg, double atol, int64_t max_it,
                       or_status *st) {
     const Csr &A = *static_cast<const Csr *>(hA);

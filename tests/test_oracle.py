@@ -241,3 +241,27 @@ def test_oracle_semismooth_newton_matches_mprgp(oracle):
     assert stm["converged"]
     assert np.linalg.norm(x - xm) <= 1e-6 * np.linalg.norm(xm)
     assert np.all(x >= lb - 1e-12)
+
+
+def test_oracle_monotone_multigrid_reference_1d_case(oracle):
+    """MonotoneMultigrid restatement (utopia_MonotoneMultigrid.hpp:135-319) on the case of
+    utopia/tests/utopia_QPSolverTest.cpp:715-771 (1D Poisson obstacle problem, 6 levels from 50
+    coarse elements, lower bound -0.8, 5 + 5 PGS steps, active-set tol 1e-15, max_it 40): it
+    converges, in the reference's lexicographic order and in the multicolour order, to the
+    minimiser the semismooth Newton restatement finds, with the same active set."""
+    H, g, lb, ub, Ps = P.poisson1d_obstacle_multilevel()
+    A = oracle.Matrix(H)
+    xs, sst = oracle.ssn_solve(A, g, lb, ub, stol=1e-14)
+    assert sst["converged"]
+    act_ref = (xs <= lb + 1e-9) | (xs >= ub - 1e-9)
+    for colour in (None, oracle.colouring(A)[0]):
+        x, st, act, AH = oracle.monotone_mg_solve(A, g, lb, ub, Ps, colour=colour, pre=5, post=5, max_it=40,
+                                                  active_tol=1e-15)
+        assert st["converged"] and st["iterates"] < 30, st
+        assert np.abs(x - xs).max() < 1e-9
+        np.testing.assert_array_equal(act.astype(bool), act_ref)
+        # the truncated coarse operator: coarse nodes whose fine support is all active are
+        # decoupled identity rows (fix_semidefinite_operator)
+        rp, ci, v = AH.arrays()
+        d = np.array([v[rp[i]:rp[i + 1]][ci[rp[i]:rp[i + 1]] == i].sum() for i in range(AH.nrows)])
+        assert np.all(d > 0) and (d == 1.0).sum() > 0

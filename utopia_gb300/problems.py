@@ -401,3 +401,49 @@ def convection_diffusion_2d(n: int, peclet: float = 20.0) -> CSR:
     A = (_sp.kron(I, T) + _sp.kron(Ty, I) + main * _sp.identity(n * n)).tocsr()
     A.sort_indices()
     return CSR.from_scipy(A)
+
+
+def poisson1d_obstacle_multilevel(n_levels: int = 6, n_coarse_elements: int = 50, lower: float = -0.8,
+                                  upper: float = 200.0):
+    """The monotone multigrid case of utopia/tests/utopia_QPSolverTest.cpp:715-771 on the problem of
+    MultiLevelTestProblem1D<Poisson1D> (utopia/tests/test_problems/large_scale_benchmark/
+    utopia_MultilevelTestProblem1D.hpp:61-150, utopia_Poisson1D.hpp problem type 2):
+
+    * level sizes n_0 = n_coarse_elements + 1, n_{l+1} = 2 (n_l - 1) + 1;
+    * interpolation n_l -> n_{l+1}: fine row 2j takes coarse j with weight 1, fine row 2j+1 takes
+      coarse j and j+1 with weight 1/2; on the finest transfer (remove_bc) the entries (0, 0) and
+      (n-1, n_c-1) are zero (kept in the structure);
+    * H = (1/h) tridiag(-1, 2, -1) with rows 0 and n-1 replaced by identity rows, h = 1/(n-1);
+    * the right-hand side is the gradient at the boundary values (all zero): -10 h on the interior,
+      0 on the boundary; box lower <= x <= upper.
+
+    Returns (H, g, lb, ub, interpolations ordered coarse -> fine)."""
+    sizes = [n_coarse_elements + 1]
+    for _ in range(1, n_levels):
+        sizes.append((sizes[-1] - 1) * 2 + 1)
+    Ps = []
+    for i in range(n_levels - 1):
+        nc, nf = sizes[i], sizes[i + 1]
+        rows, cols, vals = [], [], []
+        for j in range(nc):
+            rows.append(2 * j); cols.append(j); vals.append(1.0)
+            if j + 1 < nc:
+                rows += [2 * j + 1, 2 * j + 1]; cols += [j, j + 1]; vals += [0.5, 0.5]
+        if i == n_levels - 2:
+            vals[0] = 0.0                                  # (0, 0)
+            last = [k for k in range(len(rows)) if rows[k] == nf - 1 and cols[k] == nc - 1][0]
+            vals[last] = 0.0                               # (n-1, n_c-1)
+        m = _sp.coo_matrix((vals, (rows, cols)), shape=(nf, nc)).tocsr()
+        m.sort_indices()
+        Ps.append(CSR(nf, nc, m.indptr, m.indices, m.data))
+    n = sizes[-1]
+    h = 1.0 / (n - 1)
+    rows, cols, vals = [0, n - 1], [0, n - 1], [1.0, 1.0]
+    for i in range(1, n - 1):
+        rows += [i, i, i]
+        cols += [i - 1, i, i + 1]
+        vals += [-1.0 / h, 2.0 / h, -1.0 / h]
+    H = CSR.from_scipy(_sp.csr_matrix((vals, (rows, cols)), shape=(n, n)))
+    g = np.full(n, -10.0 * h)
+    g[0] = g[-1] = 0.0
+    return H, g, np.full(n, lower), np.full(n, upper), Ps
