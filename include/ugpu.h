@@ -66,6 +66,10 @@ extern "C" {
                                    * 74-207); box constraints by ugpu_qp_set_box_constraints; the inner linear solver
                                    * is BiCGStab + Jacobi to linear_rtol * ||residual|| unless one is set through
                                    * ugpu_solver_set_preconditioner */
+#define UGPU_SOLVER_MONOTONE_MG 10 /* utopia::MonotoneMultigrid (utopia/solvers/multilevel/utopia_MonotoneMultigrid.hpp:
+                                   * 33-377): box constraints by ugpu_qp_set_box_constraints, interpolations by
+                                   * ugpu_mg_set_transfer_operators (coarse -> fine; the last one is the fine-level
+                                   * transfer truncated on the active set) */
 
 /* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
 #define UGPU_CONVERGED_FNORM_ABS 2
@@ -261,6 +265,15 @@ UGPU_API int ugpu_pgs_colouring(const ugpu_solver *pgs, int32_t *colour, int *nc
  * level shrinks by less than 4:3), bmax,
  * weight, use_additive_correction and every multigrid key; the ugpu_mg_* queries accept it. */
 UGPU_API int ugpu_amg_parent(const ugpu_solver *amg, int level, int32_t *parent, int64_t *n, int64_t *n_coarse);
+
+/* The monotone multigrid (UGPU_SOLVER_MONOTONE_MG): keys pre_smoothing_steps, post_smoothing_steps
+ * (PGS steps on the fine level and smoothing steps of the linear multigrid), n_local_sweeps,
+ * use_symmetric_sweep, smoother, omega, active_set_tol (ActiveSet tol), coarse_space_it,
+ * use_coarse_space; read-only galerkin_assemblies and n_active.  ugpu_mg_n_levels / ugpu_mg_level_matrix
+ * see the fine operator as the finest level and the truncated Galerkin operator below it.
+ * ugpu_mmg_active_set: the active-set indicator (ActiveSet::indicator, 0/1 per fine dof, n
+ * entries; may be NULL) and its size after the last update/apply. */
+UGPU_API int ugpu_mmg_active_set(const ugpu_solver *mmg, int32_t *indicator, int64_t *n_active);
 
 /* ---------------------------------------------------------------- files ---- */
 /* PETSc binary matrices and vectors (utopia::read / write over MatLoad / VecLoad, used for the

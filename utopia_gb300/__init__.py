@@ -466,6 +466,32 @@ class MPRGP(_QPSolver):
     KIND = _abi.SOLVER_MPRGP
 
 
+class MonotoneMultigrid(_QPSolver):
+    """utopia::MonotoneMultigrid: projected Gauss-Seidel on the fine level, the fine transfer
+    truncated on the active set, a linear multigrid (smoother "jacobi", "chebyshev" or
+    "point_jacobi") on the truncated Galerkin operator.  Interpolations are given coarse -> fine;
+    the last one is the fine-level transfer."""
+
+    KIND = _abi.SOLVER_MONOTONE_MG
+
+    def __init__(self, ctx, smoother="chebyshev", **params):
+        super().__init__(ctx, smoother=SMOOTHERS[smoother] if isinstance(smoother, str) else smoother, **params)
+
+    set_transfer_operators = Multigrid.set_transfer_operators
+    pre_smoothing_steps = Multigrid.pre_smoothing_steps
+    post_smoothing_steps = Multigrid.post_smoothing_steps
+    n_levels = Multigrid.n_levels
+    level_matrix = Multigrid.level_matrix
+
+    def active_set(self):
+        """ActiveSet::indicator after the last update/apply (0/1 per fine dof)."""
+        na = C.c_int64()
+        self.ctx.check(self.ctx.lib.ugpu_mmg_active_set(self.h, None, C.byref(na)))
+        out = np.empty(self._keep[-1].nrows, np.int32)
+        self.ctx.check(self.ctx.lib.ugpu_mmg_active_set(self.h, _ptr(out), None))
+        return out
+
+
 class ProjectedGaussSeidel(_QPSolver):
     KIND = _abi.SOLVER_PGS
 

@@ -22,6 +22,7 @@ SOLVER_CG, SOLVER_MULTIGRID, SOLVER_INVDIAG, SOLVER_MPRGP, SOLVER_PGS, SOLVER_CH
 SOLVER_AMG = 7
 SOLVER_BICGSTAB = 8
 SOLVER_SSNEWTON = 9
+SOLVER_MONOTONE_MG = 10
 
 _lock = threading.Lock()
 _lib = None
@@ -113,6 +114,7 @@ SIGNATURES = {
     "ugpu_project": [_vp, _vp, _vp],
     "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
     "ugpu_amg_parent": [_vp, _int, _vp, C.POINTER(_i64), C.POINTER(_i64)],
+    "ugpu_mmg_active_set": [_vp, _vp, C.POINTER(_i64)],
     "ugpu_petsc_read_mat": [_vp, C.c_char_p, _pp],
     "ugpu_petsc_read_vec": [_vp, C.c_char_p, _pp],
     "ugpu_petsc_write_mat": [_vp, C.c_char_p],

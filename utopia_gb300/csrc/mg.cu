@@ -187,13 +187,7 @@ public:
             UGPU_CHECK(t.P64->nrows == lev[i - 1].A64->nrows, UGPU_ERR_ARG,
                        "interpolation operator rows do not match the finer level");
             lev[i].A64own = ptap(*lev[i - 1].A64, *t.P64);
-            if (get("fix_semidefinite_operators") != 0) {
-                Mat &J = *lev[i].A64own;
-                k_fix_semidefinite<<<stream_grid(*ctx, J.nrows), kBlock, 0, ctx->stream>>>(
-                    J.rowptr.as<int32_t>(), J.colidx.as<int32_t>(), J.vals.as<double>(), J.nrows);
-                ctx->launches++;
-                finalize_matrix(J);
-            }
+            if (get("fix_semidefinite_operators") != 0) fix_semidefinite_operator(*ctx, *lev[i].A64own);
             lev[i].A64 = lev[i].A64own.get();
         }
         std::reverse(lev.begin(), lev.end());
@@ -595,13 +589,24 @@ private:
 
 std::unique_ptr<Solver> make_multigrid(Context *c) { return std::make_unique<Multigrid>(c); }
 
+void fix_semidefinite_operator(Context &ctx, Mat &J) {
+    UGPU_CHECK(J.vdtype == UGPU_F64, UGPU_ERR_ARG, "fix_semidefinite_operator: FP64 operator");
+    k_fix_semidefinite<<<stream_grid(ctx, J.nrows), kBlock, 0, ctx.stream>>>(
+        J.rowptr.as<int32_t>(), J.colidx.as<int32_t>(), J.vals.as<double>(), J.nrows);
+    ctx.launches++;
+    J.has_diag = false;
+    finalize_matrix(J);
+}
+
 int mg_n_levels(const Solver *s) {
+    if (int k = mmg_n_levels(s); k >= 0) return k;
     auto m = dynamic_cast<const Multigrid *>(amg_multigrid(s));
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     return m->n_levels();
 }
 
 std::unique_ptr<Mat> mg_level_matrix(const Solver *s, int l) {
+    if (auto M = mmg_level_matrix(s, l)) return M;
     auto m = dynamic_cast<const Multigrid *>(amg_multigrid(s));
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     UGPU_CHECK(l >= 0 && l < m->n_levels(), UGPU_ERR_ARG, "level out of range");
@@ -616,6 +621,7 @@ void mg_eigs(const Solver *s, int l, double *emax, double *emin) {
 }
 
 void mg_set_transfers(Solver *s, const std::vector<const Mat *> &P) {
+    if (mmg_set_transfers(s, P)) return;
     auto m = dynamic_cast<Multigrid *>(s);
     UGPU_CHECK(m, UGPU_ERR_ARG, "not a multigrid solver");
     m->set_transfers(P);

@@ -14,6 +14,7 @@
 // in order (then in reverse order for the symmetric sweep).  The colouring is the
 // greedy first-fit colouring in index order (red-black for the 5-point grid), computed
 // on the device by dependency rounds that reproduce the sequential result exactly.
+#include <climits>
 #include <cmath>
 
 #include "abi_util.cuh"
@@ -640,7 +641,7 @@ public:
         bounds(n, &lb, &ub);
         UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
         run_loop(loop_, key_, {x.data(), lb, ub, rhs.data()}, 0.0,
-                 [&] { step(rhs.as<double>(), x.as<double>(), lb, ub); }, &dev_.as<PgsDev>()->done, dev_, host_,
+                 [&] { step(rhs.as<double>(), x.as<double>(), lb, ub, false); }, &dev_.as<PgsDev>()->done, dev_, host_,
                  sizeof(PgsDev));
         st.iterates = host_->iterates;
         st.gradient_norm = host_->pgnorm;
@@ -651,6 +652,19 @@ public:
         st.spmv_count = host_->it;
         st.execution_time = now_s() - t0;
         st.kernel_launches = ctx->launches - l0;
+    }
+
+    // ProjectedGaussSeidel::smooth with bounds (utopia_ProjectedGaussSeidel.hpp:52-69): `sweeps`
+    // steps, no stopping test
+    void smooth(const Vec &rhs, Vec &x, int sweeps) override {
+        UGPU_CHECK(op, UGPU_ERR_STATE, "PGS: update() first");
+        const int64_t n = op->nrows;
+        UGPU_CHECK(rhs.n == n && x.n == n && rhs.dtype == UGPU_F64 && x.dtype == UGPU_F64, UGPU_ERR_ARG,
+                   "PGS: FP64 vectors of the operator size");
+        const double *lb, *ub;
+        bounds(n, &lb, &ub);
+        UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
+        for (int s = 0; s < sweeps; ++s) step(rhs.as<double>(), x.as<double>(), lb, ub, true);
     }
 
     std::vector<int32_t> download_colouring() const {
@@ -714,10 +728,11 @@ private:
     }
 
     // ProjectedGaussSeidel::step (utopia_ProjectedGaussSeidel.hpp:197-318), multicolour
-    void step(const double *b, double *x, const double *lb, const double *ub) {
+    // smoothing: no projected-gradient norm and no stopping test
+    void step(const double *b, double *x, const double *lb, const double *ub, bool smoothing) {
         const int64_t n = op->nrows;
         PgsDev *dev = dev_.as<PgsDev>();
-        const int pg_stop = get("projected_gradient_stop") != 0;
+        const int pg_stop = !smoothing && get("projected_gradient_stop") != 0;
         {   // r = b - A x
             SpmvArgs a;
             a.x = x;
@@ -728,10 +743,12 @@ private:
             a.done = &dev->done;
             launch_spmv(*ctx, *op, a);
         }
-        k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, r_.as<double>(), lb, ub, dev,
-                                                                 part_.as<double>(), cnt_.as<unsigned int>() + 0,
-                                                                 get("atol"), pg_stop);
-        ctx->launches++;
+        if (!smoothing) {
+            k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, r_.as<double>(), lb, ub, dev,
+                                                                     part_.as<double>(), cnt_.as<unsigned int>() + 0,
+                                                                     get("atol"), pg_stop);
+            ctx->launches++;
+        }
         enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
         const int sweeps = int(get("n_local_sweeps"));
         const bool sym = get("use_symmetric_sweep") != 0;
@@ -750,8 +767,10 @@ private:
         }
         k_pgs_finish<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, c_.as<double>(), dev,
                                                                  part_.as<double>() + kRedBlocks,
-                                                                 cnt_.as<unsigned int>() + 1, get("stol"),
-                                                                 (long long)get("max_it"), pg_stop);
+                                                                 cnt_.as<unsigned int>() + 1,
+                                                                 smoothing ? -1.0 : get("stol"),
+                                                                 smoothing ? LLONG_MAX : (long long)get("max_it"),
+                                                                 pg_stop);
         ctx->launches++;
         UGPU_LAUNCH_CHECK();
     }

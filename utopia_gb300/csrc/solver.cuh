@@ -60,6 +60,10 @@ struct Solver {
     virtual void set_box(const Vec *, const Vec *) {
         throw Error(UGPU_ERR_UNSUPPORTED, "this solver takes no box constraints");
     }
+    // Smoother::smooth with sweeps(s): s steps of the solver's iteration, no stopping test
+    virtual void smooth(const Vec & /*b*/, Vec & /*x*/, int /*sweeps*/) {
+        throw Error(UGPU_ERR_UNSUPPORTED, "this solver cannot be used as a smoother");
+    }
 
     // IterativeSolver::check_convergence (utopia_IterativeSolver.hpp:148-191), host form
     bool check_convergence(int64_t it, double g, double r, double s) {
@@ -110,6 +114,7 @@ std::unique_ptr<Solver> make_pgs(Context *c);
 std::unique_ptr<Solver> make_amg(Context *c);
 std::unique_ptr<Solver> make_bicgstab(Context *c);
 std::unique_ptr<Solver> make_ssnewton(Context *c);
+std::unique_ptr<Solver> make_monotone_mg(Context *c);
 // the multigrid inside an algebraic multigrid solver (any other solver: itself)
 const Solver *amg_multigrid(const Solver *s);
 
@@ -118,6 +123,12 @@ int mg_n_levels(const Solver *s);
 std::unique_ptr<Mat> mg_level_matrix(const Solver *s, int l);
 void mg_eigs(const Solver *s, int l, double *emax, double *emin);
 void mg_set_transfers(Solver *s, const std::vector<const Mat *> &P);
+// LinearMultiLevel::fix_semidefinite_operator: diagonal entries with |a_ii| < 1e-12 get +1
+void fix_semidefinite_operator(Context &ctx, Mat &J);
+// the monotone multigrid's counterparts (false / -1 / null: s is not a monotone multigrid)
+bool mmg_set_transfers(Solver *s, const std::vector<const Mat *> &P);
+int mmg_n_levels(const Solver *s);
+std::unique_ptr<Mat> mmg_level_matrix(const Solver *s, int l);
 
 inline double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
