@@ -276,8 +276,9 @@ void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);
 // ------------------------------------------------------------------------------------
 // SpGEMM / transpose (spgemm.cu), dense coarse solve (dense.cu)
 // ------------------------------------------------------------------------------------
-std::unique_ptr<Mat> transpose(const Mat &A);
-std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B);
+// finalize = false: CSR arrays only (no SpMV layout), for intermediates that only feed products
+std::unique_ptr<Mat> transpose(const Mat &A, bool finalize = true);
+std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize = true);
 std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P);
 std::unique_ptr<Mat> cast_matrix(const Mat &A, int vdtype);
 std::unique_ptr<Mat> make_csr_device(Context &ctx, int64_t nrows, int64_t ncols, int64_t nnz, int vdtype);

@@ -133,8 +133,10 @@ __global__ void k_sort_rows(const int64_t *tp, int64_t n, int32_t *tci, V *tcv) 
 // ------------------------------------------------------------------------------------
 // SpGEMM
 // ------------------------------------------------------------------------------------
+// per-row upper bound of the product's row length, and their maximum (one atomic per warp)
 __global__ void k_row_upper_bound(const int32_t *arp, const int32_t *aci, const int32_t *brp, int64_t m,
-                                  int64_t *ub) {
+                                  int64_t *ub, unsigned long long *max_ub) {
+    unsigned long long mx = 0;
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m; i += int64_t(gridDim.x) * blockDim.x) {
         int64_t s = 0;
         for (int32_t k = arp[i]; k < arp[i + 1]; ++k) {
@@ -142,7 +144,13 @@ __global__ void k_row_upper_bound(const int32_t *arp, const int32_t *aci, const 
             s += brp[j + 1] - brp[j];
         }
         ub[i] = s;
+        mx = s > int64_t(mx) ? (unsigned long long)s : mx;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, mx, o);
+        mx = v > mx ? v : mx;
+    }
+    if ((threadIdx.x & 31) == 0 && mx) atomicMax(max_ub, mx);
 }
 
 constexpr int kWarpTable = 2048;      // max slots per warp (rows with upper bound <= 1024)
@@ -240,31 +248,42 @@ __device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, do
 constexpr size_t kWarpSmem = (sizeof(int32_t) + sizeof(double)) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta;
 constexpr size_t kCtaSmem = (sizeof(int32_t) + sizeof(double)) * (kCtaTable + kCtaRowsUb);
 
-template <class V, bool NUMERIC>
-__global__ void __launch_bounds__(kWarpsPerCta * 32) k_spgemm_warp(int64_t m, const int64_t *ub, const int32_t *arp,
-                                                                   const int32_t *aci, const V *acv,
-                                                                   const int32_t *brp, const int32_t *bci,
-                                                                   const V *bcv, int64_t *cnt, const int32_t *crp,
-                                                                   int32_t *cci, V *ccv, int *big_rows,
-                                                                   int *n_big) {
+// Warp tiers: each warp takes whole rows whose upper bound u lies in (LO, ROWS_UB], with a
+// hash table of TABLE slots; the small tiers keep the shared memory per warp small so that
+// many warps share an SM (the typical Galerkin row has a few tens of products).  The last
+// warp tier lists the rows beyond it for the CTA kernels (symbolic phase).
+constexpr int kTier0Table = 64, kTier0Ub = 32, kTier0Warps = 8;
+constexpr int kTier1Table = 256, kTier1Ub = 128, kTier1Warps = 8;
+template <int TABLE, int ROWS_UB, int WARPS>
+constexpr size_t tier_smem() {
+    return (sizeof(int32_t) + sizeof(double)) * size_t(TABLE + ROWS_UB) * WARPS;
+}
+
+template <class V, bool NUMERIC, int TABLE, int ROWS_UB, int WARPS, bool APPEND>
+__global__ void __launch_bounds__(WARPS * 32) k_spgemm_warp(int64_t m, int64_t lo, const int64_t *ub,
+                                                            const int32_t *arp, const int32_t *aci, const V *acv,
+                                                            const int32_t *brp, const int32_t *bci, const V *bcv,
+                                                            int64_t *cnt, const int32_t *crp, int32_t *cci, V *ccv,
+                                                            int *big_rows, int *n_big) {
     extern __shared__ unsigned char smem[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    double *vals = reinterpret_cast<double *>(smem) + size_t(w) * kWarpTable;
-    double *lvals = reinterpret_cast<double *>(smem) + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
-    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta);
-    int32_t *keys = ibase + size_t(w) * kWarpTable;
-    int32_t *lkeys = ibase + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
-    __shared__ int s_count[kWarpsPerCta];
-    const int64_t gw = int64_t(blockIdx.x) * kWarpsPerCta + w;
-    const int64_t nw = int64_t(gridDim.x) * kWarpsPerCta;
+    double *vals = reinterpret_cast<double *>(smem) + size_t(w) * TABLE;
+    double *lvals = reinterpret_cast<double *>(smem) + size_t(WARPS) * TABLE + size_t(w) * ROWS_UB;
+    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (TABLE + ROWS_UB) * WARPS);
+    int32_t *keys = ibase + size_t(w) * TABLE;
+    int32_t *lkeys = ibase + size_t(WARPS) * TABLE + size_t(w) * ROWS_UB;
+    __shared__ int s_count[WARPS];
+    const int64_t gw = int64_t(blockIdx.x) * WARPS + w;
+    const int64_t nw = int64_t(gridDim.x) * WARPS;
     for (int64_t i = gw; i < m; i += nw) {
         const int64_t u = ub[i];
-        if (u > kWarpRowsUb) {
-            if (!NUMERIC && lane == 0) big_rows[atomicAdd(n_big, 1)] = int(i);
+        if (u <= lo) continue;
+        if (u > ROWS_UB) {
+            if (APPEND && !NUMERIC && lane == 0) big_rows[atomicAdd(n_big, 1)] = int(i);
             continue;
         }
-        row_product<V, NUMERIC, false>(i, lane, 32, table_size(u, kWarpTable), keys, vals, lkeys, lvals,
-                                       &s_count[w], arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+        row_product<V, NUMERIC, false>(i, lane, 32, table_size(u, TABLE), keys, vals, lkeys, lvals, &s_count[w],
+                                       arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
     }
 }
 
@@ -421,7 +440,7 @@ int64_t device_exclusive_scan(Context &ctx, const int64_t *in, int64_t *out, int
     return total;
 }
 
-std::unique_ptr<Mat> transpose(const Mat &A) {
+std::unique_ptr<Mat> transpose(const Mat &A, bool finalize) {
     Context &ctx = *A.ctx;
     Buffer cnt, tp64, fill;
     cnt.alloc(sizeof(int64_t) * std::max<int64_t>(A.ncols, 1));
@@ -458,11 +477,11 @@ std::unique_ptr<Mat> transpose(const Mat &A) {
     ctx.launches++;
     UGPU_LAUNCH_CHECK();
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
-    finalize_matrix(*T);
+    if (finalize) finalize_matrix(*T);
     return T;
 }
 
-std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
+std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize) {
     Context &ctx = *A.ctx;
     UGPU_CHECK(A.ncols == B.nrows, UGPU_ERR_ARG, "spgemm: inner dimensions differ");
     UGPU_CHECK(A.vdtype == UGPU_F64 && B.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "spgemm: FP64 operands");
@@ -472,16 +491,18 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
     cnt.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
     crp64.alloc(sizeof(int64_t) * (m + 1));
     big.alloc(sizeof(int) * std::max<int64_t>(m, 1));
-    nbig.alloc(sizeof(int));
+    nbig.alloc(sizeof(unsigned long long));  // the maximum upper bound, then the count of big rows
     UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
     const size_t warp_smem = kWarpSmem;
     const size_t cta_smem = kCtaSmem;
     static bool attr_done = false;
     if (!attr_done) {
-        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(warp_smem)));
-        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(
+            k_spgemm_warp<double, false, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(
+            k_spgemm_warp<double, true, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>,
+            cudaFuncAttributeMaxDynamicSharedMemorySize, int(warp_smem)));
         UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(cta_smem)));
         UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -495,31 +516,49 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
     const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
     const int32_t *brp = B.rowptr.as<int32_t>(), *bci = B.colidx.as<int32_t>();
     const double *acv = A.vals.as<double>(), *bcv = B.vals.as<double>();
-    if (m) {
-        k_row_upper_bound<<<stream_grid(ctx, m), kBlock, 0, ctx.stream>>>(arp, aci, brp, m, ub.as<int64_t>());
-        ctx.launches++;
-        UGPU_LAUNCH_CHECK();
-    }
     // largest per-row upper bound decides whether every row fits a shared-memory table
-    int64_t max_ub = 0;
-    {
-        std::vector<int64_t> h(m);
-        if (m) {
-            UGPU_CUDA(cudaMemcpyAsync(h.data(), ub.ptr, sizeof(int64_t) * m, cudaMemcpyDeviceToHost, ctx.stream));
-            UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
-        }
-        for (auto v : h) max_ub = std::max(max_ub, v);
-    }
-    const bool wide = max_ub > kCtaRowsUb;  // rows beyond the shared-memory hash tables
-    const int gw = int(std::min<int64_t>((m + kWarpsPerCta - 1) / kWarpsPerCta, int64_t(ctx.sms) * 16));
-    // symbolic
+    unsigned long long max_ub = 0;
     if (m) {
-        k_spgemm_warp<double, false><<<std::max(gw, 1), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
-            m, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr, nullptr, nullptr,
-            big.as<int>(), nbig.as<int>());
+        UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(unsigned long long), ctx.stream));
+        k_row_upper_bound<<<stream_grid(ctx, m), kBlock, 0, ctx.stream>>>(arp, aci, brp, m, ub.as<int64_t>(),
+                                                                          nbig.as<unsigned long long>());
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
+        UGPU_CUDA(cudaMemcpyAsync(&max_ub, nbig.ptr, sizeof(max_ub), cudaMemcpyDeviceToHost, ctx.stream));
+        UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
+        UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
     }
+    const bool wide = max_ub > (unsigned long long)kCtaRowsUb;  // rows beyond the shared-memory hash tables
+    // the warp tiers (rows up to kWarpRowsUb products); tiers above the largest row are skipped
+    auto warp_tiers = [&](auto numeric, int64_t *cnt_p, const int32_t *crp, int32_t *cci, double *ccv) {
+        constexpr bool N = decltype(numeric)::value;
+        if (!m) return;
+        auto grid = [&](int warps, int per_sm) {
+            return int(std::max<int64_t>(1, std::min<int64_t>((m + warps - 1) / warps, int64_t(ctx.sms) * per_sm)));
+        };
+        k_spgemm_warp<double, N, kTier0Table, kTier0Ub, kTier0Warps, false>
+            <<<grid(kTier0Warps, 8), kTier0Warps * 32, tier_smem<kTier0Table, kTier0Ub, kTier0Warps>(),
+               ctx.stream>>>(m, -1, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv, nullptr,
+                             nullptr);
+        ctx.launches++;
+        if (max_ub > (unsigned long long)kTier0Ub) {
+            k_spgemm_warp<double, N, kTier1Table, kTier1Ub, kTier1Warps, false>
+                <<<grid(kTier1Warps, 6), kTier1Warps * 32, tier_smem<kTier1Table, kTier1Ub, kTier1Warps>(),
+                   ctx.stream>>>(m, kTier0Ub, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv,
+                                 nullptr, nullptr);
+            ctx.launches++;
+        }
+        if (max_ub > (unsigned long long)kTier1Ub) {
+            k_spgemm_warp<double, N, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>
+                <<<grid(kWarpsPerCta, 16), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
+                    m, kTier1Ub, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv,
+                    big.as<int>(), nbig.as<int>());
+            ctx.launches++;
+        }
+        UGPU_LAUNCH_CHECK();
+    };
+    // symbolic
+    warp_tiers(std::false_type{}, cnt.as<int64_t>(), nullptr, nullptr, nullptr);
     int h_nbig = 0;
     UGPU_CUDA(cudaMemcpyAsync(&h_nbig, nbig.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -544,14 +583,7 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
                                                                      m + 1);
     ctx.launches++;
     UGPU_LAUNCH_CHECK();
-    if (m) {
-        UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
-        k_spgemm_warp<double, true><<<std::max(gw, 1), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
-            m, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr, C->rowptr.as<int32_t>(),
-            C->colidx.as<int32_t>(), C->vals.as<double>(), big.as<int>(), nbig.as<int>());
-        ctx.launches++;
-        UGPU_LAUNCH_CHECK();
-    }
+    warp_tiers(std::true_type{}, nullptr, C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
     if (h_nbig) {
         k_spgemm_cta<double, true><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, cta_smem, ctx.stream>>>(
             big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr, C->rowptr.as<int32_t>(),
@@ -567,14 +599,14 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B) {
         }
     }
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
-    finalize_matrix(*C);
+    if (finalize) finalize_matrix(*C);
     return C;
 }
 
 std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P) {
     UGPU_CHECK(A.nrows == A.ncols && P.nrows == A.nrows, UGPU_ERR_ARG, "ptap: dimension mismatch");
-    auto R = transpose(P);
-    auto AP = spgemm(A, P);
+    auto R = transpose(P, false);   // CSR operands only: no SpMV layout for the intermediates
+    auto AP = spgemm(A, P, false);
     return spgemm(*R, *AP);
 }
 
