@@ -7,6 +7,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 #include <cstdio>
 #include <map>
@@ -80,6 +81,11 @@ struct Buffer {
         UGPU_CUDA(cudaMalloc(&ptr, b));
         bytes = b;
         owned = true;
+    }
+    // keep an owned allocation of at least b bytes (alloc only when it is too small)
+    void ensure(size_t b) {
+        if (owned && ptr && bytes >= std::max<size_t>(b, 16)) return;
+        alloc(b);
     }
     void borrow(void *p, size_t b) {
         release();

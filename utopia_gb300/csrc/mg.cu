@@ -83,6 +83,30 @@ __global__ void k_mask_final(const double *m, int64_t n, T *out, unsigned long l
     atomicAdd(zeros, z);
 }
 
+// PowerMethod loop body (utopia_PowerMethod.hpp:122-146) after y = A v and dot = (y, y):
+// lambda = ||y||, it++, stop when |lambda_old - lambda| < tol or it > max_it.  A call after the
+// stop only sets `skip` (the rescaling of the iteration that stopped still runs).
+__global__ void k_pm_check(double *st, int *done, long long *it, double tol, long long max_it) {
+    if (done[0]) {
+        done[1] = 1;
+        return;
+    }
+    const double lambda = sqrt(st[0]);
+    st[1] = lambda;
+    *it += 1;
+    if (fabs(st[2] - lambda) < tol || *it > max_it) done[0] = 1;
+    st[2] = lambda;
+}
+
+// v = (1 / lambda) y
+__global__ void k_pm_scale(int64_t n, const double *__restrict__ y, const double *lambda, const int *skip,
+                           double *__restrict__ v) {
+    if (*skip) return;
+    const double s = 1. / *lambda;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        v[i] = s * y[i];
+}
+
 // LinearMultiLevel::fix_semidefinite_operator: diagonal entries with |a_ii| < 1e-12 get +1
 __global__ void k_fix_semidefinite(const int32_t *rp, const int32_t *ci, double *cv, int64_t n) {
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
@@ -191,6 +215,16 @@ public:
             lev[i].A64 = lev[i].A64own.get();
         }
         std::reverse(lev.begin(), lev.end());
+        // a re-assembly with unchanged level sizes keeps the work buffers (no free / malloc)
+        for (int l = 0; l < L && l < int(levels_.size()); ++l) {
+            if (levels_[l].n != lev[l].A64->nrows) continue;
+            Level &o = levels_[l];
+            for (auto pr : {std::make_pair(&o.r, &lev[l].r), std::make_pair(&o.c, &lev[l].c),
+                            std::make_pair(&o.c2, &lev[l].c2), std::make_pair(&o.rR, &lev[l].rR),
+                            std::make_pair(&o.p0, &lev[l].p0), std::make_pair(&o.p1, &lev[l].p1),
+                            std::make_pair(&o.rr, &lev[l].rr), std::make_pair(&o.w, &lev[l].w)})
+                *pr.second = std::move(*pr.first);
+        }
         levels_ = std::move(lev);
         for (auto &l : levels_) l.n = l.A64->nrows;
         // storage-precision copies of operators and transfers
@@ -217,16 +251,10 @@ public:
         const size_t vs = dtype_size(vdt_);
         for (auto &l : levels_) {
             size_t b = vs * std::max<int64_t>(l.n, 1);
-            l.r.alloc(b);
-            l.c.alloc(b);
-            l.c2.alloc(b);
-            l.rR.alloc(b);
-            l.p0.alloc(b);
-            l.p1.alloc(b);
-            l.rr.alloc(b);
+            for (Buffer *q : {&l.r, &l.c, &l.c2, &l.rR, &l.p0, &l.p1, &l.rr}) q->ensure(b);
         }
-        f64_r_.alloc(sizeof(double) * std::max<int64_t>(A->nrows, 1));
-        f64_z_.alloc(sizeof(double) * std::max<int64_t>(A->nrows, 1));
+        f64_r_.ensure(sizeof(double) * std::max<int64_t>(A->nrows, 1));
+        f64_z_.ensure(sizeof(double) * std::max<int64_t>(A->nrows, 1));
         UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
         ready_ = true;
     }
@@ -304,6 +332,7 @@ private:
     int vdt_ = UGPU_F64;
     bool ready_ = false;
     Buffer f64_r_, f64_z_;
+    Buffer pm_v_, pm_w_, pm_st_;  // power-method scratch
 
     void make_masks() {
         const int L = n_levels();
@@ -349,7 +378,7 @@ private:
         Level &lv = levels_[l];
         Mat &A64 = const_cast<Mat &>(*lv.A64);
         ensure_diag(A64);
-        lv.w.alloc(dtype_size(vdt_) * std::max<int64_t>(lv.n, 1));
+        lv.w.ensure(dtype_size(vdt_) * std::max<int64_t>(lv.n, 1));
         int g = stream_grid(*ctx, lv.n);
         if (sm == 0 || sm == 2) {
             int mode = (sm == 0) ? 0 : 1;
@@ -395,9 +424,9 @@ private:
         const int64_t n = lv.n;
         std::vector<double> h(n);
         for (int64_t i = 0; i < n; ++i) h[i] = (double(rng.next()) / 2147483647.0) + 1;
-        Buffer v, w;
-        v.alloc(sizeof(double) * std::max<int64_t>(n, 1));
-        w.alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        Buffer &v = pm_v_, &w = pm_w_;
+        v.ensure(sizeof(double) * std::max<int64_t>(n, 1));
+        w.ensure(sizeof(double) * std::max<int64_t>(n, 1));
         UGPU_CUDA(cudaMemcpyAsync(v.ptr, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
         auto norm = [&](const Buffer &b) {
             DotArgs d{};
@@ -408,30 +437,47 @@ private:
             host_dots(*ctx, n, d, &s);
             return std::sqrt(s);
         };
-        Vec vv, ww;
-        vv.ctx = ww.ctx = ctx;
-        vv.n = ww.n = n;
+        Vec vv;
+        vv.ctx = ctx;
+        vv.n = n;
         vv.buf.borrow(v.ptr, v.bytes);
-        ww.buf.borrow(w.ptr, w.bytes);
         double s = 1. / norm(v);
         launch_axpby(*ctx, n, s, vv, 0.0, vv);  // v = s * v
+        // the iterations run without host round trips: a device flag set by the convergence
+        // test predicates the later products, and `skip` the later rescalings
         const double tol = get("power_method_tol");
         const int64_t max_it = int64_t(get("power_method_max_it"));
-        double lambda = 0, lambda_old = 0;
-        int64_t it = 0;
-        bool conv = false;
-        while (!conv) {
+        Buffer &st = pm_st_;  // [0] dot, [1] lambda, [2] lambda_old; then int done, int skip, int64 it
+        st.ensure(3 * sizeof(double) + 2 * sizeof(int) + sizeof(long long));
+        UGPU_CUDA(cudaMemsetAsync(st.ptr, 0, st.bytes, ctx->stream));
+        double *dst = st.as<double>();
+        int *done = reinterpret_cast<int *>(dst + 3);
+        long long *itp = reinterpret_cast<long long *>(done + 2);
+        const int g = stream_grid(*ctx, n);
+        for (int64_t k = 0; k <= max_it + 1; ++k) {
             SpmvArgs a;
             a.x = v.ptr;
             a.y = w.ptr;
             a.vec_dtype = UGPU_F64;
+            a.done = done;
             launch_spmv(*ctx, *lv.A64, a);
-            lambda = norm(w);
-            launch_axpby(*ctx, n, 1. / lambda, ww, 0.0, vv);  // v = (1/lambda) w
-            it++;
-            conv = (std::fabs(lambda_old - lambda) < tol) || it > max_it;
-            lambda_old = lambda;
+            DotArgs d{};
+            d.nd = 1;
+            d.a[0] = d.b[0] = w.ptr;
+            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
+            launch_dots(*ctx, n, d, dst);
+            k_pm_check<<<1, 1, 0, ctx->stream>>>(dst, done, itp, tol, (long long)max_it);
+            k_pm_scale<<<g, kBlock, 0, ctx->stream>>>(n, w.as<double>(), dst + 1, done + 1, v.as<double>());
+            ctx->launches += 2;
         }
+        UGPU_LAUNCH_CHECK();
+        double hs[3];
+        int hd = 0;
+        UGPU_CUDA(cudaMemcpyAsync(hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
+        UGPU_CUDA(cudaMemcpyAsync(&hd, done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        UGPU_CHECK(hd == 1, UGPU_ERR_INTERNAL, "power method: the stop test never held");
+        const double lambda = hs[1];
         lv.emax = get("scale_max_eig") * lambda;
         lv.emin = get("scale_min_eig") * lv.emax;
     }
