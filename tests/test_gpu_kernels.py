@@ -63,6 +63,27 @@ def test_vector_roundtrip_and_blas1(ctx):
     np.testing.assert_array_equal(v32.numpy(), a.astype(np.float32))
 
 
+@pytest.mark.parametrize("offset", [0, 1, 2])
+def test_pinned_host_upload_download(ctx, offset):
+    """Pinned host buffers (the kernel copy when 16-byte aligned, cudaMemcpyAsync otherwise) and
+    pageable ones give the same bytes both ways."""
+    torch = pytest.importorskip("torch")
+    n = 300_001
+    a = np.random.default_rng(offset).standard_normal(n + 2)
+    hb = torch.from_numpy(a).pin_memory()
+    hx = torch.full((n + 2,), -1.0, dtype=torch.float64).pin_memory()
+    v = U.Vector(ctx, n=n)
+    v.upload_from(hb.data_ptr() + 8 * offset)
+    np.testing.assert_array_equal(v.numpy(), a[offset:offset + n])
+    v.download_to(hx.data_ptr() + 8 * offset)
+    h = hx.numpy()
+    np.testing.assert_array_equal(h[offset:offset + n], a[offset:offset + n])
+    assert np.all(h[:offset] == -1.0) and np.all(h[offset + n:] == -1.0)
+    page = np.empty(n)
+    v.download_to(page.ctypes.data)
+    np.testing.assert_array_equal(page, a[offset:offset + n])
+
+
 def test_fp64_fp32_conversions_match_ieee(ctx):
     """The device converts FP64 <-> FP32 with integer bit operations (round to nearest even);
     results equal numpy's IEEE conversions bit for bit, on ties, the overflow boundary, the
