@@ -194,6 +194,13 @@ UGPU_API int ugpu_spgemm(const ugpu_mat *A, const ugpu_mat *B, ugpu_mat **out);
 /* Galerkin product Ac = P^T A P (utopia::ptap -> MatPtAP,
  * utopia/backend/petsc/eval/utopia_petsc_Eval_Multiply.cpp:12-61) */
 UGPU_API int ugpu_ptap(const ugpu_mat *A, const ugpu_mat *P, ugpu_mat **out);
+/* PetscEvalTripleMatrixProduct::ptap(result, A, P, reuse)
+ * (utopia/backend/petsc/eval/utopia_petsc_Eval_Multiply.cpp:9-50, MatPtAP's MatReuse):
+ * reuse = 0 (MAT_INITIAL_MATRIX): *out = P^T A P, a new matrix that keeps its product structure;
+ * reuse = 1 (MAT_REUSE_MATRIX): *out holds a product of an earlier reuse = 0 call; its values are
+ * recomputed in place for the current values of A and P (UGPU_ERR_ARG if the structure of A or P
+ * is no longer the one the product was formed from; a digest of rowptr/colidx is compared). */
+UGPU_API int ugpu_ptap_reuse(const ugpu_mat *A, const ugpu_mat *P, int reuse, ugpu_mat **out);
 
 /* ---------------------------------------------------------------- SpMV family ---- */
 /* y = A x (MatMult, utopia/backend/petsc/utopia_petsc_Matrix.cpp:1358; Operator::apply

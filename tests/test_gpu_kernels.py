@@ -65,8 +65,7 @@ def test_vector_roundtrip_and_blas1(ctx):
 
 @pytest.mark.parametrize("offset", [0, 1, 2])
 def test_pinned_host_upload_download(ctx, offset):
-    """Pinned host buffers (the kernel copy when 16-byte aligned, cudaMemcpyAsync otherwise) and
-    pageable ones give the same bytes both ways."""
+    """Pinned host buffers, aligned or not, and pageable ones give the same bytes both ways."""
     torch = pytest.importorskip("torch")
     n = 300_001
     a = np.random.default_rng(offset).standard_normal(n + 2)
@@ -366,3 +365,39 @@ def test_ptap_full_size_128(ctx):
     one = np.ones(Pm.ncols)
     ref = Pm.to_scipy().T @ (A.to_scipy() @ (Pm.to_scipy() @ one))
     np.testing.assert_allclose(S @ one, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_ptap_reuse_recomputes_values_in_place(ctx):
+    """MatPtAP with MAT_REUSE_MATRIX (ugpu_ptap_reuse): after the values of A and P change, the
+    in-place product has the bits of a fresh product; a changed structure is refused."""
+    A = P.lognormal_diffusion_3d(24, 5)[0]
+    Pm = P.interpolation_3d(24)
+    Ag, Pg = U.SparseMatrix(ctx, A), U.SparseMatrix(ctx, Pm)
+    Ac = Ag.ptap_reuse(Pg)
+    ref0 = Ag.ptap(Pg).csr()
+    for a, b in zip(Ac.csr(), ref0):
+        np.testing.assert_array_equal(a, b)
+    rng = np.random.default_rng(3)
+    Ag.update_values(A.values * rng.uniform(0.5, 2.0, A.nnz))
+    pv = Pm.values.copy()
+    pv[rng.choice(Pm.nnz, Pm.nnz // 3, replace=False)] = 0.0  # rows truncated, structure kept
+    Pg.update_values(pv)
+    out = Ag.ptap_reuse(Pg, out=Ac)
+    assert out is Ac
+    ref = Ag.ptap(Pg).csr()
+    for a, b in zip(Ac.csr(), ref):
+        np.testing.assert_array_equal(a, b)
+    # the reused product is a working operator (its SpMV layout was refreshed)
+    x = U.Vector(ctx, rng.standard_normal(Ac.ncols))
+    y, y2 = U.Vector(ctx, n=Ac.nrows), U.Vector(ctx, n=Ac.nrows)
+    Ac.apply(x, y)
+    U.SparseMatrix(ctx, P.CSR(Ac.nrows, Ac.ncols, *ref)).apply(x, y2)
+    np.testing.assert_array_equal(y.numpy(), y2.numpy())
+    with pytest.raises(U.UgpuError):  # another structure
+        U.SparseMatrix(ctx, P.lognormal_diffusion_3d(24, 5)[0]).ptap_reuse(U.SparseMatrix(ctx, P.interpolation_3d(24)),
+                                                                            out=U.SparseMatrix(ctx, P.laplacian_3d(12)))
+    import scipy.sparse as sp
+
+    Bs = A.to_scipy() + sp.eye(A.nrows, k=2) + sp.eye(A.nrows, k=-2)  # same size, another pattern
+    with pytest.raises(U.UgpuError):  # A with another structure than the product was formed from
+        U.SparseMatrix(ctx, P.CSR.from_scipy(Bs)).ptap_reuse(Pg, out=Ac)

@@ -259,6 +259,18 @@ class SparseMatrix:
         self.ctx.check(self.ctx.lib.ugpu_ptap(self.h, P.h, C.byref(h)))
         return SparseMatrix(self.ctx, _handle=h)
 
+    def ptap_reuse(self, P: "SparseMatrix", out: "SparseMatrix | None" = None) -> "SparseMatrix":
+        """MatPtAP with MatReuse: without `out` a new product that keeps its structure
+        (MAT_INITIAL_MATRIX); with `out` (such a product) its values recomputed in place for the
+        current values of self and P (MAT_REUSE_MATRIX)."""
+        if out is None:
+            h = C.c_void_p()
+            self.ctx.check(self.ctx.lib.ugpu_ptap_reuse(self.h, P.h, 0, C.byref(h)))
+            return SparseMatrix(self.ctx, _handle=h)
+        h = C.c_void_p(out.h.value if isinstance(out.h, C.c_void_p) else out.h)
+        self.ctx.check(self.ctx.lib.ugpu_ptap_reuse(self.h, P.h, 1, C.byref(h)))
+        return out
+
     # Operator::apply
     def apply(self, x: Vector, y: Vector):
         self.ctx.check(self.ctx.lib.ugpu_spmv(self.h, x.h, y.h))

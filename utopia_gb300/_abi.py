@@ -92,6 +92,7 @@ SIGNATURES = {
     "ugpu_transpose": [_vp, _pp],
     "ugpu_spgemm": [_vp, _vp, _pp],
     "ugpu_ptap": [_vp, _vp, _pp],
+    "ugpu_ptap_reuse": [_vp, _vp, _int, _pp],
     "ugpu_spmv": [_vp, _vp, _vp],
     "ugpu_spmv_add": [_vp, _vp, _vp, _vp],
     "ugpu_residual": [_vp, _vp, _vp, _vp],

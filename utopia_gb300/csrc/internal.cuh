@@ -188,6 +188,8 @@ struct Sell {
     int xwin_max = 0;   // interleaved: most x-window floats one slice stages (staged kernel's grouping)
 };
 
+struct PtapPlan;
+
 struct Mat {
     Context *ctx = nullptr;
     int64_t nrows = 0, ncols = 0, nnz = 0;
@@ -200,6 +202,7 @@ struct Mat {
     std::unique_ptr<Sell> sell;
     int format = UGPU_FORMAT_SELL;  // which layout the SpMV family uses
     int64_t max_row = 0;
+    std::shared_ptr<PtapPlan> ptap_plan;  // set when the matrix is a Galerkin product with a kept structure
 };
 
 // sliced-ELL construction (device side), validation and set-up, spmv.cu
@@ -282,9 +285,26 @@ void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);
 // ------------------------------------------------------------------------------------
 // SpGEMM / transpose (spgemm.cu), dense coarse solve (dense.cu)
 // ------------------------------------------------------------------------------------
+// what a numeric-only SpGEMM of the same structure needs: per-row product bounds, the rows
+// beyond the warp tiers
+struct SpgemmPlan {
+    Buffer ub, big;
+    int h_nbig = 0;
+    unsigned long long max_ub = 0;
+};
 // finalize = false: CSR arrays only (no SpMV layout), for intermediates that only feed products
 std::unique_ptr<Mat> transpose(const Mat &A, bool finalize = true);
-std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize = true);
+std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize = true, SpgemmPlan *plan = nullptr);
+void spgemm_numeric(const Mat &A, const Mat &B, Mat &C, const SpgemmPlan &plan);
+// Galerkin product P^T A P whose structure is kept for numeric-only recomputation
+struct PtapPlan;
+std::unique_ptr<Mat> ptap_with_plan(const Mat &A, const Mat &P, std::shared_ptr<PtapPlan> &plan);
+// recompute Ac = P^T A P in place; false (nothing done) if A or P no longer have the plan's structure
+bool ptap_numeric(const Mat &A, const Mat &P, Mat &Ac, PtapPlan &plan, bool finalize = true);
+unsigned long long structure_digest(const Mat &A);
+// T = P^T and the entry permutation (T.vals[k] = P.vals[perm[k]]) that refreshes T's values
+std::unique_ptr<Mat> transpose_with_perm(const Mat &P, Buffer &perm, bool finalize = true);
+void gather_values(Context &ctx, int64_t n, const double *src, const int64_t *perm, double *dst);
 std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P);
 std::unique_ptr<Mat> cast_matrix(const Mat &A, int vdtype);
 std::unique_ptr<Mat> make_csr_device(Context &ctx, int64_t nrows, int64_t ncols, int64_t nnz, int vdtype);

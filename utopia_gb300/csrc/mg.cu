@@ -171,6 +171,8 @@ public:
         prm["precision"] = UGPU_F64;
         prm["must_generate_masks"] = 1;   // Multigrid forces masks on, utopia_Multigrid.hpp:76
         prm["fix_semidefinite_operators"] = 0;
+        prm["keep_galerkin_structure"] = 0;  // 1: products keep their structure; an operator with the
+                                              // structure of the last one only recomputes values
         prm["scale_max_eig"] = 1.2;       // utopia_Chebyshev3level.hpp:183
         prm["scale_min_eig"] = 0.06;
         prm["power_method_tol"] = 1e-2;   // utopia_PowerMethod.hpp:150-151
@@ -203,29 +205,54 @@ public:
         vdt_ = (int(get("precision")) == UGPU_F64) ? UGPU_F64 : UGPU_F32;
         const int sdt = int(get("precision"));
         const int L = int(transfers_.size()) + 1;
-        // galerkin_assembly (utopia_LinearMultiLevel.hpp:201-226): fine first, then reverse
-        std::vector<Level> lev(L);
-        lev[0].A64 = A;
-        for (int i = 1; i < L; ++i) {
-            const Transfer &t = transfers_[L - 1 - i];
-            UGPU_CHECK(t.P64->nrows == lev[i - 1].A64->nrows, UGPU_ERR_ARG,
-                       "interpolation operator rows do not match the finer level");
-            lev[i].A64own = ptap(*lev[i - 1].A64, *t.P64);
-            if (get("fix_semidefinite_operators") != 0) fix_semidefinite_operator(*ctx, *lev[i].A64own);
-            lev[i].A64 = lev[i].A64own.get();
+        const bool keep = get("keep_galerkin_structure") != 0;
+        const bool fix = get("fix_semidefinite_operators") != 0;
+        // an operator with the structure of the last one: only the values of the Galerkin
+        // products are recomputed, in place
+        bool numeric = keep && ready_ && int(levels_.size()) == L;
+        if (numeric) {
+            levels_[L - 1].A64 = A;
+            for (int l = L - 2; l >= 0 && numeric; --l) {
+                Level &c = levels_[l];
+                numeric = c.A64own && c.A64own->ptap_plan &&
+                          ptap_numeric(*levels_[l + 1].A64, *transfers_[l].P64, *c.A64own, *c.A64own->ptap_plan,
+                                       false);
+                if (!numeric) break;
+                if (fix) fix_semidefinite_operator(*ctx, *c.A64own);
+                else finalize_matrix(*c.A64own);
+            }
         }
-        std::reverse(lev.begin(), lev.end());
-        // a re-assembly with unchanged level sizes keeps the work buffers (no free / malloc)
-        for (int l = 0; l < L && l < int(levels_.size()); ++l) {
-            if (levels_[l].n != lev[l].A64->nrows) continue;
-            Level &o = levels_[l];
-            for (auto pr : {std::make_pair(&o.r, &lev[l].r), std::make_pair(&o.c, &lev[l].c),
-                            std::make_pair(&o.c2, &lev[l].c2), std::make_pair(&o.rR, &lev[l].rR),
-                            std::make_pair(&o.p0, &lev[l].p0), std::make_pair(&o.p1, &lev[l].p1),
-                            std::make_pair(&o.rr, &lev[l].rr), std::make_pair(&o.w, &lev[l].w)})
-                *pr.second = std::move(*pr.first);
+        if (!numeric) {
+            // galerkin_assembly (utopia_LinearMultiLevel.hpp:201-226): fine first, then reverse
+            std::vector<Level> lev(L);
+            lev[0].A64 = A;
+            for (int i = 1; i < L; ++i) {
+                const Transfer &t = transfers_[L - 1 - i];
+                UGPU_CHECK(t.P64->nrows == lev[i - 1].A64->nrows, UGPU_ERR_ARG,
+                           "interpolation operator rows do not match the finer level");
+                if (keep) {
+                    std::shared_ptr<PtapPlan> plan;
+                    lev[i].A64own = ptap_with_plan(*lev[i - 1].A64, *t.P64, plan);
+                    lev[i].A64own->ptap_plan = std::move(plan);
+                } else {
+                    lev[i].A64own = ptap(*lev[i - 1].A64, *t.P64);
+                }
+                if (fix) fix_semidefinite_operator(*ctx, *lev[i].A64own);
+                lev[i].A64 = lev[i].A64own.get();
+            }
+            std::reverse(lev.begin(), lev.end());
+            // a re-assembly with unchanged level sizes keeps the work buffers (no free / malloc)
+            for (int l = 0; l < L && l < int(levels_.size()); ++l) {
+                if (levels_[l].n != lev[l].A64->nrows) continue;
+                Level &o = levels_[l];
+                for (auto pr : {std::make_pair(&o.r, &lev[l].r), std::make_pair(&o.c, &lev[l].c),
+                                std::make_pair(&o.c2, &lev[l].c2), std::make_pair(&o.rR, &lev[l].rR),
+                                std::make_pair(&o.p0, &lev[l].p0), std::make_pair(&o.p1, &lev[l].p1),
+                                std::make_pair(&o.rr, &lev[l].rr), std::make_pair(&o.w, &lev[l].w)})
+                    *pr.second = std::move(*pr.first);
+            }
+            levels_ = std::move(lev);
         }
-        levels_ = std::move(lev);
         for (auto &l : levels_) l.n = l.A64->nrows;
         // storage-precision copies of operators and transfers
         for (int l = 0; l < L; ++l) {

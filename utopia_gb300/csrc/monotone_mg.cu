@@ -158,6 +158,8 @@ public:
             v->buf.alloc(sizeof(double) * std::max<int64_t>(nc, 1));
         }
         It_ = cast_matrix(I, UGPU_F64);  // no truncation until the active set first changes
+        AH_.reset();
+        Rt_.reset();
         galerkin();
         UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
         ready_ = true;
@@ -171,18 +173,27 @@ private:
     std::unique_ptr<Solver> pgs_, mg_;
     DenseCholesky chol_;                   // coarse solve when the fine transfer is the only one
     const Vec *lb_ = nullptr, *ub_ = nullptr;
-    Buffer lbfill_, ubfill_, active_, cnt_, r_, help_, dx_, xold_, corr_;
+    Buffer lbfill_, ubfill_, active_, cnt_, r_, help_, dx_, xold_, corr_, rt_perm_;
     Vec rc_, cc_;
     bool ready_ = false;
     int64_t assemblies_ = 0;
 
     // galerkin_assembly (:212-227): A_H = P_t^T A P_t, fix_semidefinite_operator, then the
-    // linear multigrid (which assembles the levels below with the same fix) or the direct solver
+    // linear multigrid (which assembles the levels below with the same fix) or the direct
+    // solver.  Truncation only changes values, so after the first assembly every product
+    // (A_H, the levels below it, P_t^T) is recomputed in place on its kept structure.
     void galerkin() {
-        auto AH = ptap(*op, *It_);
-        fix_semidefinite_operator(*ctx, *AH);
+        const bool numeric = AH_ && AH_->ptap_plan && ptap_numeric(*op, *It_, *AH_, *AH_->ptap_plan, false);
+        std::unique_ptr<Mat> fresh;
+        if (!numeric) {
+            std::shared_ptr<PtapPlan> plan;
+            fresh = ptap_with_plan(*op, *It_, plan);
+            fresh->ptap_plan = std::move(plan);
+        }
+        Mat &AH = numeric ? *AH_ : *fresh;
+        fix_semidefinite_operator(*ctx, AH);
         if (P_.size() == 1) {
-            UGPU_CHECK(chol_.factor(*AH), UGPU_ERR_NOT_SPD, "MonotoneMultigrid: coarse operator is not SPD");
+            UGPU_CHECK(chol_.factor(AH), UGPU_ERR_NOT_SPD, "MonotoneMultigrid: coarse operator is not SPD");
         } else {
             if (!mg_) {
                 mg_ = make_multigrid(ctx);
@@ -194,10 +205,18 @@ private:
                 mg_->set(k, get(k));
             mg_->set("fix_semidefinite_operators", 1);  // MonotoneMultigrid(): algo_.fix_semidefinite_operators(true)
             mg_->set("must_generate_masks", 0);         // algo_.must_generate_masks(false)
-            mg_->update(AH.get());
+            mg_->set("keep_galerkin_structure", 1);
+            mg_->update(&AH);
         }
-        AH_ = std::move(AH);  // the multigrid keeps a pointer to this operator
-        Rt_ = transpose(*It_);
+        if (!numeric) AH_ = std::move(fresh);  // the multigrid keeps a pointer to this operator
+        // P_t^T: values gathered from P_t through the transpose's entry permutation
+        if (Rt_ && Rt_->nnz == It_->nnz) {
+            gather_values(*ctx, It_->nnz, It_->vals.as<double>(), rt_perm_.as<int64_t>(), Rt_->vals.as<double>());
+            Rt_->has_diag = false;
+            finalize_matrix(*Rt_);
+        } else {
+            Rt_ = transpose_with_perm(*It_, rt_perm_, true);
+        }
         ++assemblies_;
     }
 

@@ -481,18 +481,9 @@ std::unique_ptr<Mat> transpose(const Mat &A, bool finalize) {
     return T;
 }
 
-std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize) {
-    Context &ctx = *A.ctx;
-    UGPU_CHECK(A.ncols == B.nrows, UGPU_ERR_ARG, "spgemm: inner dimensions differ");
-    UGPU_CHECK(A.vdtype == UGPU_F64 && B.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "spgemm: FP64 operands");
-    const int64_t m = A.nrows;
-    Buffer ub, cnt, crp64, big, nbig;
-    ub.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
-    cnt.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
-    crp64.alloc(sizeof(int64_t) * (m + 1));
-    big.alloc(sizeof(int) * std::max<int64_t>(m, 1));
-    nbig.alloc(sizeof(unsigned long long));  // the maximum upper bound, then the count of big rows
-    UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
+namespace {
+
+void spgemm_set_attributes() {
     const size_t warp_smem = kWarpSmem;
     const size_t cta_smem = kCtaSmem;
     static bool attr_done = false;
@@ -513,69 +504,96 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize) {
                                        int(kWideSmem)));
         attr_done = true;
     }
+}
+
+// the warp tiers (rows up to kWarpRowsUb products); tiers above the largest row are skipped.
+// Symbolic (N = false): row counts into cnt, rows beyond the warp tiers listed in big/nbig.
+template <bool N>
+void launch_warp_tiers(Context &ctx, const Mat &A, const Mat &B, unsigned long long max_ub, const int64_t *ub,
+                       int64_t *cnt, const int32_t *crp, int32_t *cci, double *ccv, int *big, int *nbig) {
+    const int64_t m = A.nrows;
+    if (!m) return;
     const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
     const int32_t *brp = B.rowptr.as<int32_t>(), *bci = B.colidx.as<int32_t>();
     const double *acv = A.vals.as<double>(), *bcv = B.vals.as<double>();
+    auto grid = [&](int warps, int per_sm) {
+        return int(std::max<int64_t>(1, std::min<int64_t>((m + warps - 1) / warps, int64_t(ctx.sms) * per_sm)));
+    };
+    k_spgemm_warp<double, N, kTier0Table, kTier0Ub, kTier0Warps, false>
+        <<<grid(kTier0Warps, 8), kTier0Warps * 32, tier_smem<kTier0Table, kTier0Ub, kTier0Warps>(), ctx.stream>>>(
+            m, -1, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, nullptr, nullptr);
+    ctx.launches++;
+    if (max_ub > (unsigned long long)kTier0Ub) {
+        k_spgemm_warp<double, N, kTier1Table, kTier1Ub, kTier1Warps, false>
+            <<<grid(kTier1Warps, 6), kTier1Warps * 32, tier_smem<kTier1Table, kTier1Ub, kTier1Warps>(),
+               ctx.stream>>>(m, kTier0Ub, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, nullptr, nullptr);
+        ctx.launches++;
+    }
+    if (max_ub > (unsigned long long)kTier1Ub) {
+        k_spgemm_warp<double, N, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>
+            <<<grid(kWarpsPerCta, 16), kWarpsPerCta * 32, kWarpSmem, ctx.stream>>>(
+                m, kTier1Ub, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, big, nbig);
+        ctx.launches++;
+    }
+    UGPU_LAUNCH_CHECK();
+}
+
+// rows beyond the warp tiers: one CTA per row (hash table), then the windowed wide rows
+template <bool N>
+void launch_big_rows(Context &ctx, const Mat &A, const Mat &B, unsigned long long max_ub, const int64_t *ub,
+                     const int *big, int h_nbig, int64_t *cnt, const int32_t *crp, int32_t *cci, double *ccv) {
+    if (!h_nbig) return;
+    const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
+    const int32_t *brp = B.rowptr.as<int32_t>(), *bci = B.colidx.as<int32_t>();
+    const double *acv = A.vals.as<double>(), *bcv = B.vals.as<double>();
+    k_spgemm_cta<double, N><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, kCtaSmem, ctx.stream>>>(
+        big, h_nbig, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    if (max_ub > (unsigned long long)kCtaRowsUb) {
+        k_spgemm_wide<N><<<std::min(h_nbig, ctx.sms * 2), kWideThreads, kWideSmem, ctx.stream>>>(
+            big, h_nbig, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+}
+
+}  // namespace
+
+std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPlan *plan) {
+    Context &ctx = *A.ctx;
+    UGPU_CHECK(A.ncols == B.nrows, UGPU_ERR_ARG, "spgemm: inner dimensions differ");
+    UGPU_CHECK(A.vdtype == UGPU_F64 && B.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "spgemm: FP64 operands");
+    const int64_t m = A.nrows;
+    Buffer ub, cnt, crp64, big, nbig;
+    ub.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
+    cnt.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
+    crp64.alloc(sizeof(int64_t) * (m + 1));
+    big.alloc(sizeof(int) * std::max<int64_t>(m, 1));
+    nbig.alloc(sizeof(unsigned long long));  // the maximum upper bound, then the count of big rows
+    UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
+    spgemm_set_attributes();
     // largest per-row upper bound decides whether every row fits a shared-memory table
     unsigned long long max_ub = 0;
     if (m) {
         UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(unsigned long long), ctx.stream));
-        k_row_upper_bound<<<stream_grid(ctx, m), kBlock, 0, ctx.stream>>>(arp, aci, brp, m, ub.as<int64_t>(),
-                                                                          nbig.as<unsigned long long>());
+        k_row_upper_bound<<<stream_grid(ctx, m), kBlock, 0, ctx.stream>>>(
+            A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), B.rowptr.as<int32_t>(), m, ub.as<int64_t>(),
+            nbig.as<unsigned long long>());
         ctx.launches++;
         UGPU_LAUNCH_CHECK();
         UGPU_CUDA(cudaMemcpyAsync(&max_ub, nbig.ptr, sizeof(max_ub), cudaMemcpyDeviceToHost, ctx.stream));
         UGPU_CUDA(cudaMemsetAsync(nbig.ptr, 0, sizeof(int), ctx.stream));
         UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
     }
-    const bool wide = max_ub > (unsigned long long)kCtaRowsUb;  // rows beyond the shared-memory hash tables
-    // the warp tiers (rows up to kWarpRowsUb products); tiers above the largest row are skipped
-    auto warp_tiers = [&](auto numeric, int64_t *cnt_p, const int32_t *crp, int32_t *cci, double *ccv) {
-        constexpr bool N = decltype(numeric)::value;
-        if (!m) return;
-        auto grid = [&](int warps, int per_sm) {
-            return int(std::max<int64_t>(1, std::min<int64_t>((m + warps - 1) / warps, int64_t(ctx.sms) * per_sm)));
-        };
-        k_spgemm_warp<double, N, kTier0Table, kTier0Ub, kTier0Warps, false>
-            <<<grid(kTier0Warps, 8), kTier0Warps * 32, tier_smem<kTier0Table, kTier0Ub, kTier0Warps>(),
-               ctx.stream>>>(m, -1, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv, nullptr,
-                             nullptr);
-        ctx.launches++;
-        if (max_ub > (unsigned long long)kTier0Ub) {
-            k_spgemm_warp<double, N, kTier1Table, kTier1Ub, kTier1Warps, false>
-                <<<grid(kTier1Warps, 6), kTier1Warps * 32, tier_smem<kTier1Table, kTier1Ub, kTier1Warps>(),
-                   ctx.stream>>>(m, kTier0Ub, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv,
-                                 nullptr, nullptr);
-            ctx.launches++;
-        }
-        if (max_ub > (unsigned long long)kTier1Ub) {
-            k_spgemm_warp<double, N, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>
-                <<<grid(kWarpsPerCta, 16), kWarpsPerCta * 32, warp_smem, ctx.stream>>>(
-                    m, kTier1Ub, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt_p, crp, cci, ccv,
-                    big.as<int>(), nbig.as<int>());
-            ctx.launches++;
-        }
-        UGPU_LAUNCH_CHECK();
-    };
     // symbolic
-    warp_tiers(std::false_type{}, cnt.as<int64_t>(), nullptr, nullptr, nullptr);
+    launch_warp_tiers<false>(ctx, A, B, max_ub, ub.as<int64_t>(), cnt.as<int64_t>(), nullptr, nullptr, nullptr,
+                             big.as<int>(), nbig.as<int>());
     int h_nbig = 0;
     UGPU_CUDA(cudaMemcpyAsync(&h_nbig, nbig.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
-    if (h_nbig) {
-        k_spgemm_cta<double, false><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, cta_smem, ctx.stream>>>(
-            big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr,
-            nullptr, nullptr);
-        ctx.launches++;
-        UGPU_LAUNCH_CHECK();
-        if (wide) {
-            k_spgemm_wide<false><<<std::min(h_nbig, ctx.sms * 2), kWideThreads, kWideSmem, ctx.stream>>>(
-                big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, cnt.as<int64_t>(), nullptr,
-                nullptr, nullptr);
-            ctx.launches++;
-            UGPU_LAUNCH_CHECK();
-        }
-    }
+    launch_big_rows<false>(ctx, A, B, max_ub, ub.as<int64_t>(), big.as<int>(), h_nbig, cnt.as<int64_t>(), nullptr,
+                           nullptr, nullptr);
     int64_t nnz = device_exclusive_scan(ctx, cnt.as<int64_t>(), crp64.as<int64_t>(), m);
     UGPU_CHECK(nnz < (1ll << 31), UGPU_ERR_UNSUPPORTED, "spgemm: product has more than 2^31 entries");
     auto C = make_csr_device(ctx, m, B.ncols, nnz, UGPU_F64);
@@ -583,24 +601,29 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize) {
                                                                      m + 1);
     ctx.launches++;
     UGPU_LAUNCH_CHECK();
-    warp_tiers(std::true_type{}, nullptr, C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
-    if (h_nbig) {
-        k_spgemm_cta<double, true><<<std::min(h_nbig, ctx.sms * 2), kCtaThreads, cta_smem, ctx.stream>>>(
-            big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr, C->rowptr.as<int32_t>(),
-            C->colidx.as<int32_t>(), C->vals.as<double>());
-        ctx.launches++;
-        UGPU_LAUNCH_CHECK();
-        if (wide) {
-            k_spgemm_wide<true><<<std::min(h_nbig, ctx.sms * 2), kWideThreads, kWideSmem, ctx.stream>>>(
-                big.as<int>(), h_nbig, ub.as<int64_t>(), arp, aci, acv, brp, bci, bcv, nullptr,
-                C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
-            ctx.launches++;
-            UGPU_LAUNCH_CHECK();
-        }
-    }
+    // numeric
+    launch_warp_tiers<true>(ctx, A, B, max_ub, ub.as<int64_t>(), nullptr, C->rowptr.as<int32_t>(),
+                            C->colidx.as<int32_t>(), C->vals.as<double>(), nullptr, nullptr);
+    launch_big_rows<true>(ctx, A, B, max_ub, ub.as<int64_t>(), big.as<int>(), h_nbig, nullptr,
+                          C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    if (plan) {
+        plan->ub = std::move(ub);
+        plan->big = std::move(big);
+        plan->h_nbig = h_nbig;
+        plan->max_ub = max_ub;
+    }
     if (finalize) finalize_matrix(*C);
     return C;
+}
+
+// values of C = A B again, for A and B with the structure the plan was made from
+void spgemm_numeric(const Mat &A, const Mat &B, Mat &C, const SpgemmPlan &plan) {
+    Context &ctx = *A.ctx;
+    launch_warp_tiers<true>(ctx, A, B, plan.max_ub, plan.ub.as<int64_t>(), nullptr, C.rowptr.as<int32_t>(),
+                            C.colidx.as<int32_t>(), C.vals.as<double>(), nullptr, nullptr);
+    launch_big_rows<true>(ctx, A, B, plan.max_ub, plan.ub.as<int64_t>(), plan.big.as<int>(), plan.h_nbig, nullptr,
+                          C.rowptr.as<int32_t>(), C.colidx.as<int32_t>(), C.vals.as<double>());
 }
 
 std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P) {
@@ -608,6 +631,143 @@ std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P) {
     auto R = transpose(P, false);   // CSR operands only: no SpMV layout for the intermediates
     auto AP = spgemm(A, P, false);
     return spgemm(*R, *AP);
+}
+
+// ------------------------------------------------------------------------------------
+// Galerkin products with a kept structure: ptap_with_plan keeps what a later numeric-only
+// product needs (the transpose's entry permutation, the A P intermediate and both products'
+// row bounds and long-row lists); ptap_numeric recomputes the values of the same product in
+// place after the values of A and P changed.  A structure digest of A and P guards the reuse.
+// ------------------------------------------------------------------------------------
+namespace {
+
+__global__ void k_iota_f64(int64_t n, double *out) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = double(i);
+}
+
+__global__ void k_f64_to_i64(int64_t n, const double *in, int64_t *out) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        out[i] = int64_t(in[i]);
+}
+
+__global__ void k_gather_f64(int64_t n, const double *__restrict__ src, const int64_t *__restrict__ perm,
+                             double *__restrict__ dst) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        dst[i] = src[perm[i]];
+}
+
+__device__ __forceinline__ unsigned long long mix64(unsigned long long x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdull;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ull;
+    x ^= x >> 33;
+    return x;
+}
+
+// order-independent digest of (rowptr, colidx): a wrapping sum of mixed (position, value) pairs
+__global__ void k_structure_digest(const int32_t *rp, const int32_t *ci, int64_t n, int64_t nnz,
+                                   unsigned long long *out) {
+    unsigned long long acc = 0;
+    const int64_t stride = int64_t(gridDim.x) * blockDim.x;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i <= n; i += stride)
+        acc += mix64((unsigned long long)(i) * 0x9e3779b97f4a7c15ull ^ (unsigned long long)(uint32_t(rp[i])));
+    for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < nnz; k += stride)
+        acc += mix64(((unsigned long long)(k) << 1 | 1ull) * 0xbf58476d1ce4e5b9ull ^
+                     (unsigned long long)(uint32_t(ci[k])));
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, acc);
+}
+
+}  // namespace
+
+unsigned long long structure_digest(const Mat &A) {
+    Context &ctx = *A.ctx;
+    Buffer d;
+    d.alloc(sizeof(unsigned long long));
+    UGPU_CUDA(cudaMemsetAsync(d.ptr, 0, sizeof(unsigned long long), ctx.stream));
+    k_structure_digest<<<stream_grid(ctx, std::max<int64_t>(A.nnz, A.nrows + 1)), kBlock, 0, ctx.stream>>>(
+        A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), A.nrows, A.nnz, d.as<unsigned long long>());
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    unsigned long long h = 0;
+    UGPU_CUDA(cudaMemcpyAsync(&h, d.ptr, sizeof(h), cudaMemcpyDeviceToHost, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    return h ^ (unsigned long long)(A.nrows) * 31ull ^ (unsigned long long)(A.ncols) << 20;
+}
+
+// T = P^T and perm with T.vals[k] = P.vals[perm[k]] (the transpose of P's entry positions)
+std::unique_ptr<Mat> transpose_with_perm(const Mat &P, Buffer &perm, bool finalize) {
+    UGPU_CHECK(P.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "transpose_with_perm: FP64 matrix");
+    Context &ctx = *P.ctx;
+    Mat idx;
+    idx.ctx = &ctx;
+    idx.nrows = P.nrows;
+    idx.ncols = P.ncols;
+    idx.nnz = P.nnz;
+    idx.vdtype = UGPU_F64;
+    idx.rowptr.borrow(P.rowptr.ptr, P.rowptr.bytes);
+    idx.colidx.borrow(P.colidx.ptr, P.colidx.bytes);
+    idx.vals.alloc(sizeof(double) * std::max<int64_t>(P.nnz, 1));
+    k_iota_f64<<<stream_grid(ctx, P.nnz), kBlock, 0, ctx.stream>>>(P.nnz, idx.vals.as<double>());
+    ctx.launches++;
+    auto T = transpose(idx, false);  // synchronises before it returns
+    perm.ensure(sizeof(int64_t) * std::max<int64_t>(P.nnz, 1));
+    k_f64_to_i64<<<stream_grid(ctx, P.nnz), kBlock, 0, ctx.stream>>>(P.nnz, T->vals.as<double>(),
+                                                                     perm.as<int64_t>());
+    ctx.launches++;
+    gather_values(ctx, P.nnz, P.vals.as<double>(), perm.as<int64_t>(), T->vals.as<double>());
+    if (finalize) {
+        UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+        finalize_matrix(*T);
+    }
+    return T;
+}
+
+void gather_values(Context &ctx, int64_t n, const double *src, const int64_t *perm, double *dst) {
+    if (n == 0) return;
+    k_gather_f64<<<stream_grid(ctx, n), kBlock, 0, ctx.stream>>>(n, src, perm, dst);
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+}
+
+struct PtapPlan {
+    unsigned long long a_digest = 0, p_digest = 0;
+    int64_t p_nnz = 0;
+    std::unique_ptr<Mat> R, AP;  // P^T (values gathered from P through rperm) and A P
+    Buffer rperm;
+    SpgemmPlan s1, s2;           // A P and R (A P)
+};
+
+std::unique_ptr<Mat> ptap_with_plan(const Mat &A, const Mat &P, std::shared_ptr<PtapPlan> &plan) {
+    UGPU_CHECK(A.nrows == A.ncols && P.nrows == A.nrows, UGPU_ERR_ARG, "ptap: dimension mismatch");
+    UGPU_CHECK(A.vdtype == UGPU_F64 && P.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "ptap: FP64 operands");
+    auto pl = std::make_shared<PtapPlan>();
+    pl->a_digest = structure_digest(A);
+    pl->p_digest = structure_digest(P);
+    pl->p_nnz = P.nnz;
+    pl->R = transpose_with_perm(P, pl->rperm, false);
+    pl->AP = spgemm(A, P, false, &pl->s1);
+    auto C = spgemm(*pl->R, *pl->AP, true, &pl->s2);
+    plan = std::move(pl);
+    return C;
+}
+
+bool ptap_numeric(const Mat &A, const Mat &P, Mat &Ac, PtapPlan &pl, bool finalize) {
+    Context &ctx = *A.ctx;
+    if (P.nnz != pl.p_nnz || A.nrows != pl.AP->nrows || P.ncols != pl.R->nrows || Ac.nrows != pl.R->nrows)
+        return false;
+    if (structure_digest(A) != pl.a_digest || structure_digest(P) != pl.p_digest) return false;
+    gather_values(ctx, P.nnz, P.vals.as<double>(), pl.rperm.as<int64_t>(), pl.R->vals.as<double>());
+    spgemm_numeric(A, P, *pl.AP, pl.s1);
+    spgemm_numeric(*pl.R, *pl.AP, Ac, pl.s2);
+    Ac.has_diag = false;
+    if (finalize) {
+        UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+        finalize_matrix(Ac);
+    }
+    return true;
 }
 
 }  // namespace ugpu
@@ -648,6 +808,29 @@ int ugpu_ptap(const ugpu_mat *A, const ugpu_mat *P, ugpu_mat **out) {
     auto h = new ugpu_mat;
     h->impl = std::move(*C);
     *out = h;
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
+
+int ugpu_ptap_reuse(const ugpu_mat *A, const ugpu_mat *P, int reuse, ugpu_mat **out) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(P);
+    UGPU_REQUIRE(out);
+    UGPU_CHECK(reuse == 0 || reuse == 1, UGPU_ERR_ARG, "reuse: 0 (initial matrix) or 1 (reuse matrix)");
+    if (reuse == 1) {
+        UGPU_CHECK(*out && (*out)->impl.ptap_plan, UGPU_ERR_ARG,
+                   "reuse: the matrix must come from an earlier ugpu_ptap_reuse(..., 0, ...)");
+        Mat &Ac = (*out)->impl;
+        UGPU_CHECK(ptap_numeric(A->impl, P->impl, Ac, *Ac.ptap_plan, true), UGPU_ERR_ARG,
+                   "reuse: A or P no longer has the structure the product was formed from");
+    } else {
+        std::shared_ptr<PtapPlan> plan;
+        auto C = ptap_with_plan(A->impl, P->impl, plan);
+        C->ptap_plan = std::move(plan);
+        auto h = new ugpu_mat;
+        h->impl = std::move(*C);
+        *out = h;
+    }
     UGPU_ABI_END(A ? A->impl.ctx : nullptr)
 }
 
