@@ -216,6 +216,17 @@ def test_mixed_precision_fcg(ctx, oracle, precision):
     assert rel(xg, x64) <= 1e-6
 
 
+@pytest.mark.parametrize("shape", [(1, 1), (8, 8), (40, 25), (33, 63)])
+def test_cholesky_solver_block_sizes(ctx, shape):
+    """The blocked factorisation and inversion on sizes that are not multiples of the block (64)."""
+    A = P.laplacian_2d(*shape)
+    b = np.random.default_rng(1).standard_normal(A.nrows)
+    x = U.Vector(ctx, n=A.nrows)
+    U.CholeskySolver(ctx).solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    xr = np.linalg.solve(A.to_scipy().toarray(), b)
+    assert rel(x.numpy(), xr) <= 1e-12
+
+
 def test_cholesky_solver_and_not_spd(ctx):
     A = P.lognormal_diffusion_3d(9, 3)[0]
     b = np.random.default_rng(0).standard_normal(A.nrows)

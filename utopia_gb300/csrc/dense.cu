@@ -55,10 +55,11 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double *A, int64_t n, int64_
         for (int i = j + 1 + threadIdx.x; i < kb; i += blockDim.x) a[i][j] /= d;
         __syncthreads();
         // trailing update of the lower triangle: a[i][c] -= a[i][j] * a[c][j], j < c <= i
-        const int m = kb - j - 1;
-        for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
-            int i = j + 1 + e / m, c = j + 1 + e % m;
-            if (c <= i) a[i][c] -= a[i][j] * a[c][j];
+        // (16 x 16 threads over rows and columns)
+        const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+        for (int i = j + 1 + ty; i < kb; i += 16) {
+            const double aij = a[i][j];
+            for (int c = j + 1 + tx; c <= i; c += 16) a[i][c] -= aij * a[c][j];
         }
         __syncthreads();
     }
@@ -68,22 +69,33 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double *A, int64_t n, int64_
     }
 }
 
-// rows below the diagonal block: x * L11^T = a  (one thread per row, in place)
-__global__ void __launch_bounds__(256) k_trsm_panel(double *A, int64_t n, int64_t k0, int kb) {
-    __shared__ double l[NB][NB + 1];
-    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-        int i = e / kb, j = e % kb;
-        l[i][j] = A[(k0 + i) * n + k0 + j];
+// inverse of the lower-triangular kb x kb diagonal block of L at (k0, k0), into Li (row-major,
+// leading dimension NB): one thread per column solves L_bb x = e_c by forward substitution
+__global__ void __launch_bounds__(NB) k_trinv_diag(const double *L, int64_t n, int64_t k0, int kb, double *Li) {
+    __shared__ double x[NB][NB + 1];
+    const int c = threadIdx.x;
+    const double *Lb = L + k0 * n + k0;
+    if (c < kb) {
+        for (int i = 0; i < c; ++i) x[i][c] = 0.0;
+        for (int i = c; i < kb; ++i) {
+            double s = (i == c) ? 1.0 : 0.0;
+            for (int q = c; q < i; ++q) s -= Lb[int64_t(i) * n + q] * x[q][c];
+            x[i][c] = s / Lb[int64_t(i) * n + i];
+        }
     }
     __syncthreads();
-    for (int64_t r = k0 + kb + blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n;
-         r += int64_t(gridDim.x) * blockDim.x) {
-        double *row = A + r * n + k0;
-        for (int c = 0; c < kb; ++c) {
-            double s = row[c];
-            for (int q = 0; q < c; ++q) s -= row[q] * l[c][q];
-            row[c] = s / l[c][c];
-        }
+    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
+        const int i = e / NB, j = e % NB;
+        Li[e] = (i < kb && j < kb) ? x[i][j] : 0.0;
+    }
+}
+
+// dst (rows x cols, leading dimension ldd) = src (leading dimension lds)
+__global__ void k_copy_block(const double *src, int64_t lds, double *dst, int64_t ldd, int rows, int cols) {
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < int64_t(rows) * cols;
+         e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = e / cols, j = e % cols;
+        dst[i * ldd + j] = src[i * lds + j];
     }
 }
 
@@ -141,34 +153,6 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
                 *c = (beta == 0.0 ? 0.0 : beta * *c) + alpha * acc[p][q];
             }
         }
-}
-
-// L_bb X = B for ncols right-hand-side columns stored in rows r0..r0+kb of Y (ld n),
-// columns [0, ncols); X overwrites B, scaled by sign.  One thread per column.
-__global__ void __launch_bounds__(256) k_trsm_left_lower(const double *L, double *Y, int64_t n, int64_t r0, int kb,
-                                                         int ncols, double sign) {
-    __shared__ double l[NB][NB + 1];
-    for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-        int i = e / kb, j = e % kb;
-        l[i][j] = L[(r0 + i) * n + r0 + j];
-    }
-    __syncthreads();
-    for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < ncols; c += gridDim.x * blockDim.x) {
-        double x[NB];
-        for (int i = 0; i < kb; ++i) {
-            double s = Y[(r0 + i) * n + c];
-            for (int q = 0; q < i; ++q) s -= l[i][q] * x[q];
-            x[i] = s / l[i][i];
-        }
-        for (int i = 0; i < kb; ++i) Y[(r0 + i) * n + c] = sign * x[i];
-    }
-}
-
-__global__ void k_set_identity_block(double *Y, int64_t n, int64_t r0, int kb) {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < kb * kb; e += gridDim.x * blockDim.x) {
-        int i = e / kb, j = e % kb;
-        Y[(r0 + i) * n + r0 + j] = (i == j) ? 1.0 : 0.0;
-    }
 }
 
 __global__ void k_zero(double *p, int64_t m) {
@@ -249,21 +233,35 @@ bool DenseCholesky::factor(const Mat &A) {
     Buffer bad;
     bad.alloc(sizeof(int));
     UGPU_CUDA(cudaMemsetAsync(bad.ptr, 0, sizeof(int), c.stream));
-    // blocked right-looking Cholesky
+    // blocked right-looking Cholesky; the panel below each diagonal block is A21 L11^-T, one
+    // GEMM with the block's explicit inverse (kept for the inversion below)
+    const int64_t nblk = (n + NB - 1) / NB;
+    Buffer Li, T;
+    Li.alloc(sizeof(double) * size_t(nblk) * NB * NB);
+    T.alloc(sizeof(double) * size_t(std::max<int64_t>(n * NB, 1)));
+    double *Lip = Li.as<double>(), *Tp = T.as<double>();
+    auto copy_block = [&](const double *src, int64_t lds, double *dst, int64_t ldd, int rows, int cols) {
+        const int g = int(std::min<int64_t>((int64_t(rows) * cols + 255) / 256, int64_t(c.sms) * 8));
+        k_copy_block<<<std::max(g, 1), 256, 0, c.stream>>>(src, lds, dst, ldd, rows, cols);
+        c.launches++;
+    };
     for (int64_t k0 = 0; k0 < n; k0 += NB) {
-        int kb = int(std::min<int64_t>(NB, n - k0));
+        const int kb = int(std::min<int64_t>(NB, n - k0));
+        double *Lb = Lip + (k0 / NB) * NB * NB;
         k_potrf_diag<<<1, 256, 0, c.stream>>>(Lp, n, k0, kb, bad.as<int>());
-        int64_t rest = n - k0 - kb;
+        k_trinv_diag<<<1, NB, 0, c.stream>>>(Lp, n, k0, kb, Lb);
+        c.launches += 2;
+        const int64_t rest = n - k0 - kb;
         if (rest > 0) {
-            int g = int(std::min<int64_t>((rest + 255) / 256, 1024));
-            k_trsm_panel<<<g, 256, 0, c.stream>>>(Lp, n, k0, kb);
+            double *A21 = Lp + (k0 + kb) * n + k0;
+            copy_block(A21, n, Tp, kb, int(rest), kb);
+            dim3 gp(unsigned((kb + 63) / 64), unsigned((rest + 63) / 64));
+            k_dgemm<false, true><<<gp, 256, 0, c.stream>>>(int(rest), kb, kb, 1.0, Tp, kb, Lb, NB, 0.0, A21, n, false);
             dim3 grid(unsigned((rest + 63) / 64), unsigned((rest + 63) / 64));
-            k_dgemm<false, true><<<grid, 256, 0, c.stream>>>(int(rest), int(rest), kb, -1.0, Lp + (k0 + kb) * n + k0,
-                                                             n, Lp + (k0 + kb) * n + k0, n, 1.0,
+            k_dgemm<false, true><<<grid, 256, 0, c.stream>>>(int(rest), int(rest), kb, -1.0, A21, n, A21, n, 1.0,
                                                              Lp + (k0 + kb) * n + k0 + kb, n, true);
             c.launches += 2;
         }
-        c.launches++;
         UGPU_LAUNCH_CHECK();
     }
     int hbad = 0;
@@ -274,20 +272,19 @@ bool DenseCholesky::factor(const Mat &A) {
     k_zero<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Y, n * n);
     c.launches++;
     for (int64_t r0 = 0; r0 < n; r0 += NB) {
-        int kb = int(std::min<int64_t>(NB, n - r0));
+        const int kb = int(std::min<int64_t>(NB, n - r0));
+        const double *Lb = Lip + (r0 / NB) * NB * NB;
         if (r0 > 0) {
             dim3 grid(unsigned((r0 + 63) / 64), unsigned((kb + 63) / 64));
-            // T = L[r0:r0+kb, 0:r0] * Y[0:r0, 0:r0] written into Y[r0:r0+kb, 0:r0]
+            // T = L[r0:r0+kb, 0:r0] Y[0:r0, 0:r0]  (kb x r0, leading dimension r0)
             k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(kb, int(r0), int(r0), 1.0, Lp + r0 * n, n, Y, n, 0.0,
-                                                              Y + r0 * n, n, false);
-            int g = int(std::min<int64_t>((r0 + 255) / 256, 1024));
-            k_trsm_left_lower<<<g, 256, 0, c.stream>>>(Lp, Y, n, r0, kb, int(r0), -1.0);
+                                                              Tp, r0, false);
+            // Y[r0:r0+kb, 0:r0] = -L_bb^-1 T
+            k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(kb, int(r0), kb, -1.0, Lb, NB, Tp, r0, 0.0, Y + r0 * n,
+                                                              n, false);
             c.launches += 2;
         }
-        k_set_identity_block<<<16, 256, 0, c.stream>>>(Y, n, r0, kb);
-        // the identity block occupies columns r0..r0+kb; solve in place on those columns only
-        k_trsm_left_lower<<<1, 256, 0, c.stream>>>(Lp, Y + r0, n, r0, kb, kb, 1.0);
-        c.launches += 2;
+        copy_block(Lb, NB, Y + r0 * n + r0, n, kb, kb);
         UGPU_LAUNCH_CHECK();
     }
     // Ainv = Y^T Y  (stored in L's buffer, then swapped)
