@@ -401,3 +401,26 @@ def test_ptap_reuse_recomputes_values_in_place(ctx):
     Bs = A.to_scipy() + sp.eye(A.nrows, k=2) + sp.eye(A.nrows, k=-2)  # same size, another pattern
     with pytest.raises(U.UgpuError):  # A with another structure than the product was formed from
         U.SparseMatrix(ctx, P.CSR.from_scipy(Bs)).ptap_reuse(Pg, out=Ac)
+
+
+@pytest.mark.parametrize("dtype", [U.F64, U.F32, U.BF16])
+@pytest.mark.parametrize("name", ["lognormal", "interp", "random"])
+def test_update_values_refreshes_the_spmv_layout(ctx, dtype, name):
+    """New values through ugpu_mat_update_values reach every SpMV layout (the sliced-ELL values are
+    refilled on the kept slice keys): the product equals a matrix created with those values."""
+    A = MATRICES[name]()
+    M = U.SparseMatrix(ctx, A)
+    if dtype != U.F64:
+        M = M.cast(dtype)
+    v2 = A.values * np.random.default_rng(9).uniform(-2.0, 2.0, A.nnz)
+    M.update_values(v2)
+    ref = U.SparseMatrix(ctx, P.CSR(A.nrows, A.ncols, A.rowptr, A.colidx, v2))
+    if dtype != U.F64:
+        ref = ref.cast(dtype)
+    vt = U.F64 if dtype == U.F64 else U.F32
+    x = U.Vector(ctx, np.random.default_rng(2).standard_normal(A.ncols).astype(np.float32 if vt == U.F32 else np.float64),
+                 dtype=vt)
+    y1, y2 = U.Vector(ctx, n=A.nrows, dtype=vt), U.Vector(ctx, n=A.nrows, dtype=vt)
+    M.apply(x, y1)
+    ref.apply(x, y2)
+    np.testing.assert_array_equal(y1.numpy(), y2.numpy())

@@ -101,8 +101,8 @@ void graph_assemble(Graph &g, const Vec &theta, Mat &A) {
                                                                 g.boundary.as<double>(), g.n, A.vals.as<double>());
     c.launches++;
     UGPU_LAUNCH_CHECK();
-    A.has_diag = false;
-    finalize_matrix(A);  // refresh the sliced-ELL copy of the values
+    refresh_values(A);  // refresh the sliced-ELL copy of the values
+    UGPU_CUDA(cudaStreamSynchronize(c.stream));
 }
 
 }  // namespace ugpu

@@ -186,6 +186,7 @@ struct Sell {
     // the shared-memory staged kernel); otherwise lane l owns rows l R + r at position l R + r
     bool interleaved = false;
     int xwin_max = 0;   // interleaved: most x-window floats one slice stages (staged kernel's grouping)
+    Buffer keys;        // int32[nslices * kMaxDiagSlots] slice keys of the analysis (values-only refresh)
 };
 
 struct PtapPlan;
@@ -210,6 +211,7 @@ void build_sell(Mat &A);
 void ensure_diag(Mat &A);
 void validate_csr(Mat &A);
 void finalize_matrix(Mat &A);
+void refresh_values(Mat &A);  // values changed, structure unchanged: refill the SpMV layout
 int64_t device_exclusive_scan(Context &ctx, const int64_t *in, int64_t *out, int64_t n);
 
 // ------------------------------------------------------------------------------------

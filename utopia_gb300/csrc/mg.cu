@@ -219,7 +219,7 @@ public:
                                        false);
                 if (!numeric) break;
                 if (fix) fix_semidefinite_operator(*ctx, *c.A64own);
-                else finalize_matrix(*c.A64own);
+                else refresh_values(*c.A64own);
             }
         }
         if (!numeric) {
@@ -667,8 +667,7 @@ void fix_semidefinite_operator(Context &ctx, Mat &J) {
     k_fix_semidefinite<<<stream_grid(ctx, J.nrows), kBlock, 0, ctx.stream>>>(
         J.rowptr.as<int32_t>(), J.colidx.as<int32_t>(), J.vals.as<double>(), J.nrows);
     ctx.launches++;
-    J.has_diag = false;
-    finalize_matrix(J);
+    refresh_values(J);
 }
 
 int mg_n_levels(const Solver *s) {

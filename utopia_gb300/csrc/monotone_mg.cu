@@ -212,8 +212,7 @@ private:
         // P_t^T: values gathered from P_t through the transpose's entry permutation
         if (Rt_ && Rt_->nnz == It_->nnz) {
             gather_values(*ctx, It_->nnz, It_->vals.as<double>(), rt_perm_.as<int64_t>(), Rt_->vals.as<double>());
-            Rt_->has_diag = false;
-            finalize_matrix(*Rt_);
+            refresh_values(*Rt_);
         } else {
             Rt_ = transpose_with_perm(*It_, rt_perm_, true);
         }
@@ -282,8 +281,7 @@ void MonotoneMultigrid::step(const Vec &b, Vec &x, const double *lb, const doubl
             k_mmg_truncate<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(
                 n, I.rowptr.as<int32_t>(), active_.as<int32_t>(), I.vals.as<double>(), It_->vals.as<double>());
             ctx->launches++;
-            It_->has_diag = false;
-            finalize_matrix(*It_);
+            refresh_values(*It_);
             galerkin();
         }
         // r = b - A x; r_H = P_t^T r

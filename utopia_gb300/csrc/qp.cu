@@ -898,8 +898,8 @@ public:
             UGPU_LAUNCH_CHECK();
             int changed = 0;
             UGPU_CUDA(cudaMemcpyAsync(&changed, changed_.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-            mat_->has_diag = false;
-            finalize_matrix(*mat_);  // new values: refresh the sliced-ELL copy
+            refresh_values(*mat_);  // new values: refresh the sliced-ELL copy
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));  // `changed` is read below
             enq_set(*ctx, UGPU_F64, n, 0.0, c, nullptr);
             if (!user_linear_) {
                 lin->set("atol", get("linear_rtol") * norm(res));

@@ -763,10 +763,7 @@ bool ptap_numeric(const Mat &A, const Mat &P, Mat &Ac, PtapPlan &pl, bool finali
     spgemm_numeric(A, P, *pl.AP, pl.s1);
     spgemm_numeric(*pl.R, *pl.AP, Ac, pl.s2);
     Ac.has_diag = false;
-    if (finalize) {
-        UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
-        finalize_matrix(Ac);
-    }
+    if (finalize) refresh_values(Ac);
     return true;
 }
 

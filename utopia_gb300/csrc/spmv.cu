@@ -1401,7 +1401,35 @@ void build_sell(Mat &A) {
     }
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));  // host vectors above must outlive the copies
     s->xwin_max = h_wmax;
+    s->keys = std::move(offs_tmp);  // kept: a later values-only refresh re-runs the fill alone
     A.sell = std::move(s);
+}
+
+// The values of A changed, its structure did not: the sliced-ELL values are filled again from
+// the CSR values with the slice keys of the analysis (a matrix without the layout is finalised)
+void refresh_values(Mat &A) {
+    A.has_diag = false;
+    Sell *s = A.sell.get();
+    if (!s || !s->keys.ptr || A.nnz == 0) {
+        finalize_matrix(A);
+        return;
+    }
+    Context &ctx = *A.ctx;
+    const int64_t ns = s->nslices;
+    if (ns == 0) return;
+    const int gA = int(std::min<int64_t>(ns, int64_t(ctx.sms) * 16));
+    auto fill = [&](auto tag) {
+        using V = decltype(tag);
+        k_sell_fill<V><<<gA, kAnalyzeThreads, 0, ctx.stream>>>(
+            A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), A.vals.as<V>(), A.nrows, A.ncols, s->S, ns,
+            s->slice_w.as<int32_t>(), s->slice_ptr.as<int64_t>(), s->slice_aux.as<int64_t>(), s->keys.as<int32_t>(),
+            s->offs.as<int32_t>(), s->cols.as<int32_t>(), s->vals.as<V>(), s->interleaved);
+    };
+    if (A.vdtype == UGPU_F64) fill(double{});
+    else if (A.vdtype == UGPU_F32) fill(float{});
+    else fill(__nv_bfloat16{});
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
 }
 
 void ensure_diag(Mat &A) {
@@ -1640,8 +1668,8 @@ int ugpu_mat_update_values(ugpu_mat *A, const double *values) {
         launch_convert(c, tmp.ptr, UGPU_F64, M.vals.ptr, M.vdtype, M.nnz);
         UGPU_CUDA(cudaStreamSynchronize(c.stream));
     }
-    M.has_diag = false;
-    finalize_matrix(M);
+    refresh_values(M);
+    UGPU_CUDA(cudaStreamSynchronize(c.stream));
     UGPU_ABI_END(A ? A->impl.ctx : nullptr)
 }
 
