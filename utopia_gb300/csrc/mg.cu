@@ -98,6 +98,13 @@ __global__ void k_pm_check(double *st, int *done, long long *it, double tol, lon
     st[2] = lambda;
 }
 
+// v = (1 / ||v||) v with ||v||^2 in dot[0] (the start vector's normalisation)
+__global__ void k_pm_normalise(int64_t n, const double *dot, double *__restrict__ v) {
+    const double s = 1. / sqrt(dot[0]);
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+        v[i] = s * v[i];
+}
+
 // v = (1 / lambda) y
 __global__ void k_pm_scale(int64_t n, const double *__restrict__ y, const double *lambda, const int *skip,
                            double *__restrict__ v) {
@@ -154,6 +161,11 @@ struct Level {
     Buffer r, c, c2, rR, p0, p1, rr;  // work vectors (vector dtype)
 };
 
+// power-method scratch of one level
+struct PmScratch {
+    Buffer v, w, st, part, cnt;  // st: [0] dot, [1] lambda, [2] lambda_old; int done, int skip, int64 it
+};
+
 struct Transfer {
     std::unique_ptr<Mat> P64, R64;    // FP64 interpolation and explicit restriction R = P^T
     std::unique_ptr<Mat> Pw, Rw;      // storage-precision copies
@@ -163,6 +175,12 @@ struct Transfer {
 
 class Multigrid final : public Solver {
 public:
+    ~Multigrid() override {
+        if (!pm_streams_.empty() || pm_fork_) cudaStreamSynchronize(ctx->stream);
+        for (auto st : pm_streams_) cudaStreamDestroy(st);
+        if (pm_fork_) cudaEventDestroy(pm_fork_);
+        if (pm_join_) cudaEventDestroy(pm_join_);
+    }
     explicit Multigrid(Context *c) : Solver(c, UGPU_SOLVER_MULTIGRID) {
         prm["pre_smoothing_steps"] = 3;   // utopia_MultiLevelBase.hpp:35-42
         prm["post_smoothing_steps"] = 3;
@@ -271,7 +289,11 @@ public:
         // Multigrid::update(): smoothers of levels 1..L-1 in order, then the coarse solver
         GlibcRand rng(uint32_t(get("rand_seed")));
         const int sm = int(get("smoother"));
-        for (int l = 1; l < L; ++l) setup_smoother(l, sm, rng);
+        for (int l = 1; l < L; ++l) setup_smoother(l, sm);
+        if (sm == 1) {
+            power_methods(rng);
+            for (int l = 1; l < L; ++l) chebyshev_coefficients(levels_[l]);
+        }
         UGPU_CHECK(coarse_.factor(*levels_[0].A64), UGPU_ERR_NOT_SPD,
                    "coarse operator is not symmetric positive definite");
         if (vdt_ == UGPU_F32) coarse_.make_fp32_inverse();
@@ -359,7 +381,9 @@ private:
     int vdt_ = UGPU_F64;
     bool ready_ = false;
     Buffer f64_r_, f64_z_;
-    Buffer pm_v_, pm_w_, pm_st_;  // power-method scratch
+    std::vector<PmScratch> pm_;            // power-method scratch per level
+    std::vector<cudaStream_t> pm_streams_;  // one stream per level for the concurrent power methods
+    cudaEvent_t pm_fork_ = nullptr, pm_join_ = nullptr;
 
     void make_masks() {
         const int L = n_levels();
@@ -401,7 +425,7 @@ private:
         UGPU_LAUNCH_CHECK();
     }
 
-    void setup_smoother(int l, int sm, GlibcRand &rng) {
+    void setup_smoother(int l, int sm) {
         Level &lv = levels_[l];
         Mat &A64 = const_cast<Mat &>(*lv.A64);
         ensure_diag(A64);
@@ -426,87 +450,127 @@ private:
                 int sdt = int(get("precision"));
                 lv.LU = (sdt == UGPU_F64) ? std::move(lu) : cast_matrix(*lu, sdt);
             }
-        } else {
-            power_method(lv, rng);
-            // Chebyshev3level::solve recurrence coefficients (utopia_Chebyshev3level.hpp:138-156)
-            const int nu = std::max(int(get("pre_smoothing_steps")), int(get("post_smoothing_steps")));
-            const double avg = (lv.emax + lv.emin) / 2.0, dif = (lv.emax - lv.emin) / 2.0;
-            lv.cheb_alpha.assign(std::max(nu, 1), 0.0);
-            lv.cheb_beta.assign(std::max(nu, 1), 0.0);
-            double alpha = 1.0 / avg;
-            lv.cheb_alpha[0] = alpha;
-            for (int k = 1; k < nu; ++k) {
-                double da = dif * alpha;
-                double beta = (k == 1 ? 0.5 : 0.25) * da * da;
-                alpha = 1.0 / (avg - (beta / alpha));
-                lv.cheb_beta[k] = beta;
-                lv.cheb_alpha[k] = alpha;
-            }
         }
     }
 
-    // PowerMethod::get_max_eig / compute_max_eig (utopia_PowerMethod.hpp:95-146) in FP64;
-    // Chebyshev3level::init_eigs scales the result (utopia_Chebyshev3level.hpp:118-121)
-    void power_method(Level &lv, GlibcRand &rng) {
-        const int64_t n = lv.n;
-        std::vector<double> h(n);
-        for (int64_t i = 0; i < n; ++i) h[i] = (double(rng.next()) / 2147483647.0) + 1;
-        Buffer &v = pm_v_, &w = pm_w_;
-        v.ensure(sizeof(double) * std::max<int64_t>(n, 1));
-        w.ensure(sizeof(double) * std::max<int64_t>(n, 1));
-        UGPU_CUDA(cudaMemcpyAsync(v.ptr, h.data(), sizeof(double) * n, cudaMemcpyHostToDevice, ctx->stream));
-        auto norm = [&](const Buffer &b) {
-            DotArgs d{};
-            d.nd = 1;
-            d.a[0] = d.b[0] = b.ptr;
-            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
-            double s;
-            host_dots(*ctx, n, d, &s);
-            return std::sqrt(s);
-        };
-        Vec vv;
-        vv.ctx = ctx;
-        vv.n = n;
-        vv.buf.borrow(v.ptr, v.bytes);
-        double s = 1. / norm(v);
-        launch_axpby(*ctx, n, s, vv, 0.0, vv);  // v = s * v
-        // the iterations run without host round trips: a device flag set by the convergence
-        // test predicates the later products, and `skip` the later rescalings
-        const double tol = get("power_method_tol");
-        const int64_t max_it = int64_t(get("power_method_max_it"));
-        Buffer &st = pm_st_;  // [0] dot, [1] lambda, [2] lambda_old; then int done, int skip, int64 it
-        st.ensure(3 * sizeof(double) + 2 * sizeof(int) + sizeof(long long));
-        UGPU_CUDA(cudaMemsetAsync(st.ptr, 0, st.bytes, ctx->stream));
-        double *dst = st.as<double>();
-        int *done = reinterpret_cast<int *>(dst + 3);
-        long long *itp = reinterpret_cast<long long *>(done + 2);
-        const int g = stream_grid(*ctx, n);
-        for (int64_t k = 0; k <= max_it + 1; ++k) {
-            SpmvArgs a;
-            a.x = v.ptr;
-            a.y = w.ptr;
-            a.vec_dtype = UGPU_F64;
-            a.done = done;
-            launch_spmv(*ctx, *lv.A64, a);
-            DotArgs d{};
-            d.nd = 1;
-            d.a[0] = d.b[0] = w.ptr;
-            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
-            launch_dots(*ctx, n, d, dst);
-            k_pm_check<<<1, 1, 0, ctx->stream>>>(dst, done, itp, tol, (long long)max_it);
-            k_pm_scale<<<g, kBlock, 0, ctx->stream>>>(n, w.as<double>(), dst + 1, done + 1, v.as<double>());
-            ctx->launches += 2;
+    // Chebyshev3level::solve recurrence coefficients (utopia_Chebyshev3level.hpp:138-156)
+    void chebyshev_coefficients(Level &lv) {
+        const int nu = std::max(int(get("pre_smoothing_steps")), int(get("post_smoothing_steps")));
+        const double avg = (lv.emax + lv.emin) / 2.0, dif = (lv.emax - lv.emin) / 2.0;
+        lv.cheb_alpha.assign(std::max(nu, 1), 0.0);
+        lv.cheb_beta.assign(std::max(nu, 1), 0.0);
+        double alpha = 1.0 / avg;
+        lv.cheb_alpha[0] = alpha;
+        for (int k = 1; k < nu; ++k) {
+            double da = dif * alpha;
+            double beta = (k == 1 ? 0.5 : 0.25) * da * da;
+            alpha = 1.0 / (avg - (beta / alpha));
+            lv.cheb_beta[k] = beta;
+            lv.cheb_alpha[k] = alpha;
         }
-        UGPU_LAUNCH_CHECK();
-        double hs[3];
-        int hd = 0;
-        UGPU_CUDA(cudaMemcpyAsync(hs, dst, sizeof(hs), cudaMemcpyDeviceToHost, ctx->stream));
-        UGPU_CUDA(cudaMemcpyAsync(&hd, done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-        UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
-        UGPU_CHECK(hd == 1, UGPU_ERR_INTERNAL, "power method: the stop test never held");
-        const double lambda = hs[1];
-        lv.emax = get("scale_max_eig") * lambda;
-        lv.emin = get("scale_min_eig") * lv.emax;
+    }
+
+    // PowerMethod::get_max_eig / compute_max_eig (utopia_PowerMethod.hpp:95-146) in FP64 for every
+    // smoothed level; Chebyshev3level::init_eigs scales the result (utopia_Chebyshev3level.hpp:118-121).
+    // The start vectors are drawn from the rand() sequence in level order (as the reference's
+    // levels are updated one after the other); the levels' iterations are independent, so they
+    // run concurrently on one stream per level (each with its own reduction scratch), joined
+    // back into the context's stream before the estimates are read.
+    void power_methods(GlibcRand &rng) {
+        const int L = n_levels();
+        const double tol = get("power_method_tol");
+        const long long max_it = (long long)get("power_method_max_it");
+        std::vector<std::vector<double>> h(L);
+        for (int l = 1; l < L; ++l) {
+            h[l].resize(size_t(levels_[l].n));
+            for (auto &x : h[l]) x = (double(rng.next()) / 2147483647.0) + 1;
+        }
+        if (pm_.size() < size_t(L)) pm_.resize(L);
+        while (pm_streams_.size() < size_t(L)) {
+            cudaStream_t st;
+            UGPU_CUDA(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            pm_streams_.push_back(st);
+        }
+        if (!pm_fork_) {
+            UGPU_CUDA(cudaEventCreateWithFlags(&pm_fork_, cudaEventDisableTiming));
+            UGPU_CUDA(cudaEventCreateWithFlags(&pm_join_, cudaEventDisableTiming));
+        }
+        cudaStream_t main = ctx->stream;
+        struct Restore {  // the context's stream is switched per level below
+            Context *c;
+            cudaStream_t s;
+            ~Restore() { c->stream = s; }
+        } restore{ctx, main};
+        for (int l = 1; l < L; ++l) {
+            const int64_t n = levels_[l].n;
+            PmScratch &ps = pm_[l];
+            ps.v.ensure(sizeof(double) * std::max<int64_t>(n, 1));
+            ps.w.ensure(sizeof(double) * std::max<int64_t>(n, 1));
+            ps.st.ensure(3 * sizeof(double) + 2 * sizeof(int) + sizeof(long long));
+            ps.part.ensure(sizeof(double) * kRedBlocks);
+            if (!ps.cnt.ptr) {  // reduction tickets; the last CTA of every reduction resets its ticket
+                ps.cnt.alloc(sizeof(unsigned int) * 4);
+                UGPU_CUDA(cudaMemsetAsync(ps.cnt.ptr, 0, ps.cnt.bytes, main));
+            }
+        }
+        UGPU_CUDA(cudaEventRecord(pm_fork_, main));
+        for (int l = 1; l < L; ++l) {
+            const Level &lv = levels_[l];
+            const int64_t n = lv.n;
+            PmScratch &ps = pm_[l];
+            UGPU_CUDA(cudaStreamWaitEvent(pm_streams_[l], pm_fork_, 0));
+            ctx->stream = pm_streams_[l];
+            double *dst = ps.st.as<double>();
+            int *done = reinterpret_cast<int *>(dst + 3);
+            long long *itp = reinterpret_cast<long long *>(done + 2);
+            const double *v = ps.v.as<double>(), *w = ps.w.as<double>();
+            UGPU_CUDA(cudaMemsetAsync(ps.st.ptr, 0, ps.st.bytes, ctx->stream));
+            if (n) UGPU_CUDA(cudaMemcpyAsync(ps.v.ptr, h[l].data(), sizeof(double) * n, cudaMemcpyHostToDevice,
+                                             ctx->stream));
+            DotArgs d{};
+            d.nd = 1;
+            d.dtype_a[0] = d.dtype_b[0] = UGPU_F64;
+            // v = v / ||v||
+            d.a[0] = d.b[0] = v;
+            launch_dots_into(*ctx, n, d, dst, ps.part.as<double>(), ps.cnt.as<unsigned int>());
+            const int g = stream_grid(*ctx, n);
+            k_pm_normalise<<<g, kBlock, 0, ctx->stream>>>(n, dst, ps.v.as<double>());
+            ctx->launches++;
+            // the iterations run without host round trips: a device flag set by the stop test
+            // predicates the later products, and `skip` the later rescalings
+            for (long long k = 0; k <= max_it + 1; ++k) {
+                SpmvArgs a;
+                a.x = v;
+                a.y = ps.w.ptr;
+                a.vec_dtype = UGPU_F64;
+                a.done = done;
+                launch_spmv(*ctx, *lv.A64, a);
+                d.a[0] = d.b[0] = w;
+                launch_dots_into(*ctx, n, d, dst, ps.part.as<double>(), ps.cnt.as<unsigned int>());
+                k_pm_check<<<1, 1, 0, ctx->stream>>>(dst, done, itp, tol, max_it);
+                k_pm_scale<<<g, kBlock, 0, ctx->stream>>>(n, w, dst + 1, done + 1, ps.v.as<double>());
+                ctx->launches += 2;
+            }
+            UGPU_LAUNCH_CHECK();
+            UGPU_CUDA(cudaEventRecord(pm_join_, ctx->stream));
+            UGPU_CUDA(cudaStreamWaitEvent(main, pm_join_, 0));
+        }
+        ctx->stream = main;
+        std::vector<double> hs(size_t(L) * 3);
+        std::vector<int> hd(size_t(L), 1);
+        for (int l = 1; l < L; ++l) {
+            UGPU_CUDA(cudaMemcpyAsync(&hs[size_t(l) * 3], pm_[l].st.ptr, 3 * sizeof(double), cudaMemcpyDeviceToHost,
+                                      main));
+            UGPU_CUDA(cudaMemcpyAsync(&hd[size_t(l)], pm_[l].st.as<double>() + 3, sizeof(int), cudaMemcpyDeviceToHost,
+                                      main));
+        }
+        UGPU_CUDA(cudaStreamSynchronize(main));
+        for (int l = 1; l < L; ++l) {
+            UGPU_CHECK(hd[size_t(l)] == 1, UGPU_ERR_INTERNAL, "power method: the stop test never held");
+            Level &lv = levels_[l];
+            lv.emax = get("scale_max_eig") * hs[size_t(l) * 3 + 1];
+            lv.emin = get("scale_min_eig") * lv.emax;
+        }
     }
 
     // ---------------------------------------------------------------- cycle ----
