@@ -226,8 +226,12 @@ UGPU_API int ugpu_jacobi_sweep(const ugpu_mat *A, const ugpu_vec *b, const ugpu_
  * utopia_ProjectedGaussSeidel.hpp:34-41 use_symmetric_sweep, n_local_sweeps) plus the
  * backend's own keys: "smoother" (0 Jacobi, 1 Chebyshev3level, 2 PointJacobi), "omega",
  * "precision" (UGPU_F64 / UGPU_F32 / UGPU_BF16 level storage of the multigrid), "flexible"
- * (flexible CG outer iteration), "fix_semidefinite_operators", "graph_batch" (iterations per
- * captured CUDA graph), "use_graphs", "multicolour" (PGS colouring), "format". */
+ * (flexible CG outer iteration), "fix_semidefinite_operators", "keep_galerkin_structure" (1: the
+ * Galerkin products keep their structure and an update with an operator of the same structure
+ * recomputes values only), "rand_seed" (power-method start vectors), "use_graphs" (1: a solve is
+ * one CUDA graph launch), "projected_gradient_stop" (PGS), "reset_initial_guess"; read-only
+ * results: "lambda_max" (MPRGP), "galerkin_assemblies", "n_active" (monotone multigrid).  The
+ * algebraic, BiCGStab, semismooth Newton and monotone multigrid keys are listed with their kinds. */
 UGPU_API int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out);
 UGPU_API int ugpu_solver_destroy(ugpu_solver *s);
 UGPU_API int ugpu_solver_set(ugpu_solver *s, const char *key, double value);
