@@ -148,8 +148,9 @@ UGPU_API int ugpu_pseudo_inverse(const ugpu_vec *in, ugpu_vec *out, double tol);
  * no synchronisation).  a, b: host arrays of k device pointers; dtype_a/dtype_b: their
  * element types.  Scratch is a fixed 38.9 KB device array inside the library (held by
  * every GPU that loads it until exit): k is limited to 8 pairs, larger k is rejected
- * with UGPU_ERR_ARG.  The first call on a device looks up the array's device address;
- * make that first call before any stream capture.  All calls share the one array, so
+ * with UGPU_ERR_ARG.  Each call looks up the array's device address in the current
+ * context; the first call in a context also loads the library's device module, so make
+ * that first call before any stream capture.  All calls share the one array, so
  * calls that overlap on the GPU (different streams, or several host threads) race. */
 UGPU_API int ugpu_dots_noalloc(int k, const void *const *a, const void *const *b, const int *dtype_a,
                                const int *dtype_b, int64_t n, double *d_out, void *stream);

@@ -1,7 +1,7 @@
 """Generate the committed fixtures under tests/golden/.
 
 1. Decode the reference's own PETSc-binary test inputs (read from the reference
-   checkout given as argv[1], default /root/reference) into .npz files:
+   checkout given as the first command-line argument, which is required) into .npz files:
    * utopia/data/laplace/matrices_for_petsc/{f_A, f_rhs, I_1, I_2, I_3}: the 4-level
      2D hierarchy of petsc_cg_mg / petsc_mg_jacobi
      (utopia/tests/petsc/utopia_PetscLinearSolverTest.cpp:400-508)
@@ -65,7 +65,9 @@ def structure_digest(rp, ci):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) < 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the utopia reference checkout>")
+    ref = sys.argv[1]
     base = os.path.join(ref, "utopia", "data")
     d = {}
     lap = os.path.join(base, "laplace", "matrices_for_petsc")

@@ -46,6 +46,28 @@ def test_dots_noalloc_matches_ugpu_dots(ctx):
         np.testing.assert_allclose(got, ref, rtol=1e-10)
 
 
+def test_dots_noalloc_allocates_nothing(ctx):
+    """After a first call (which loads the library's device module in this context), a
+    batch of calls leaves the device's free memory unchanged: nothing is allocated."""
+    import torch
+
+    lib = _abi.load()
+    rng = np.random.default_rng(12)
+    n = 300_001
+    va, vb = U.Vector(ctx, rng.standard_normal(n)), U.Vector(ctx, rng.standard_normal(n))
+    out = U.Vector(ctx, n=2)
+    assert _noalloc(lib, [(va, vb), (vb, vb)], n, out, ctx.stream) == 0
+    ctx.synchronize()
+    first = out.numpy()
+    free0, _ = torch.cuda.mem_get_info(0)
+    for _ in range(50):
+        assert _noalloc(lib, [(va, vb), (vb, vb)], n, out, ctx.stream) == 0
+    ctx.synchronize()
+    free1, _ = torch.cuda.mem_get_info(0)
+    assert free1 == free0
+    np.testing.assert_array_equal(out.numpy(), first)  # deterministic call to call
+
+
 def test_dots_noalloc_limits(ctx):
     lib = _abi.load()
     v = U.Vector(ctx, np.ones(10))

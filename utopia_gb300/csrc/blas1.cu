@@ -397,6 +397,8 @@ int ugpu_vec_wrap_device(ugpu_ctx *ctx, void *device_ptr, int64_t n, int dtype, 
     UGPU_REQUIRE(ctx);
     UGPU_REQUIRE(out);
     UGPU_CHECK(n == 0 || device_ptr, UGPU_ERR_ARG, "null device pointer");
+    UGPU_CHECK(dtype >= UGPU_F64 && dtype <= UGPU_BF16, UGPU_ERR_ARG, "unknown dtype");
+    UGPU_CHECK(n >= 0, UGPU_ERR_ARG, "negative length");
     auto v = std::make_unique<ugpu_vec>();
     v->impl.ctx = &ctx->impl;
     v->impl.n = n;
@@ -564,34 +566,26 @@ int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x) {
 // ticket) is a file-scope device array of fixed size, reserved in every GPU that loads
 // the library until the process exits.
 // ======================================================================================
-#include <mutex>
-
 namespace {
 
 constexpr int kNoAllocMaxPairs = kMaxDots;               // at most 8 dot pairs per call
 constexpr int kNoAllocPartials = kMaxDots * kRedBlocks;  // 4864 doubles of CTA partials
-constexpr int kNoAllocMaxDevices = 64;
 
 // [0, kNoAllocPartials): CTA partials; the next 32 doubles hold the last-CTA ticket
 // (38.9 KB in total)
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocPartials + 32];
 
-std::mutex g_noalloc_mutex;
-double *g_noalloc_ptr[kNoAllocMaxDevices] = {};
-
-// Device address of the scratch array on the current device.  The array's name is a
-// host-side stand-in in host code, so the address comes from cudaGetSymbolAddress,
-// once per device (the first call on a device performs this set-up).
-double *noalloc_scratch(int device) {
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[device]) {
-        double *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
-        if (e != cudaSuccess || !p)
-            throw Error(UGPU_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-        g_noalloc_ptr[device] = p;
-    }
-    return g_noalloc_ptr[device];
+// Device address of the scratch array in the current context.  The array's name is a
+// host-side stand-in in host code, so the address comes from cudaGetSymbolAddress.  It is
+// looked up on every call (cheap once the module is loaded), so a reset device or another
+// context on the same device never sees a stale address.  The first call in a context
+// loads the module's device globals, so it should come before any stream capture.
+double *noalloc_scratch() {
+    double *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void **>(&p), g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+        throw Error(UGPU_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    return p;
 }
 
 }  // namespace
@@ -616,17 +610,15 @@ extern "C" int ugpu_dots_noalloc(int k, const void *const *a, const void *const 
         args.dtype_a[i] = dtype_a[i];
         args.dtype_b[i] = dtype_b[i];
     }
-    int device = 0;
-    UGPU_CUDA(cudaGetDevice(&device));
-    UGPU_CHECK(device >= 0 && device < kNoAllocMaxDevices, UGPU_ERR_UNSUPPORTED, "dots_noalloc: device index");
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (n == 0) {
         UGPU_CUDA(cudaMemsetAsync(d_out, 0, sizeof(double) * k, s));
         return UGPU_OK;
     }
-    double *partials = noalloc_scratch(device);
+    double *partials = noalloc_scratch();
+    // The ticket starts at zero (the array is zero-initialised when the module loads) and
+    // the last CTA of every k_dots launch puts it back to zero, so no per-call clear.
     unsigned int *ticket = reinterpret_cast<unsigned int *>(partials + kNoAllocPartials);
-    UGPU_CUDA(cudaMemsetAsync(ticket, 0, sizeof(unsigned int), s));  // the ticket must start at zero
     bool all64 = true, all32 = true;
     for (int i = 0; i < k; ++i) {
         all64 &= args.dtype_a[i] == UGPU_F64 && args.dtype_b[i] == UGPU_F64;

@@ -499,8 +499,15 @@ private:
         struct Restore {  // the context's stream is switched per level below
             Context *c;
             cudaStream_t s;
-            ~Restore() { c->stream = s; }
-        } restore{ctx, main};
+            const std::vector<cudaStream_t> *level_streams;
+            int started = 0;  // level streams holding work the main stream has not joined
+            ~Restore() {
+                // on an exception part-way through, later work on the main stream must not
+                // run beside unfinished power-method kernels: wait for the started levels
+                for (int l = 1; l <= started; ++l) cudaStreamSynchronize((*level_streams)[size_t(l)]);
+                c->stream = s;
+            }
+        } restore{ctx, main, &pm_streams_};
         for (int l = 1; l < L; ++l) {
             const int64_t n = levels_[l].n;
             PmScratch &ps = pm_[l];
@@ -519,6 +526,7 @@ private:
             const int64_t n = lv.n;
             PmScratch &ps = pm_[l];
             UGPU_CUDA(cudaStreamWaitEvent(pm_streams_[l], pm_fork_, 0));
+            restore.started = l;
             ctx->stream = pm_streams_[l];
             double *dst = ps.st.as<double>();
             int *done = reinterpret_cast<int *>(dst + 3);
@@ -555,6 +563,7 @@ private:
             UGPU_CUDA(cudaEventRecord(pm_join_, ctx->stream));
             UGPU_CUDA(cudaStreamWaitEvent(main, pm_join_, 0));
         }
+        restore.started = 0;  // every level stream is joined into the main stream
         ctx->stream = main;
         std::vector<double> hs(size_t(L) * 3);
         std::vector<int> hd(size_t(L), 1);
