@@ -133,12 +133,13 @@ def oracle_setup(A, Ps):
     return O, Am, mg, time.perf_counter() - t0
 
 
-def oracle_solve(O, Am, mg, b):
+def oracle_solve(O, Am, mg, b, with_x=False):
     """One complete FP64 MG-PCG solve on the CPU oracle (hierarchy already built)."""
     nb = float(np.linalg.norm(b))
     t0 = time.perf_counter()
     x, st = O.cg_solve(Am, b, precond="mg", mg=mg, atol=RTOL * nb)
-    return time.perf_counter() - t0, st
+    dt = time.perf_counter() - t0
+    return (dt, st, x) if with_x else (dt, st)
 
 
 def run_reference(args):
@@ -556,12 +557,26 @@ def main():
                 + sum(p.rowptr.nbytes + p.colidx.nbytes + p.values.nbytes for p in Ps))
 
     cpu = None
+    parity = None
     if rank == 0 and not args.no_cpu and not args.profile:
         O, Aor, mgor, setup_s = oracle_setup(A, Ps)
-        dt, st = oracle_solve(O, Aor, mgor, b)
+        dt, st, x_or = oracle_solve(O, Aor, mgor, b, with_x=True)
         cpu = {"value": dt * 1e3, "unit": "ms", "cores": O.max_threads(), "kind": "port",
                "sample": f"one complete FP64 MG-PCG solve of the same {args.size}^3 problem on the oracle "
                          f"({st['iterates'] + 1} iterations); hierarchy set-up {setup_s:.1f} s untimed"}
+        # the GPU results against the oracle's solve of the same problem: Galerkin structure
+        # of every level, iteration counts and solutions
+        same_structure = True
+        for lev in range(mg_plain.n_levels() - 1):
+            rp, ci, _ = mg_plain.level_matrix(lev).csr()
+            orp, oci, _ = mgor.level_matrix(lev).arrays()
+            same_structure &= bool(np.array_equal(rp, orp) and np.array_equal(ci, oci))
+        nrm = float(np.linalg.norm(x_or))
+        parity = {"oracle_iterations": st["iterates"] + 1,
+                  "fp64_rel_err_vs_oracle": float(np.linalg.norm(x_plain - x_or) / nrm),
+                  "mixed_rel_err_vs_oracle": float(np.linalg.norm(x_mixed - x_or) / nrm),
+                  "fp64_iterations_minus_oracle": int(st_plain["iterates"] - st["iterates"]),
+                  "galerkin_structure_identical": same_structure, "levels": mg_plain.n_levels()}
 
     if rank == 0:
         line = {
@@ -580,6 +595,8 @@ def main():
             "fp64": {"ms": ms_plain, "iterations": st_plain["iterates"] + 1, "rel_residual_fp64": res_plain,
                      "setup_ms": setup_plain * 1e3},
             "speedup_mixed_vs_fp64": ms_plain / ms_mixed,
+            "speedup_fp64_gpu_vs_cpu": (cpu["value"] / ms_plain) if cpu else None,
+            "parity_vs_oracle": parity,
             "spmv": spmv,
             "roofline": roofline,
             "roofline_bf16_spmv": roofline_bf16,

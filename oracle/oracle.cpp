@@ -5,11 +5,11 @@
 // checker for the GPU library (tests, smoke() and the CPU-baseline leg of the
 // benchmark load it); the GPU library never links or calls it.
 //
-// The reference's own templates cannot be compiled here without its CMake
-// build (they include the generated utopia_Config.hpp) and their numeric
-// kernels live in PETSc 3.20.2 / BLAS, which are not available, so the
-// restatement below is checked against the reference's own test problems and
-// tolerances instead (parity of the restatement with a reference run is unpinned).
+// The restatement is pinned against the reference itself: oracle/ref/ compiles
+// the reference's own solver templates, unchanged, over a CPU CSR backend that
+// restates the PETSc kernels they call (PETSc 3.20.2 is not available), and
+// tests/test_oracle_ref.py checks that both agree bit for bit (iterations,
+// solutions, Galerkin operators, active sets) on the workloads' problems.
 //
 // Reduction order: every dot / norm sums fixed blocks of ORACLE_BLK entries in
 // index order and then the block partials in order, so results do not depend on
