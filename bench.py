@@ -272,6 +272,67 @@ def run_amg(args):
     print(json.dumps(out), flush=True)
 
 
+def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True):
+    """MPRGP and multicolour projected Gauss-Seidel on the N^2 obstacle problem (5-point
+    Laplacian, Gaussian-bump lower bound, seed 3) with b = -1 (scale None, the problem as
+    specified) or b = -scale h^2.  Complete solves timed by CUDA events on the library's
+    stream (operator, bounds and b resident); stop at the projected-gradient norm 1e-8
+    (MPRGP's own criterion; PGS stops on it too, evaluated every iteration)."""
+    import torch
+    import utopia_gb300 as U
+    from utopia_gb300 import problems as P
+
+    h = 1.0 / (N + 1)
+    A, b, lb, ub = P.obstacle_qp(N, seed=3, rhs=-1.0 if scale is None else -scale * h * h)
+    atol = 1e-8 if scale is None else 1e-8 * h * h
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    Am, bv, x = U.SparseMatrix(ctx, A), U.Vector(ctx, b), U.Vector(ctx, n=A.nrows)
+    lbv, ubv = U.Vector(ctx, lb), U.Vector(ctx, ub)
+    out = {"n": A.nrows, "b": "-1" if scale is None else f"-{scale:g} h^2", "atol": atol}
+    makers = {"mprgp": lambda: U.MPRGP(ctx, atol=atol, rtol=1e-30, max_it=max_it, use_graphs=0 if eager else 1)}
+    if pgs:
+        makers["pgs_multicolour"] = lambda: U.ProjectedGaussSeidel(
+            ctx, atol=atol, max_it=max_it, projected_gradient_stop=1, use_graphs=0 if eager else 1)
+    for name, make in makers.items():
+        s = make()
+        s.set_box_constraints(lbv, ubv)
+        s.update(Am)
+        times = []
+        for i in range(1 + max(1, steps)):
+            x.set(0.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            l0 = ctx.launch_count()
+            e0.record(stream)
+            s.apply(bv, x)
+            e1.record(stream)
+            e1.synchronize()
+            if i >= 1:
+                times.append(e0.elapsed_time(e1))
+            launches = ctx.launch_count() - l0
+        st = s.solution_status()
+        xg = x.numpy()
+        rec = {"ms": float(np.median(times)), "iterations": int(st["iterates"]), "converged": bool(st["converged"]),
+               "active_fraction": float((xg == lb).mean()), "gpu_launches": int(launches)}
+        rec["us_per_iteration"] = rec["ms"] * 1e3 / max(rec["iterations"], 1)
+        out[name] = rec
+    return out
+
+
+def run_qp(args):
+    """Box-constrained QP throughput (one JSON line): the 1024^2 obstacle problem as specified
+    (b = -1: every node ends in contact) and with b = -20 h^2 (a free boundary), MPRGP and
+    multicolour PGS, plus the per-iteration byte model of MPRGP's CG step."""
+    import utopia_gb300 as U
+
+    ctx = U.Context(0)
+    N = args.size if args.size != N_GRID else 1024
+    out = {"metric": f"box-QP time-to-solution, obstacle {N}^2", "unit": "ms", "higher_is_better": False}
+    out["as_specified"] = qp_measure(ctx, N, None, args.steps, eager=args.eager)
+    out["free_boundary"] = qp_measure(ctx, N, 20.0, args.steps, eager=args.eager, max_it=args.qp_max_it,
+                                      pgs=not args.no_pgs)
+    print(json.dumps(out), flush=True)
+
+
 def run_mmg(args):
     """MonotoneMultigrid on the 2D obstacle problem (5-point Laplacian on an N x N interior grid,
     b = -20 h^2, Gaussian-bump lower bound), 7-level geometric hierarchy: complete solves
@@ -354,6 +415,10 @@ def main():
                     help="AMG-PCG measurement (algebraic multigrid), one JSON line; not the headline metric")
     ap.add_argument("--mmg", action="store_true",
                     help="MonotoneMultigrid measurement (2D obstacle problem), one JSON line; not the headline metric")
+    ap.add_argument("--qp", action="store_true",
+                    help="box-constrained QP measurement (MPRGP, multicolour PGS on the 1024^2 obstacle problem)")
+    ap.add_argument("--qp-max-it", type=int, default=400000, help="iteration cap of the --qp free-boundary solves")
+    ap.add_argument("--no-pgs", action="store_true", help="--qp: MPRGP only")
     ap.add_argument("--cg-jacobi", action="store_true",
                     help="profiling case: four eager iterations of FP64 Jacobi-preconditioned CG, nothing else")
     ap.add_argument("--spmv-only", action="store_true",
@@ -374,6 +439,9 @@ def main():
         return
     if args.mmg:
         run_mmg(args)
+        return
+    if args.qp:
+        run_qp(args)
         return
 
     import torch

@@ -52,6 +52,27 @@ extern "C" {
 #define UGPU_EMIN 2
 #define UGPU_EMAX 3
 
+/* vector reductions (ugpu_vec_reduce) */
+#define UGPU_RED_SUM 0  /* sum_i v_i       (Reducible::reduce(Plus)) */
+#define UGPU_RED_MIN 1  /* min_i v_i       (Reducible::reduce(Min)) */
+#define UGPU_RED_MAX 2  /* max_i v_i       (Reducible::reduce(Max)) */
+#define UGPU_RED_ASUM 3 /* sum_i |v_i|     (Normed::norm1) */
+#define UGPU_RED_AMAX 4 /* max_i |v_i|     (Normed::norm_infty) */
+
+/* element-wise transforms (ugpu_vec_transform) */
+#define UGPU_TR_SQRT 0
+#define UGPU_TR_POW2 1
+#define UGPU_TR_LOG 2
+#define UGPU_TR_EXP 3
+#define UGPU_TR_COS 4
+#define UGPU_TR_SIN 5
+#define UGPU_TR_ABS 6
+#define UGPU_TR_MINUS 7
+#define UGPU_TR_POW 8        /* v^param */
+#define UGPU_TR_RECIPROCAL 9 /* param / v */
+#define UGPU_TR_SHIFT 10     /* v + param */
+#define UGPU_TR_SCALE 11     /* v * param */
+
 /* solver kinds */
 #define UGPU_SOLVER_CG 1          /* utopia::ConjugateGradient */
 #define UGPU_SOLVER_MULTIGRID 2   /* utopia::Multigrid */
@@ -140,6 +161,15 @@ UGPU_API int ugpu_norm2(const ugpu_vec *a, double *out);
 UGPU_API int ugpu_pointwise(int op, const ugpu_vec *a, const ugpu_vec *b, ugpu_vec *out);
 /* e_pseudo_inv (utopia/utopia_core/utopia_ElementWisePseudoInverse.hpp:20-65) */
 UGPU_API int ugpu_pseudo_inverse(const ugpu_vec *in, ugpu_vec *out, double tol);
+/* Reducible::reduce(Plus/Min/Max) and Normed::norm1/norm_infty
+ * (utopia/utopia_core/interfaces/utopia_Reducible.hpp:13-15, utopia_Normed.hpp:12-13; PETSc VecSum,
+ * VecMin, VecMax, VecNorm(NORM_1/NORM_INFINITY)); op = UGPU_RED_*, FP64 result, fixed order for sums.
+ * An empty vector gives 0. */
+UGPU_API int ugpu_vec_reduce(const ugpu_vec *v, int op, double *out);
+/* Transformable::transform (utopia/utopia_core/interfaces/utopia_Transformable.hpp:13-23; PETSc
+ * VecSqrtAbs/VecLog/VecExp/VecAbs/VecScale/VecShift/VecReciprocal): v = f(v), op = UGPU_TR_*,
+ * param for POW, RECIPROCAL, SHIFT and SCALE. */
+UGPU_API int ugpu_vec_transform(ugpu_vec *v, int op, double param);
 /* Allocation-free fused dots (no counterpart in the reference).  For callers that cannot
  * allocate device memory -- host codes whose device memory belongs to their own pool or
  * memory space, and hot loops that cannot afford cudaFree's device-wide synchronisation.

@@ -50,6 +50,9 @@
 #include "utopia_Vector.hpp"
 #include "utopia_Wrapper.hpp"
 
+#include "utopia_LinearSolver.hpp"
+#include "utopia_RowView.hpp"
+
 #include <algorithm>
 #include <cmath>
 #include <iostream>
@@ -759,6 +762,76 @@ public:
         RefMatrix::ptap(Eval<M2, Traits_>::apply(expr.left().right()), Eval<M1, Traits_>::apply(expr.right()),
                         result);
     }
+};
+
+
+// row access of the CSR backend (used by ProjectedGaussSeidel::step)
+template <class Tensor>
+class RowView<Tensor, 2, FillType::SPARSE, HOMEMADE> {
+public:
+    using SizeType = typename utopia::Traits<Tensor>::SizeType;
+    using Scalar = typename utopia::Traits<Tensor>::Scalar;
+
+    inline RowView(Tensor &t, const SizeType row) : t_(t), row_(row) {}
+    inline SizeType n_values() const { return t_.rowptr[size_t(row_) + 1] - t_.rowptr[size_t(row_)]; }
+    inline SizeType col(const SizeType index) const { return t_.colidx[size_t(t_.rowptr[size_t(row_)] + index)]; }
+    inline Scalar get(const SizeType index) const { return t_.vals[size_t(t_.rowptr[size_t(row_)] + index)]; }
+
+private:
+    Tensor &t_;
+    SizeType row_;
+};
+
+// dense Cholesky direct solver for the coarse level
+class RefCholesky final : public LinearSolver<RefMatrix, RefVector> {
+public:
+    RefCholesky *clone() const override { return new RefCholesky(*this); }
+    void update(const std::shared_ptr<const RefMatrix> &op) override {
+        LinearSolver<RefMatrix, RefVector>::update(op);
+        const RefMatrix &A = *op;
+        n_ = A.nrows;
+        L_.assign(size_t(n_ * n_), 0.0);
+        for (SizeType i = 0; i < n_; ++i)
+            for (int k = A.rowptr[size_t(i)]; k < A.rowptr[size_t(i) + 1]; ++k)
+                L_[size_t(i * n_ + A.colidx[size_t(k)])] = A.vals[size_t(k)];
+        ok_ = true;
+        for (SizeType j = 0; j < n_ && ok_; ++j) {
+            double s = L_[size_t(j * n_ + j)];
+            for (SizeType k = 0; k < j; ++k) s -= L_[size_t(j * n_ + k)] * L_[size_t(j * n_ + k)];
+            if (!(s > 0.0)) {
+                ok_ = false;
+                break;
+            }
+            const double ljj = std::sqrt(s);
+            L_[size_t(j * n_ + j)] = ljj;
+            for (SizeType i = j + 1; i < n_; ++i) {
+                double t = L_[size_t(i * n_ + j)];
+                for (SizeType k = 0; k < j; ++k) t -= L_[size_t(i * n_ + k)] * L_[size_t(j * n_ + k)];
+                L_[size_t(i * n_ + j)] = t / ljj;
+            }
+        }
+    }
+    bool apply(const RefVector &b, RefVector &x) override {
+        if (!ok_) throw std::runtime_error("coarse operator is not SPD");
+        if (x.size() != n_) x.zeros(RefTraits::Layout(SelfCommunicator(), n_, n_));
+        std::vector<double> y(static_cast<size_t>(n_), 0.0);
+        for (SizeType i = 0; i < n_; ++i) {
+            double s = b.get(i);
+            for (SizeType k = 0; k < i; ++k) s -= L_[size_t(i * n_ + k)] * y[size_t(k)];
+            y[size_t(i)] = s / L_[size_t(i * n_ + i)];
+        }
+        for (SizeType i = n_ - 1; i >= 0; --i) {
+            double s = y[size_t(i)];
+            for (SizeType k = i + 1; k < n_; ++k) s -= L_[size_t(k * n_ + i)] * x.get(k);
+            x.set(i, s / L_[size_t(i * n_ + i)]);
+        }
+        return true;
+    }
+
+private:
+    SizeType n_ = 0;
+    std::vector<double> L_;
+    bool ok_ = false;
 };
 
 }  // namespace utopia

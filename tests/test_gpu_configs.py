@@ -117,7 +117,7 @@ def test_obstacle1024_as_specified(ctx, oracle):
 
 def test_obstacle512_free_boundary(ctx, oracle):
     """b = -20 h^2: about a third of the nodes in contact; MPRGP bit-exact active set against
-    the oracle, PGS (stopped on the projected gradient) on the same active set."""
+    the oracle, multicolour PGS (stopped at ||x - x_old|| <= 1e-12) on the same active set."""
     N = 512
     h = 1.0 / (N + 1)
     A, b, lb, ub = P.obstacle_qp(N, seed=3, rhs=-20 * h * h)
@@ -132,7 +132,7 @@ def test_obstacle512_free_boundary(ctx, oracle):
     assert np.array_equal(xg == lb, xo == lb)
     assert rel(xg, xo) <= 1e-9
     assert abs(st["iterates"] - so["iterates"]) <= max(2, 0.02 * so["iterates"])
-    xp, sp = _pgs(ctx, A, b, lb, ub, atol=0.01 * atol, max_it=400000, projected_gradient_stop=1)
+    xp, sp = _pgs(ctx, A, b, lb, ub, stol=1e-12, max_it=400000)
     assert sp["converged"]
     assert np.array_equal(xp == lb, xo == lb)
     assert rel(xp, xo) <= 1e-9

@@ -168,6 +168,68 @@ __global__ void k_min2(int64_t n, const double *a, const double *b, double *part
     }
 }
 
+// Reducible / Normed reductions: sums in a fixed two-stage order, min/max as a min of
+// (optionally negated, absolute) values
+__global__ void k_vec_reduce(int op, int64_t n, const double *v, double *partials, double *out,
+                             unsigned int *counter) {
+    const bool is_sum = (op == UGPU_RED_SUM || op == UGPU_RED_ASUM);
+    double acc = is_sum ? 0.0 : DBL_MAX_D;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const double x = v[i];
+        switch (op) {
+            case UGPU_RED_SUM: acc += x; break;
+            case UGPU_RED_ASUM: acc += fabs(x); break;
+            case UGPU_RED_MIN: acc = fmin(acc, x); break;
+            case UGPU_RED_MAX: acc = fmin(acc, -x); break;
+            default: acc = fmin(acc, -fabs(x)); break;
+        }
+    }
+    if (is_sum) {
+        double a[1] = {acc};
+        block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
+        double s[1];
+        if (finish_last_block(1, partials, gridDim.x, s, counter) && threadIdx.x == 0) *out = s[0];
+        return;
+    }
+    acc = block_reduce_min(acc);
+    if (threadIdx.x == 0) partials[blockIdx.x] = acc;
+    __threadfence();
+    __shared__ bool last;
+    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
+    __syncthreads();
+    if (last) {
+        double m = DBL_MAX_D;
+        for (int j = threadIdx.x; j < gridDim.x; j += blockDim.x) m = fmin(m, __ldcg(partials + j));
+        m = block_reduce_min(m);
+        if (threadIdx.x == 0) {
+            *out = (op == UGPU_RED_MIN) ? m : -m;
+            *counter = 0;
+        }
+    }
+}
+
+__global__ void k_vec_transform(int op, int64_t n, double param, double *v) {
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+        const double x = v[i];
+        double r;
+        switch (op) {
+            case UGPU_TR_SQRT: r = sqrt(x); break;
+            case UGPU_TR_POW2: r = x * x; break;
+            case UGPU_TR_LOG: r = log(x); break;
+            case UGPU_TR_EXP: r = exp(x); break;
+            case UGPU_TR_COS: r = cos(x); break;
+            case UGPU_TR_SIN: r = sin(x); break;
+            case UGPU_TR_ABS: r = fabs(x); break;
+            case UGPU_TR_MINUS: r = -x; break;
+            case UGPU_TR_POW: r = pow(x, param); break;
+            case UGPU_TR_RECIPROCAL: r = param / x; break;
+            case UGPU_TR_SHIFT: r = x + param; break;
+            default: r = x * param; break;
+        }
+        v[i] = r;
+    }
+}
+
 }  // namespace
 
 int reduce_grid(int64_t n) {
@@ -539,6 +601,43 @@ int ugpu_multi_min(const ugpu_vec *a, const ugpu_vec *b, double *out) {
                "multi_min: FP64 vectors of equal size");
     *out = launch_min_reduce(*a->impl.ctx, a->impl.n, a->impl.as<double>(), b->impl.as<double>());
     UGPU_ABI_END(a ? a->impl.ctx : nullptr)
+}
+
+int ugpu_vec_reduce(const ugpu_vec *v, int op, double *out) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(v);
+    UGPU_REQUIRE(out);
+    UGPU_CHECK(v->impl.dtype == UGPU_F64, UGPU_ERR_ARG, "vec_reduce: FP64 vector");
+    UGPU_CHECK(op >= UGPU_RED_SUM && op <= UGPU_RED_AMAX, UGPU_ERR_ARG, "vec_reduce: unknown op");
+    Context &ctx = *v->impl.ctx;
+    const int64_t n = v->impl.n;
+    if (n == 0) {
+        *out = 0.0;
+        return UGPU_OK;
+    }
+    k_vec_reduce<<<reduce_grid(n), kBlock, 0, ctx.stream>>>(op, n, v->impl.as<double>(), ctx.d_partials(),
+                                                            ctx.d_scalars(), ctx.d_counters());
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    UGPU_CUDA(cudaMemcpyAsync(ctx.host_scalars, ctx.d_scalars(), sizeof(double), cudaMemcpyDeviceToHost, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    *out = ctx.host_scalars[0];
+    UGPU_ABI_END(v ? v->impl.ctx : nullptr)
+}
+
+int ugpu_vec_transform(ugpu_vec *v, int op, double param) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(v);
+    UGPU_CHECK(v->impl.dtype == UGPU_F64, UGPU_ERR_ARG, "vec_transform: FP64 vector");
+    UGPU_CHECK(op >= UGPU_TR_SQRT && op <= UGPU_TR_SCALE, UGPU_ERR_ARG, "vec_transform: unknown op");
+    Context &ctx = *v->impl.ctx;
+    const int64_t n = v->impl.n;
+    if (n) {
+        k_vec_transform<<<stream_grid(ctx, n), kBlock, 0, ctx.stream>>>(op, n, param, v->impl.as<double>());
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    UGPU_ABI_END(v ? v->impl.ctx : nullptr)
 }
 
 int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x) {
