@@ -149,4 +149,39 @@ __device__ __forceinline__ bool finish_last_block(int nd, const double *partials
     return true;
 }
 
+// ---- exact comparisons of doubles with integer operations ---------------------------
+// GB300 retires about two FP64 operations per clock per SM, so comparisons, minima and
+// selects of the box-constrained solvers run on the integer pipes instead: a double's bit
+// pattern, read as a signed-magnitude integer, orders like the double itself.  Operands are not
+// NaN (bounds, iterates); -0 and +0 compare equal, as in IEEE arithmetic.
+constexpr long long kMag = 0x7fffffffffffffffll;
+// signed key: a < b <=> dkey(a) < dkey(b) (-0 and +0 share the key 0)
+__device__ __forceinline__ long long dkey(double d) {
+    const long long u = __double_as_longlong(d);
+    return u < 0 ? -(u & kMag) : u;
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return dkey(a) < dkey(b); }
+// |d| < t for t > 0 (false for NaN, as the FP comparison)
+__device__ __forceinline__ bool dabs_lt(double d, double t) {
+    return (__double_as_longlong(d) & kMag) < __double_as_longlong(t);
+}
+// std::min(0.0, g) = (g < 0) ? g : 0.0 and std::max(0.0, g) = (0 < g) ? g : 0.0
+__device__ __forceinline__ double dmin0(double g) {
+    const long long u = __double_as_longlong(g);
+    return (u < 0 && (u & kMag) != 0 && (u & kMag) <= 0x7ff0000000000000ll) ? g : 0.0;
+}
+__device__ __forceinline__ double dmax0(double g) {
+    const long long u = __double_as_longlong(g);
+    return (u > 0 && u <= 0x7ff0000000000000ll) ? g : 0.0;
+}
+// order-preserving unsigned 64-bit keys of doubles (x < y <=> key(x) < key(y); -0 and +0 share
+// a key), so a minimum over doubles can be combined with atomicMin on the keys
+__device__ __forceinline__ unsigned long long qp_key(double d) {
+    return static_cast<unsigned long long>(dkey(d)) ^ 0x8000000000000000ull;
+}
+__device__ __forceinline__ double qp_unkey(unsigned long long k) {
+    const long long s = static_cast<long long>(k ^ 0x8000000000000000ull);
+    return __longlong_as_double(s < 0 ? ((-s) | static_cast<long long>(0x8000000000000000ull)) : s);
+}
+
 }  // namespace ugpu

@@ -280,6 +280,13 @@ struct SpmvArgs {
     unsigned int *dot_counter = nullptr;
     const int *done = nullptr;       // if set and *done != 0: the kernel does nothing
     const int *gate = nullptr;       // if set and *gate == 0: the kernel does nothing
+    // xmode 3 (box-constrained QP, FP64): input xin = *qmode ? x : xalt; with *qmode the step bound
+    // min over rows of (qx - qlb) / xin (xin > 0), (qx - qub) / xin (xin < 0), 1e15 is atomically
+    // min-combined into *qmin as an order-preserving key (qp_key)
+    const int *qmode = nullptr;
+    const void *xalt = nullptr;
+    const void *qx = nullptr, *qlb = nullptr, *qub = nullptr;
+    unsigned long long *qmin = nullptr;
     bool use_csr = false;
 };
 void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);

@@ -29,8 +29,9 @@ namespace {
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < (n); i += int64_t(gridDim.x) * blockDim.x)
 
 struct QpDev {
-    double beta_Abeta, g_betta;   // written by the proportioning SpMV (in this order)
-    double pAp, gp_dot;           // written by the CG SpMV (in this order)
+    double qa0, qa1;              // the iteration's product s -> A s: (s, A s), (s, g); s = p or beta
+    double neg_bsc;               // -beta_sc of the pending direction p = fi - beta_sc p (0: p = fi)
+    unsigned long long amin;      // key (qp_key) of alpha_f = min step bound, reset after each use
     double alpha_cg, alpha_f, beta_sc;
     double beta_beta, fi_fi, gnorm, gnorm0;
     long long it, iterates;
@@ -39,10 +40,17 @@ struct QpDev {
     int step;                           // 0: CG step, 1: expansion step
 };
 
-__device__ __forceinline__ double proj(double l, double u, double x) { return (l >= x) ? l : ((u <= x) ? u : x); }
-__device__ __forceinline__ double phi(double l, double u, double x, double g) { return (l < x && x < u) ? g : 0.0; }
+// the predicates of MPRGP / VariableBoundSolverInterface with their comparisons on the integer
+// pipes (device_util.cuh: exact for non-NaN bounds and iterates)
+__device__ __forceinline__ double proj(double l, double u, double x) {
+    const long long xk = dkey(x);
+    return (dkey(l) >= xk) ? l : ((dkey(u) <= xk) ? u : x);
+}
+__device__ __forceinline__ double phi(double l, double u, double x, double g) { return (dlt(l, x) && dlt(x, u)) ? g : 0.0; }
+// (|l - x| < 1e-14) ? min(0, g) : ((|u - x| < 1e-14) ? max(0, g) : 0)
 __device__ __forceinline__ double chopped(double l, double u, double x, double g) {
-    return (fabs(l - x) < 1e-14) ? fmin(0.0, g) : ((fabs(u - x) < 1e-14) ? fmax(0.0, g) : 0.0);
+    if (dabs_lt(l - x, 1e-14)) return dmin0(g);
+    return dabs_lt(u - x, 1e-14) ? dmax0(g) : 0.0;
 }
 
 __device__ __forceinline__ void qp_stop(QpDev *d, int reason, int converged) {
@@ -57,104 +65,162 @@ __global__ void k_qp_project(int64_t n, const double *lb, const double *ub, doub
     QP_LOOP(i, n) x[i] = proj(lb[i], ub[i], x[i]);
 }
 
-// c: alpha_cg = (g,p)/(p,Ap) (negative curvature stops), alpha_f = min(h1, h2), step choice
-__global__ void __launch_bounds__(kBlock) k_mprgp_alpha_f(int64_t n, const double *x, const double *p,
-                                                         const double *lb, const double *ub, QpDev *dev,
-                                                         double *partials, unsigned int *counter) {
-    if (dev->done || !dev->gate_cg) return;
-    if (dev->pAp <= 0.0) {
-        // `if (pAp <= 0.0) return true;` (negative curvature)
+// the iteration's direction: p = fi - beta_sc p after a CG step, p = fi otherwise (neg_bsc = 0)
+__global__ void __launch_bounds__(kBlock) k_mprgp_direction(int64_t n, double *p, const double *fi,
+                                                           const QpDev *dev) {
+    if (dev->done) return;
+    const double nb = dev->neg_bsc;
+    const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+    const int64_t nth = int64_t(gridDim.x) * blockDim.x;
+    const int64_t n2 = n >> 1;
+    double2 *p2 = reinterpret_cast<double2 *>(p);
+    const double2 *f2 = reinterpret_cast<const double2 *>(fi);
+#pragma unroll 4
+    for (int64_t j = tid; j < n2; j += nth) {
+        const double2 pv = p2[j], fv = f2[j];
+        p2[j] = make_double2(fma(nb, pv.x, fv.x), fma(nb, pv.y, fv.y));
+    }
+    if ((n & 1) && tid == 0) p[n - 1] = fma(nb, p[n - 1], fi[n - 1]);
+}
+
+// convergence test of the iteration that ends with the three dots s = {(beta, beta), (fi, fi),
+// (gp, gp)} (check_convergence(it, gnorm, gnorm / gnorm0, 1)) and the next branch
+__device__ __forceinline__ void mprgp_close_iteration(QpDev *dev, const double *s, double atol, double rtol,
+                                                      long long max_it) {
+    dev->beta_beta = s[0];
+    dev->fi_fi = s[1];
+    const double gnorm = sqrt(s[2]);
+    dev->gnorm = gnorm;
+    if (dev->it == 0) dev->gnorm0 = gnorm;
+    dev->it += 1;
+    const double rel = gnorm / dev->gnorm0;
+    int reason = 0;
+    if (gnorm <= atol) reason = UGPU_CONVERGED_FNORM_ABS;
+    if (rel <= rtol) reason = UGPU_CONVERGED_FNORM_RELATIVE;
+    if (dev->it >= max_it) reason = UGPU_DIVERGED_MAX_IT;
+    if (reason) qp_stop(dev, reason, reason > 0);
+    const int cgpath = s[0] <= s[1];  // beta_beta <= gamma^2 fi_fi, gamma = 1
+    dev->gate_cg = cgpath;
+    dev->gate_prop = !cgpath;
+}
+
+// One MPRGP iteration after its product (utopia_MPRGP.hpp:125-258).  The product kernel before it
+// took s (p on the CG path, beta on the proportioning path) and formed q = A s, the dots
+// qa0 = (s, q), qa1 = (s, g) and, on the CG path, the step bound alpha_f.  Every CTA takes the
+// same decisions from those scalars:
+//   negative curvature (qa0 <= 0)       -> stop
+//   CG path, alpha_cg <= alpha_f (CG)   -> x -= alpha_cg p, g -= alpha_cg Ap, next fi, beta, dots;
+//                                          p = fi - beta_sc p (beta_sc = (fi, Ap) / pAp) is formed by
+//                                          the next iteration's direction kernel
+//   CG path, expansion                  -> x = P(x - alpha_f p - alpha_bar phi(x - alpha_f p,
+//                                          g - alpha_f Ap)); g = A x - b and the rest follow in
+//                                          the gated product and closing kernels
+//   proportioning path                  -> x -= alpha beta, g -= alpha A beta, p = fi
+// and the last CTA closes the iteration (convergence, next branch, beta_sc, alpha_f reset).
+__global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, double *g, const double *p,
+                                                      double *fi, double *beta, const double *q,
+                                                      const double *lb, const double *ub, double alpha_bar,
+                                                      QpDev *dev, double *partials, unsigned int *counter,
+                                                      double atol, double rtol, long long max_it) {
+    if (dev->done) return;
+    const int cg = dev->gate_cg;
+    const double a0 = dev->qa0, a1 = dev->qa1;
+    if (a0 <= 0.0) {
+        // `if (pAp <= 0.0) return true;` / `if (beta_Abeta <= 0.0) return true;` (negative curvature)
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             qp_stop(dev, UGPU_DIVERGED_INDEFINITE, 1);
             dev->gate_exp = 0;
         }
         return;
     }
-    double m = DBL_MAX_D;
-    QP_LOOP(i, n) {
-        const double xi = x[i], pi = p[i];
-        const double h1 = (pi > 0) ? ((xi - lb[i]) / pi) : 1e15;
-        const double h2 = (pi < 0) ? ((xi - ub[i]) / pi) : 1e15;
-        m = fmin(m, fmin(h1, h2));
-    }
-    m = block_reduce_min(m);
-    if (threadIdx.x == 0) partials[blockIdx.x] = m;
-    __threadfence();
-    __shared__ bool last;
-    if (threadIdx.x == 0) last = (atomicAdd(counter, 1u) == gridDim.x - 1);
-    __syncthreads();
-    if (!last) return;
-    double v = DBL_MAX_D;
-    for (int j = threadIdx.x; j < gridDim.x; j += blockDim.x) v = fmin(v, __ldcg(partials + j));
-    v = block_reduce_min(v);
-    if (threadIdx.x == 0) {
-        const double alpha_cg = dev->gp_dot / dev->pAp;
-        dev->alpha_cg = alpha_cg;
-        dev->alpha_f = v;
-        dev->step = (alpha_cg <= v) ? 0 : 1;
-        dev->gate_exp = dev->step;
-        *counter = 0u;
-    }
-}
-
-// d: the row-local part of the taken branch
-__global__ void __launch_bounds__(kBlock) k_mprgp_update(int64_t n, double *x, double *g, const double *p,
-                                                        const double *Ap, const double *beta, const double *Abeta,
-                                                        const double *lb, const double *ub, double alpha_bar,
-                                                        QpDev *dev, double *partials, unsigned int *counter) {
-    if (dev->done) return;
-    const int prop = dev->gate_prop;
-    const int step = dev->step;
+    int step = 0;
     double alpha;
-    if (prop) {
-        if (dev->beta_Abeta <= 0.0) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) qp_stop(dev, UGPU_DIVERGED_INDEFINITE, 1);
-            return;
+    if (cg) {
+        const double alpha_cg = a1 / a0;
+        const double alpha_f = qp_unkey(dev->amin);
+        step = (alpha_cg <= alpha_f) ? 0 : 1;
+        alpha = step == 0 ? alpha_cg : alpha_f;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dev->alpha_cg = alpha_cg;
+            dev->alpha_f = alpha_f;
+            dev->step = step;
+            dev->gate_exp = step;
         }
-        alpha = dev->g_betta / dev->beta_Abeta;
     } else {
-        alpha = (step == 0) ? dev->alpha_cg : dev->alpha_f;
-    }
-    double acc = 0.0;
-    QP_LOOP(i, n) {
-        if (prop) {
-            x[i] = x[i] - alpha * beta[i];
-            g[i] = g[i] - alpha * Abeta[i];
-        } else {
-            const double xi = x[i] - alpha * p[i];
-            const double gi = g[i] - alpha * Ap[i];
-            g[i] = gi;
-            const double fi = phi(lb[i], ub[i], xi, gi);
-            if (step == 0) {
-                x[i] = xi;
-                acc = fma(fi, Ap[i], acc);
-            } else {
-                x[i] = proj(lb[i], ub[i], xi - alpha_bar * fi);
-            }
+        alpha = a1 / a0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            dev->step = 0;
+            dev->gate_exp = 0;
         }
     }
-    if (prop || step != 0) return;
-    double a[1] = {acc};
-    block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
-    double s[1];
-    if (finish_last_block(1, partials, gridDim.x, s, counter) && threadIdx.x == 0) dev->beta_sc = s[0] / dev->pAp;
+    double acc_fq = 0, acc_bb = 0, acc_ff = 0, acc_gg = 0;
+    QP_LOOP(i, n) {
+        const double l = lb[i], u = ub[i], xi = x[i], gi = g[i], qi = q[i];
+        if (cg) {
+            const double pn = p[i];  // the direction the product used
+            const double xn = xi - alpha * pn;
+            const double gn = gi - alpha * qi;
+            if (step == 0) {
+                x[i] = xn;
+                g[i] = gn;
+                const double f = phi(l, u, xn, gn);
+                const double b = chopped(l, u, xn, gn);
+                fi[i] = f;
+                beta[i] = b;
+                const double gp = f + b;
+                acc_fq = fma(f, qi, acc_fq);
+                acc_bb = fma(b, b, acc_bb);
+                acc_ff = fma(f, f, acc_ff);
+                acc_gg = fma(gp, gp, acc_gg);
+            } else {
+                x[i] = proj(l, u, xn - alpha_bar * phi(l, u, xn, gn));
+            }
+        } else {
+            const double xn = xi - alpha * beta[i];
+            const double gn = gi - alpha * qi;
+            x[i] = xn;
+            g[i] = gn;
+            const double f = phi(l, u, xn, gn);
+            const double b = chopped(l, u, xn, gn);
+            fi[i] = f;
+            beta[i] = b;
+            const double gp = f + b;
+            acc_bb = fma(b, b, acc_bb);
+            acc_ff = fma(f, f, acc_ff);
+            acc_gg = fma(gp, gp, acc_gg);
+        }
+    }
+    double a[4] = {acc_fq, acc_bb, acc_ff, acc_gg};
+    block_reduce_store<4>(a, 4, partials, gridDim.x, blockIdx.x);
+    double s[4];
+    if (finish_last_block(4, partials, gridDim.x, s, counter) && threadIdx.x == 0) {
+        dev->amin = qp_key(DBL_MAX_D);
+        if (cg && step == 1) return;  // expansion: closed by the gated product and closing kernels
+        const double bsc = cg ? s[0] / a0 : 0.0;
+        dev->beta_sc = bsc;
+        dev->neg_bsc = -bsc;
+        mprgp_close_iteration(dev, s + 1, atol, rtol, max_it);
+    }
 }
 
-// f: fi, beta, gp = fi + beta, next direction p, three dots, convergence and next branch
+// fi = phi(x, g), beta, p = fi, the three dots and the next branch: the start of the solve
+// (first = 1, no convergence test), and the end of an expansion step (first = 0: runs only when
+// the step kernel chose the expansion, after g = A x - b)
 __global__ void __launch_bounds__(kBlock) k_mprgp_final(int64_t n, const double *x, const double *g, double *p,
-                                                       double *beta, const double *lb, const double *ub, QpDev *dev,
-                                                       double *partials, unsigned int *counter, double atol,
-                                                       double rtol, long long max_it, int first) {
+                                                       double *fi_out, double *beta, const double *lb,
+                                                       const double *ub, QpDev *dev, double *partials,
+                                                       unsigned int *counter, double atol, double rtol,
+                                                       long long max_it, int first) {
     if (dev->done) return;
-    const bool cgstep = !first && dev->gate_cg && dev->step == 0;
-    const double bsc = cgstep ? dev->beta_sc : 0.0;
+    if (!first && !dev->gate_exp) return;
     double a0 = 0, a1 = 0, a2 = 0;
     QP_LOOP(i, n) {
         const double l = lb[i], u = ub[i], xi = x[i], gi = g[i];
         const double fi = phi(l, u, xi, gi);
         const double bi = chopped(l, u, xi, gi);
         beta[i] = bi;
-        p[i] = cgstep ? fi - bsc * p[i] : fi;
+        p[i] = fi;
+        fi_out[i] = fi;
         const double gp = fi + bi;
         a0 = fma(bi, bi, a0);
         a1 = fma(fi, fi, a1);
@@ -164,26 +230,18 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_final(int64_t n, const double 
     block_reduce_store<3>(a, 3, partials, gridDim.x, blockIdx.x);
     double s[3];
     if (finish_last_block(3, partials, gridDim.x, s, counter) && threadIdx.x == 0) {
-        dev->beta_beta = s[0];
-        dev->fi_fi = s[1];
-        if (!first) {
-            const double gnorm = sqrt(s[2]);
-            dev->gnorm = gnorm;
-            if (dev->it == 0) dev->gnorm0 = gnorm;
-            dev->it += 1;
-            // check_convergence(it, gnorm, gnorm / gnorm0, 1)
-            const double rel = gnorm / dev->gnorm0;
-            int reason = 0;
-            if (gnorm <= atol) reason = UGPU_CONVERGED_FNORM_ABS;
-            if (rel <= rtol) reason = UGPU_CONVERGED_FNORM_RELATIVE;
-            if (dev->it >= max_it) reason = UGPU_DIVERGED_MAX_IT;
-            if (reason) qp_stop(dev, reason, reason > 0);
-        }
-        const int cgpath = s[0] <= s[1];  // beta_beta <= gamma^2 fi_fi, gamma = 1
-        dev->gate_cg = cgpath;
-        dev->gate_prop = !cgpath;
+        dev->neg_bsc = 0.0;
         dev->gate_exp = 0;
         dev->step = 0;
+        if (first) {
+            dev->beta_beta = s[0];
+            dev->fi_fi = s[1];
+            const int cgpath = s[0] <= s[1];
+            dev->gate_cg = cgpath;
+            dev->gate_prop = !cgpath;
+        } else {
+            mprgp_close_iteration(dev, s, atol, rtol, max_it);
+        }
     }
 }
 
@@ -191,6 +249,7 @@ __global__ void k_qp_init(QpDev *d) {
     QpDev z{};
     z.gnorm = -1;
     z.gnorm0 = -1;
+    z.amin = qp_key(DBL_MAX_D);
     *d = z;
 }
 
@@ -417,7 +476,7 @@ public:
         UGPU_CHECK(A && A->nrows == A->ncols && A->vdtype == UGPU_F64, UGPU_ERR_ARG, "MPRGP: square FP64 operator");
         op = A;
         const size_t b = sizeof(double) * std::max<int64_t>(A->nrows, 1);
-        for (Buffer *v : {&fi_, &beta_, &p_, &Ap_, &Abeta_, &g_, &h1_, &h2_}) v->alloc(b);
+        for (Buffer *v : {&fi_, &beta_, &p_, &Ap_, &g_, &h1_, &h2_}) v->alloc(b);
         dev_.alloc(sizeof(QpDev));
         part_.alloc(sizeof(double) * 8 * std::max(kSpmvDotGrid, kRedBlocks));
         cnt_.alloc(sizeof(unsigned int) * 8);
@@ -469,7 +528,7 @@ public:
     }
 
 private:
-    Buffer fi_, beta_, p_, Ap_, Abeta_, g_, h1_, h2_, dev_, part_, cnt_;
+    Buffer fi_, beta_, p_, Ap_, g_, h1_, h2_, dev_, part_, cnt_;
     QpDev *host_ = nullptr;
     double alpha_bar_ = 1;
     const double *rhs_ = nullptr;
@@ -479,54 +538,54 @@ private:
     void final_kernel(double *x, const double *lb, const double *ub, int first) {
         const int64_t n = op->nrows;
         k_mprgp_final<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
-            n, x, g_.as<double>(), p_.as<double>(), beta_.as<double>(), lb, ub, dev_.as<QpDev>(),
+            n, x, g_.as<double>(), p_.as<double>(), fi_.as<double>(), beta_.as<double>(), lb, ub, dev_.as<QpDev>(),
             part_.as<double>() + 6 * kSpmvDotGrid, cnt_.as<unsigned int>() + 3, get("atol"), get("rtol"),
             (long long)get("max_it"), first);
         ctx->launches++;
         UGPU_LAUNCH_CHECK();
     }
 
+    // one MPRGP iteration: the direction p = fi - beta_sc p; the product of p (CG path) or beta
+    // (proportioning path, chosen on the device) with its two dots and, on the CG path, the step
+    // bound alpha_f; the step kernel; and, after an expansion step only, g = A x - b and the closing
+    // kernel
     void iteration(double *x, const double *lb, const double *ub) {
         const int64_t n = op->nrows;
         QpDev *dev = dev_.as<QpDev>();
         double *part = part_.as<double>();
         unsigned int *cnt = cnt_.as<unsigned int>();
-        {   // a: Ap = A p ; (p, Ap), (p, g)   [proportional branch]
+        {   // p = fi - beta_sc p (or fi)
+            const int gp = int(std::max<int64_t>(1, std::min<int64_t>((n / 2 + kBlock - 1) / kBlock,
+                                                                      int64_t(ctx->sms) * 8)));
+            k_mprgp_direction<<<gp, kBlock, 0, ctx->stream>>>(n, p_.as<double>(), fi_.as<double>(), dev);
+            ctx->launches++;
+            UGPU_LAUNCH_CHECK();
+        }
+        {
             SpmvArgs a;
+            a.xmode = 3;
             a.x = p_.ptr;
+            a.xalt = beta_.ptr;
+            a.qmode = &dev->gate_cg;
+            a.qx = x;
+            a.qlb = lb;
+            a.qub = ub;
+            a.qmin = &dev->amin;
             a.y = Ap_.ptr;
             a.vec_dtype = UGPU_F64;
             a.dot_partials = part;
             a.dv = g_.ptr;
-            a.dot_out = &dev->pAp;
+            a.dot_out = &dev->qa0;
             a.dot_counter = cnt + 0;
             a.done = &dev->done;
-            a.gate = &dev->gate_cg;
             launch_spmv(*ctx, *op, a);
         }
-        {   // b: Abeta = A beta ; (beta, Abeta), (beta, g)   [proportioning branch]
-            SpmvArgs a;
-            a.x = beta_.ptr;
-            a.y = Abeta_.ptr;
-            a.vec_dtype = UGPU_F64;
-            a.dot_partials = part + 2 * kSpmvDotGrid;
-            a.dv = g_.ptr;
-            a.dot_out = &dev->beta_Abeta;
-            a.dot_counter = cnt + 1;
-            a.done = &dev->done;
-            a.gate = &dev->gate_prop;
-            launch_spmv(*ctx, *op, a);
-        }
-        // c
-        k_mprgp_alpha_f<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, p_.as<double>(), lb, ub, dev,
-                                                                    part + 4 * kSpmvDotGrid, cnt + 2);
-        // d
-        k_mprgp_update<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
-            n, x, g_.as<double>(), p_.as<double>(), Ap_.as<double>(), beta_.as<double>(), Abeta_.as<double>(), lb,
-            ub, alpha_bar_, dev, part + 5 * kSpmvDotGrid, cnt + 4);
-        ctx->launches += 2;
+        k_mprgp_step<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
+            n, x, g_.as<double>(), p_.as<double>(), fi_.as<double>(), beta_.as<double>(), Ap_.as<double>(), lb, ub,
+            alpha_bar_, dev, part + 2 * kSpmvDotGrid, cnt + 4, get("atol"), get("rtol"), (long long)get("max_it"));
+        ctx->launches++;
         UGPU_LAUNCH_CHECK();
-        {   // e: g = A x - b   [expansion step]
+        {   // g = A x - b   [expansion step only]
             SpmvArgs a;
             a.x = x;
             a.v = rhs_;

@@ -313,8 +313,47 @@ struct EpiParams {
     unsigned int *dot_counter;
     const int *done;
     const int *gate;
+    // box-constrained QP input (XM 3): xin = qmode ? x : xalt, and with qmode the step bound (the
+    // minimum over rows of qp_alpha_f_key) folded into *qmin with atomicMin
+    const int *qmode;
+    const T *xalt;
+    const T *qx, *qlb, *qub;
+    unsigned long long *qmin;
     int vec_ok;      // every vector pointer above is 16-byte aligned
 };
+
+// the MPRGP step bound of one row as an order key (utopia_MPRGP.hpp:289-316, get_alpha_f:
+// min((p > 0) ? (x - l) / p : 1e15, (p < 0) ? (x - u) / p : 1e15)), one division, the
+// comparisons on the integer pipes
+__device__ __forceinline__ unsigned long long qp_alpha_f_key(double x, double p, double l, double u) {
+    const long long pk = dkey(p);
+    if (pk == 0) return qp_key(1e15);
+    const double h = (x - (pk > 0 ? l : u)) / p;
+    const unsigned long long hk = qp_key(h), big = qp_key(1e15);
+    return hk < big ? hk : big;
+}
+__device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+        v = w < v ? w : v;
+    }
+    return v;
+}
+// CTA minimum of the keys, folded into *out with one atomicMin (every thread of the CTA calls it)
+__device__ __forceinline__ void block_atomic_min_u64(unsigned long long v, unsigned long long *out) {
+    __shared__ unsigned long long sh[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_min_u64(v);
+    __syncthreads();
+    if (lane == 0) sh[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        unsigned long long t = lane < nw ? sh[lane] : ~0ull;
+        t = warp_min_u64(t);
+        if (lane == 0) atomicMin(out, t);
+    }
+}
 
 // R consecutive entries of a vector as 16-byte loads / stores (R * sizeof(T) is 16 or 32;
 // the caller guarantees 16-byte alignment)
@@ -340,9 +379,11 @@ __device__ __forceinline__ void st16(T *p, const T (&a)[R]) {
 // the product's input vector: x (XM 0), x + beta*p (XM 1), or w .* v formed on the fly
 // (XM 2: the first Jacobi iterate from zero, x1 = w .* rhs)
 template <class T, int XM>
-__device__ __forceinline__ T xin_at(const EpiParams<T> &e, T beta, int64_t j) {
+__device__ __forceinline__ T xin_at(const EpiParams<T> &e, T beta, int64_t j, bool qpc = false) {
     if constexpr (XM == 1) {
         return __ldg(e.x + j) + beta * __ldg(e.wvec + j);
+    } else if constexpr (XM == 3) {
+        return qpc ? __ldg(e.x + j) : __ldg(e.xalt + j);
     } else if constexpr (XM == 2) {
         return __ldg(e.w + j) * __ldg(e.v + j);
     } else {
@@ -438,7 +479,10 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     const V *vals = static_cast<const V *>(m.vals);
     T beta = T(0);
     if constexpr (XM == 1) beta = T(*e.beta_ptr);
+    bool qpc = false;
+    if constexpr (XM == 3) qpc = *e.qmode != 0;
     double dacc = 0.0, dacc2 = 0.0;
+    unsigned long long qmn = ~0ull;
     // Slices are interleaved over warps (neighbouring warps stream neighbouring slices, which
     // keeps DRAM pages and the x-gathers local).  Each slice's header is one 16-byte load;
     // headers are fetched two slices ahead and diagonal offsets one slice ahead, so a slice
@@ -497,7 +541,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 for (int r = 0; r < R; ++r) {
                     int c = r0i + r * rs + off;
                     c = c < 0 ? 0 : (c > cmax ? cmax : c);
-                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
+                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c, qpc), acc[r]);
                 }
             }
         } else if (w >= kAnchoredTag) {
@@ -516,7 +560,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 for (int r = 0; r < R; ++r) {
                     int c = gb[r] + off;
                     c = c < 0 ? 0 : (c > cmax ? cmax : c);
-                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c), acc[r]);
+                    acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c, qpc), acc[r]);
                 }
             }
         } else {
@@ -529,7 +573,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 VecLoad<V, R>::load(vals + base + int64_t(k) * S + lane * R, v);
                 load_cols<R>(cols + int64_t(k) * S + lane * R, c);
 #pragma unroll
-                for (int r = 0; r < R; ++r) acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c[r]), acc[r]);
+                for (int r = 0; r < R; ++r) acc[r] = fma(T(v[r]), xin_at<T, XM>(e, beta, c[r], qpc), acc[r]);
             }
         }
         constexpr bool kVecEpi = EPI != EPI_CHEB && EPI != EPI_CHEB0;
@@ -550,6 +594,22 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     ld16<T, R>(e.v + row0, b);
 #pragma unroll
                     for (int r = 0; r < R; ++r) xr[r] = a[r] * b[r];
+                } else if constexpr (XM == 3) {
+                    if (qpc) {
+                        T xx[R], l[R], u[R];
+                        ld16<T, R>(e.x + row0, xr);
+                        ld16<T, R>(e.qx + row0, xx);
+                        ld16<T, R>(e.qlb + row0, l);
+                        ld16<T, R>(e.qub + row0, u);
+#pragma unroll
+                        for (int r = 0; r < R; ++r) {
+                            const unsigned long long k = qp_alpha_f_key(double(xx[r]), double(xr[r]), double(l[r]),
+                                                                        double(u[r]));
+                            qmn = k < qmn ? k : qmn;
+                        }
+                    } else {
+                        ld16<T, R>(e.xalt + row0, xr);
+                    }
                 } else {
                     ld16<T, R>(e.x + row0, xr);
                 }
@@ -580,8 +640,15 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 const int64_t row = row0 + int64_t(r) * rs;
                 if (row < m.nrows) {
                     T xr = T(0);
-                    if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row);
+                    if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row, qpc);
                     if constexpr (XM == 1) e.pout[row] = xr;
+                    if constexpr (XM == 3) {
+                        if (qpc) {
+                            const unsigned long long k = qp_alpha_f_key(double(e.qx[row]), double(xr),
+                                                                        double(e.qlb[row]), double(e.qub[row]));
+                            qmn = k < qmn ? k : qmn;
+                        }
+                    }
                     T out = epilogue<T, EPI>(e, row, acc[r], xr);
                     e.y[row] = out;
                     if constexpr (DOT) {
@@ -591,6 +658,9 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                 }
             }
         }
+    }
+    if constexpr (XM == 3) {
+        if (qpc) block_atomic_min_u64(qmn, e.qmin);
     }
     if constexpr (DOT) {
         const int nd = e.dv ? 2 : 1;
@@ -1038,21 +1108,31 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
     const int64_t nwarps = (int64_t(gridDim.x) * blockDim.x) >> 5;
     T beta = T(0);
     if constexpr (XM == 1) beta = T(*e.beta_ptr);
+    bool qpc = false;
+    if constexpr (XM == 3) qpc = *e.qmode != 0;
     double dacc = 0.0, dacc2 = 0.0;
+    unsigned long long qmn = ~0ull;
     for (int64_t wb = warp0 * RPW; wb < nrows; wb += nwarps * RPW) {
         const int64_t row = wb + lane / G;
         T acc = T(0);
         if (row < nrows) {
             const int32_t k1 = __ldg(rp + row + 1);
             for (int32_t k = __ldg(rp + row) + sub; k < k1; k += G)
-                acc = fma(cvt<T>(__ldcs(cv + k)), xin_at<T, XM>(e, beta, __ldcs(ci + k)), acc);
+                acc = fma(cvt<T>(__ldcs(cv + k)), xin_at<T, XM>(e, beta, __ldcs(ci + k), qpc), acc);
         }
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o, G);
         if (row < nrows && sub == 0) {
             T xr = T(0);
-            if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row);
+            if constexpr (epi_reads_x<EPI, XM, DOT>()) xr = xin_at<T, XM>(e, beta, row, qpc);
             if constexpr (XM == 1) e.pout[row] = xr;
+            if constexpr (XM == 3) {
+                if (qpc) {
+                    const unsigned long long k = qp_alpha_f_key(double(e.qx[row]), double(xr), double(e.qlb[row]),
+                                                                double(e.qub[row]));
+                    qmn = k < qmn ? k : qmn;
+                }
+            }
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
             if constexpr (DOT) {
@@ -1060,6 +1140,9 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
                 if (e.dv) dacc2 = fma(double(xr), double(e.dv[row]), dacc2);
             }
         }
+    }
+    if constexpr (XM == 3) {
+        if (qpc) block_atomic_min_u64(qmn, e.qmin);
     }
     if constexpr (DOT) {
         const int nd = e.dv ? 2 : 1;
@@ -1092,8 +1175,15 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.dot_counter = a.dot_counter;
     e.done = a.done;
     e.gate = a.gate;
+    e.qmode = a.qmode;
+    e.xalt = static_cast<const T *>(a.xalt);
+    e.qx = static_cast<const T *>(a.qx);
+    e.qlb = static_cast<const T *>(a.qlb);
+    e.qub = static_cast<const T *>(a.qub);
+    e.qmin = a.qmin;
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
-    e.vec_ok = al(a.x) && al(a.p) && al(a.pout) && al(a.v) && al(a.w) && al(a.y) && al(a.dv);
+    e.vec_ok = al(a.x) && al(a.p) && al(a.pout) && al(a.v) && al(a.w) && al(a.y) && al(a.dv) && al(a.xalt) &&
+               al(a.qx) && al(a.qlb) && al(a.qub);
     return e;
 }
 
@@ -1259,9 +1349,19 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
 
 template <class V, class T>
 void dispatch_epi(Context &ctx, const Mat &A, const SpmvArgs &a) {
-    const int xm = a.p ? 1 : a.xmode;
+    const int xm = a.xmode == 3 ? 3 : (a.p ? 1 : a.xmode);  // 3: the QP input select
     const bool dot = a.dot_partials != nullptr;
-    UGPU_CHECK(xm >= 0 && xm <= 2, UGPU_ERR_INTERNAL, "unknown SpMV input mode");
+    UGPU_CHECK(xm >= 0 && xm <= 3, UGPU_ERR_INTERNAL, "unknown SpMV input mode");
+    if (xm == 3) {
+        // box-constrained QP input: FP64 only, product stored, two dots
+        UGPU_CHECK(a.epilogue == EPI_STORE && dot && a.qmode && a.qmin && a.xalt && a.qx && a.qlb && a.qub,
+                   UGPU_ERR_INTERNAL, "QP input mode: EPI_STORE with dots and the QP operands");
+        if constexpr (std::is_same<T, double>::value) {
+            dispatch_fmt<V, T, EPI_STORE, 3, true>(ctx, A, a);
+            return;
+        }
+        throw Error(UGPU_ERR_INTERNAL, "QP input mode needs FP64 vectors");
+    }
 #define UGPU_EPI_CASE(E)                                                                   \
     case E:                                                                                \
         UGPU_CHECK(xm == 0 && !dot, UGPU_ERR_INTERNAL, "fused forms need EPI_STORE/EPI_JACOBI"); \
