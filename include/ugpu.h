@@ -73,6 +73,10 @@ extern "C" {
 #define UGPU_TR_SHIFT 10     /* v + param */
 #define UGPU_TR_SCALE 11     /* v * param */
 
+/* index sets of a box-constrained iterate (ugpu_active_set_compact) */
+#define UGPU_SET_ACTIVE 0 /* |l_i - x_i| < 1e-14 or |u_i - x_i| < 1e-14 (MPRGP::get_beta's chopped set) */
+#define UGPU_SET_FREE 1   /* l_i < x_i < u_i                            (MPRGP::get_fi's free set) */
+
 /* solver kinds */
 #define UGPU_SOLVER_CG 1          /* utopia::ConjugateGradient */
 #define UGPU_SOLVER_MULTIGRID 2   /* utopia::Multigrid */
@@ -357,6 +361,13 @@ UGPU_API int ugpu_pattern_grad(const ugpu_mat *A, const ugpu_vec *lam, const ugp
 /* ---------------------------------------------------------------- box constraints ---- */
 /* project(lb, ub, x) (utopia/solvers/nonlinear/constrained/utopia_VariableBoundSolverInterface.hpp:134-155) */
 UGPU_API int ugpu_project(const ugpu_vec *lb, const ugpu_vec *ub, ugpu_vec *x);
+/* Active-set compaction (the predicates of MPRGP::get_beta / get_fi,
+ * utopia/solvers/nonlinear/constrained/quadratic_programming/utopia_MPRGP.hpp:266-348): the indices i
+ * of x in the set `which` (UGPU_SET_ACTIVE or UGPU_SET_FREE), ascending, written to the DEVICE int32
+ * array `indices` (capacity n; may be NULL to count only), their number to *count (synchronous).
+ * lb / ub may be NULL (unbounded side). */
+UGPU_API int ugpu_active_set_compact(const ugpu_vec *x, const ugpu_vec *lb, const ugpu_vec *ub, int which,
+                                     int32_t *indices, int64_t *count);
 
 #ifdef __cplusplus
 }

@@ -124,3 +124,53 @@ def test_semismooth_newton_matches_oracle(ctx, oracle):
     assert np.linalg.norm(xg - xr) <= 1e-9 * np.linalg.norm(xr)
     xm, _ = oracle.mprgp_solve(Am, b, lb, ub, atol=1e-12, max_it=50000)
     assert np.linalg.norm(xg - xm) <= 1e-6 * np.linalg.norm(xm)
+
+
+def test_active_set_compaction_matches_the_predicates(ctx):
+    """ugpu_active_set_compact against numpy on the MPRGP predicates, ties at 1e-14 included,
+    with and without an upper bound."""
+    rng = np.random.default_rng(5)
+    n = 1_000_003
+    lb = rng.uniform(-1, 0, n)
+    ub = lb + rng.uniform(0.5, 1.0, n)
+    x = lb + rng.uniform(0, 1, n) * (ub - lb)
+    k = rng.integers(0, n, 200_000)
+    x[k[:100_000]] = lb[k[:100_000]]                      # on the lower bound
+    x[k[100_000:150_000]] = lb[k[100_000:150_000]] + 5e-15  # inside the chop tolerance
+    x[k[150_000:]] = ub[k[150_000:]]                      # on the upper bound
+    vx, vl, vu = U.Vector(ctx, x), U.Vector(ctx, lb), U.Vector(ctx, ub)
+    act = (np.abs(lb - x) < 1e-14) | (np.abs(ub - x) < 1e-14)
+    free = (lb < x) & (x < ub)
+    np.testing.assert_array_equal(U.active_set(vx, vl, vu, U.SET_ACTIVE), np.flatnonzero(act))
+    np.testing.assert_array_equal(U.active_set(vx, vl, vu, U.SET_FREE), np.flatnonzero(free))
+    np.testing.assert_array_equal(U.active_set(vx, vl, None, U.SET_ACTIVE), np.flatnonzero(np.abs(lb - x) < 1e-14))
+    np.testing.assert_array_equal(U.active_set(vx, vl, None, U.SET_FREE), np.flatnonzero(lb < x))
+
+
+def test_mprgp_active_set_by_compaction(ctx, oracle):
+    """The MPRGP solution's active set, compacted on the device, equals the oracle's."""
+    A, b, lb, ub = obstacle(128, False)
+    xo, _ = oracle.mprgp_solve(oracle.Matrix(A), b, lb, ub, atol=1e-10, rtol=1e-14, max_it=5000)
+    s = U.MPRGP(ctx, atol=1e-10, rtol=1e-14, max_it=5000)
+    vlb, vub = U.Vector(ctx, lb), U.Vector(ctx, ub)
+    s.set_box_constraints(vlb, vub)
+    x = U.Vector(ctx, n=A.nrows)
+    s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    got = U.active_set(x, vlb, vub, U.SET_ACTIVE)
+    np.testing.assert_array_equal(got, np.flatnonzero((np.abs(lb - xo) < 1e-14) | (np.abs(ub - xo) < 1e-14)))
+
+
+def test_vector_reductions_and_transforms(ctx):
+    rng = np.random.default_rng(6)
+    v = rng.standard_normal(300_001)
+    dv = U.Vector(ctx, v)
+    np.testing.assert_allclose(U.reduce(dv, U.RED_SUM), v.sum(), rtol=1e-12)
+    assert U.reduce(dv, U.RED_MIN) == v.min() and U.reduce(dv, U.RED_MAX) == v.max()
+    np.testing.assert_allclose(U.reduce(dv, U.RED_ASUM), np.abs(v).sum(), rtol=1e-12)
+    assert U.reduce(dv, U.RED_AMAX) == np.abs(v).max()
+    lib = ctx.lib
+    for op, param, f in ((6, 0.0, np.abs), (7, 0.0, np.negative), (10, 2.5, lambda a: a + 2.5),
+                         (11, -3.0, lambda a: a * -3.0), (1, 0.0, lambda a: a * a)):
+        w = U.Vector(ctx, v)
+        assert lib.ugpu_vec_transform(w.h, op, param) == 0
+        np.testing.assert_allclose(w.numpy(), f(v), rtol=1e-15)

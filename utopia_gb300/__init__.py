@@ -170,6 +170,32 @@ def dots(pairs):
     return list(out)
 
 
+SET_ACTIVE, SET_FREE = 0, 1
+RED_SUM, RED_MIN, RED_MAX, RED_ASUM, RED_AMAX = 0, 1, 2, 3, 4
+
+
+def active_set(x: Vector, lb: Vector | None, ub: Vector | None, which=SET_ACTIVE):
+    """Indices (ascending, int32) of the active (|l - x| < 1e-14 or |u - x| < 1e-14) or free
+    (l < x < u) set of x, compacted on the device (ugpu_active_set_compact)."""
+    import torch
+
+    ctx = x.ctx
+    buf = torch.empty(max(x.n, 1), dtype=torch.int32, device=torch.device("cuda", torch.cuda.current_device()))
+    cnt = C.c_int64()
+    ctx.check(ctx.lib.ugpu_active_set_compact(x.h, lb.h if lb is not None else None,
+                                              ub.h if ub is not None else None, int(which),
+                                              C.c_void_p(buf.data_ptr()), C.byref(cnt)))
+    return buf[: cnt.value].cpu().numpy()
+
+
+def reduce(v: Vector, op: int) -> float:
+    """Reducible::reduce / Normed norms on the device (ugpu_vec_reduce): RED_SUM, RED_MIN, RED_MAX,
+    RED_ASUM (norm1), RED_AMAX (norm_infty)."""
+    out = C.c_double()
+    v.ctx.check(v.ctx.lib.ugpu_vec_reduce(v.h, int(op), C.byref(out)))
+    return out.value
+
+
 class SparseMatrix:
     """Device CSR matrix (``ugpu_mat``) with its sliced-ELL SpMV layout."""
 

@@ -212,6 +212,7 @@ void ensure_diag(Mat &A);
 void validate_csr(Mat &A);
 void finalize_matrix(Mat &A);
 void refresh_values(Mat &A);  // values changed, structure unchanged: refill the SpMV layout
+// exclusive scan of n int64 into out[0..n] (out holds n + 1 entries; out[n] = the total, returned)
 int64_t device_exclusive_scan(Context &ctx, const int64_t *in, int64_t *out, int64_t n);
 
 // ------------------------------------------------------------------------------------

@@ -245,6 +245,20 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_final(int64_t n, const double 
     }
 }
 
+// active-set compaction: flag[i] = row i is in the set, then the indices in ascending order
+__global__ void k_set_flags(int64_t n, const double *x, const double *lb, const double *ub, int which,
+                            int64_t *flag) {
+    QP_LOOP(i, n) {
+        const double l = lb ? lb[i] : -DBL_MAX_D, u = ub ? ub[i] : DBL_MAX_D, xi = x[i];
+        const bool in = which == UGPU_SET_FREE ? (dlt(l, xi) && dlt(xi, u))
+                                               : (dabs_lt(l - xi, 1e-14) || dabs_lt(u - xi, 1e-14));
+        flag[i] = in ? 1 : 0;
+    }
+}
+__global__ void k_set_scatter(int64_t n, const int64_t *flag, const int64_t *pos, int32_t *idx) {
+    QP_LOOP(i, n) if (flag[i]) idx[pos[i]] = int32_t(i);
+}
+
 __global__ void k_qp_init(QpDev *d) {
     QpDev z{};
     z.gnorm = -1;
@@ -1003,6 +1017,28 @@ std::unique_ptr<Solver> make_ssnewton(Context *c) { return std::make_unique<Semi
 std::unique_ptr<Solver> make_mprgp(Context *c) { return std::make_unique<Mprgp>(c); }
 std::unique_ptr<Solver> make_pgs(Context *c) { return std::make_unique<Pgs>(c); }
 
+// indices of the active (chopped) or free set of x in [lb, ub], ascending, into a device array;
+// returns their number (synchronous)
+int64_t active_set_compact(Context &ctx, int64_t n, const double *x, const double *lb, const double *ub, int which,
+                           int32_t *idx) {
+    if (n == 0) return 0;
+    Buffer flag, pos;
+    flag.alloc(sizeof(int64_t) * n);
+    pos.alloc(sizeof(int64_t) * (n + 1));  // the scan also writes the total at pos[n]
+    const int g = stream_grid(ctx, n);
+    k_set_flags<<<g, kBlock, 0, ctx.stream>>>(n, x, lb, ub, which, flag.as<int64_t>());
+    ctx.launches++;
+    UGPU_LAUNCH_CHECK();
+    const int64_t cnt = device_exclusive_scan(ctx, flag.as<int64_t>(), pos.as<int64_t>(), n);
+    if (idx && cnt) {
+        k_set_scatter<<<g, kBlock, 0, ctx.stream>>>(n, flag.as<int64_t>(), pos.as<int64_t>(), idx);
+        ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+    }
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    return cnt;
+}
+
 std::vector<int32_t> pgs_colouring(const Solver *s, int *ncolours) {
     auto p = dynamic_cast<const Pgs *>(s);
     UGPU_CHECK(p, UGPU_ERR_ARG, "not a projected Gauss-Seidel solver");
@@ -1022,4 +1058,21 @@ extern "C" int ugpu_pgs_colouring(const ugpu_solver *s, int32_t *colour, int *nc
     auto v = pgs_colouring(s->impl.get(), ncolours);
     if (colour) std::copy(v.begin(), v.end(), colour);
     UGPU_ABI_END(s ? s->impl->ctx : nullptr)
+}
+
+extern "C" int ugpu_active_set_compact(const ugpu_vec *x, const ugpu_vec *lb, const ugpu_vec *ub, int which,
+                                       int32_t *indices, int64_t *count) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(x);
+    UGPU_REQUIRE(count);
+    UGPU_CHECK(which == UGPU_SET_ACTIVE || which == UGPU_SET_FREE, UGPU_ERR_ARG, "active_set_compact: which");
+    UGPU_CHECK(x->impl.dtype == UGPU_F64, UGPU_ERR_ARG, "active_set_compact: FP64 vectors");
+    const int64_t n = x->impl.n;
+    UGPU_CHECK(n < (int64_t(1) << 31), UGPU_ERR_ARG, "active_set_compact: int32 indices");
+    for (const ugpu_vec *b : {lb, ub})
+        UGPU_CHECK(!b || (b->impl.n == n && b->impl.dtype == UGPU_F64), UGPU_ERR_ARG,
+                   "active_set_compact: bounds of the vector's size, FP64");
+    *count = active_set_compact(*x->impl.ctx, n, x->impl.as<double>(), lb ? lb->impl.as<double>() : nullptr,
+                                ub ? ub->impl.as<double>() : nullptr, which, indices);
+    UGPU_ABI_END(x ? x->impl.ctx : nullptr)
 }

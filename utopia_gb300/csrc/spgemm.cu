@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kWideThreads) k_spgemm_wide(const int *big_row
 
 }  // namespace
 
-// host: exclusive scan of n int64 -> out[0..n] (out[n] = total); returns total
+// host: exclusive scan of n int64 -> out[0..n] (out[n] = total: `out` holds n + 1 entries); returns total
 int64_t device_exclusive_scan(Context &ctx, const int64_t *in, int64_t *out, int64_t n) {
     const int64_t per = int64_t(kScanBlock) * kScanItems;
     const int64_t nb = (n + per - 1) / per;
