@@ -243,6 +243,15 @@ UGPU_API int ugpu_ptap_reuse(const ugpu_mat *A, const ugpu_mat *P, int reuse, ug
 UGPU_API int ugpu_spmv(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y);
 /* y = A x + v (MatMultAdd, utopia_petsc_Matrix.cpp:1400-1404); y may alias v */
 UGPU_API int ugpu_spmv_add(const ugpu_mat *A, const ugpu_vec *x, const ugpu_vec *v, ugpu_vec *y);
+/* Test of the staged product's bounded waits (no counterpart in the reference): y = A x through
+ * the shared-memory staged kernel (FP32 / BF16 operator, FP32 vectors) with every wait for a
+ * stage's copies limited to spin_cycles (1 .. 1e8) and, in the first CTA's first warp, no copy
+ * issued for its first slice, so that wait runs out.  The kernel then records the context's error
+ * flag, lets its other copies land and returns; the next synchronising call (ugpu_synchronize)
+ * returns UGPU_ERR_CUDA and clears the flag, and the context stays usable.  *launched = 0 when the
+ * operator does not take the staged kernel (nothing runs). */
+UGPU_API int ugpu_test_staged_wait_timeout(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y, int64_t spin_cycles,
+                                           int *launched);
 /* r = b - A x (Eval_Residual, utopia/utopia_core/eval/utopia_Eval_Residual.hpp:19-38), one pass */
 UGPU_API int ugpu_residual(const ugpu_mat *A, const ugpu_vec *b, const ugpu_vec *x, ugpu_vec *r);
 /* fused Jacobi sweep x_out = x + omega * d^+ (b - A x) (utopia/solvers/smoothers/utopia_Jacobi.hpp:131-141

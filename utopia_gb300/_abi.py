@@ -80,6 +80,7 @@ SIGNATURES = {
     "ugpu_vec_reduce": [_vp, _i32, C.POINTER(_d)],
     "ugpu_vec_transform": [_vp, _i32, _d],
     "ugpu_active_set_compact": [_vp, _vp, _vp, _i32, _vp, C.POINTER(_i64)],
+    "ugpu_test_staged_wait_timeout": [_vp, _vp, _vp, _i64, C.POINTER(_int)],
     "ugpu_dots_noalloc": [_int, _pp, _pp, C.POINTER(_int), C.POINTER(_int), _i64, _vp, _vp],
     "ugpu_csr_create": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _pp],
     "ugpu_csr_create_device": [_vp, _i64, _i64, _i64, _vp, _vp, _vp, _pp],

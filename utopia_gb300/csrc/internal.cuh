@@ -116,6 +116,7 @@ struct Context {
     Buffer scalars;    // generic device scalars (results of reductions), 256 doubles
     Buffer counters;   // last-CTA tickets of the reductions
     Buffer kflags;     // int[4] device error flags; [0]: a staged SpMV gave up waiting for its copies
+    long long staged_test_spin = 0;  // > 0 only inside ugpu_test_staged_wait_timeout
     double *host_scalars = nullptr;  // pinned mirror
     int64_t launches = 0;            // kernels launched through this context (instrumentation)
     Context(int dev);

@@ -696,6 +696,9 @@ constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[3
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
 
 struct StagedCfg {
+    long long spin;        // cycles a wait for a stage's copies may take before the kernel gives up
+    int withhold;          // test only: warp 0 of CTA 0 issues no copy for its first slice (the
+                           // expected bytes never arrive, so that wait runs out)
     int nst;               // stages per warp
     uint32_t warp_bytes;   // shared bytes per warp (barriers + descriptors + stages)
     uint32_t hdr_bytes;    // barriers + descriptors
@@ -730,12 +733,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// bounded wait for a stage's copies; false if they did not land within kStagedSpinCycles
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+// bounded wait for a stage's copies; false if they did not land within `spin` cycles
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, long long spin) {
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kStagedSpinCycles) return false;
+        if (clock64() - t0 > spin) return false;
     }
     return true;
 }
@@ -932,6 +935,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         __syncwarp();
         if (lane == 0) mbar_arrive_expect_tx(&bar[st], total);
         __syncwarp();
+        // test only: the first slice of warp 0 in CTA 0 gets no copy at all (nothing of that
+        // stage is in flight; its wait runs out)
+        if (cfg.withhold && blockIdx.x == 0 && wib == 0 && s == warp0) return;
         if (lane == 0 && vbytes) bulk_g2s(sg, vals + mt.base, vbytes, &bar[st]);
         if (start) {
             if constexpr (XM == 2) {
@@ -1076,7 +1082,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const int64_t s_next = s + int64_t(nst) * nwarps;
         const Meta mt = meta_of(hq);  // in flight while this slice is computed
         hq = load_hdr(s_next + nwarps);
-        if (!mbar_wait_bounded(&bar[st], uint32_t(it / nst) & 1u)) {
+        if (!mbar_wait_bounded(&bar[st], uint32_t(it / nst) & 1u, cfg.spin)) {
             ok = false;
             break;
         }
@@ -1089,7 +1095,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (lane == 0) atomicExch(kflag, 1);
         for (int j = 0; j < nst; ++j) {
             const int64_t s = warp0 + int64_t(it + j) * nwarps;
-            if (s < ns) mbar_wait_bounded(&bar[(it + j) % nst], uint32_t((it + j) / nst) & 1u);
+            if (s < ns) mbar_wait_bounded(&bar[(it + j) % nst], uint32_t((it + j) / nst) & 1u, cfg.spin);
         }
     }
 }
@@ -1286,6 +1292,8 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (best_nst == 0) return false;
     if (best_per_sm * kStagedWarps < kStagedMinWarps && s.nslices >= 16 * int64_t(ctx.sms)) return false;
     c.nst = best_nst;
+    c.spin = ctx.staged_test_spin > 0 ? ctx.staged_test_spin : kStagedSpinCycles;
+    c.withhold = ctx.staged_test_spin > 0 ? 1 : 0;
     c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
     const uint32_t cta = kStagedWarps * c.warp_bytes;
     SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
@@ -1666,6 +1674,39 @@ void check_spmv_vec(const Mat &A, const Vec *x, int64_t n, const char *what) {
 }  // namespace
 
 extern "C" {
+
+int ugpu_test_staged_wait_timeout(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y, int64_t spin_cycles,
+                                  int *launched) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(x);
+    UGPU_REQUIRE(y);
+    UGPU_REQUIRE(launched);
+    UGPU_CHECK(spin_cycles > 0 && spin_cycles <= 100000000ll, UGPU_ERR_ARG,
+               "test wait limit: 1 .. 1e8 cycles");
+    Context &ctx = *A->impl.ctx;
+    UGPU_CHECK(x->impl.dtype == UGPU_F32 && y->impl.dtype == UGPU_F32 && A->impl.vdtype != UGPU_F64, UGPU_ERR_ARG,
+               "the staged kernel takes FP32 / BF16 operators with FP32 vectors");
+    check_spmv_vec(A->impl, &x->impl, A->impl.ncols, "x");
+    check_spmv_vec(A->impl, &y->impl, A->impl.nrows, "y");
+    SpmvArgs a;
+    a.x = x->impl.data();
+    a.y = y->impl.data();
+    a.vec_dtype = UGPU_F32;
+    struct Reset {
+        Context &c;
+        ~Reset() { c.staged_test_spin = 0; }
+    } reset{ctx};
+    ctx.staged_test_spin = spin_cycles;
+    bool staged = false;
+    if (A->impl.sell && A->impl.format == UGPU_FORMAT_SELL) {
+        if (A->impl.vdtype == UGPU_F32) staged = staged_launch<float, EPI_STORE, 0>(ctx, A->impl, a);
+        else staged = staged_launch<__nv_bfloat16, EPI_STORE, 0>(ctx, A->impl, a);
+    }
+    UGPU_LAUNCH_CHECK();
+    *launched = staged ? 1 : 0;
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
 
 int ugpu_csr_create(ugpu_ctx *ctx, int64_t nrows, int64_t ncols, int64_t nnz, const int32_t *rowptr,
                     const int32_t *colidx, const double *values, ugpu_mat **out) {
