@@ -269,7 +269,8 @@ UGPU_API int ugpu_jacobi_sweep(const ugpu_mat *A, const ugpu_vec *b, const ugpu_
  * quadratic_programming/utopia_MPRGP.hpp:29-35 eig_comp_tol, power_method_max_it;
  * utopia_ProjectedGaussSeidel.hpp:34-41 use_symmetric_sweep, n_local_sweeps) plus the
  * backend's own keys: "smoother" (0 Jacobi, 1 Chebyshev3level, 2 PointJacobi), "omega",
- * "precision" (UGPU_F64 / UGPU_F32 / UGPU_BF16 level storage of the multigrid), "flexible"
+ * "precision" (UGPU_F64 / UGPU_F32 / UGPU_BF16 level storage of the multigrid; the coarse solve
+ * stays FP64 unless "coarse_fp32" = 1 applies an FP32 copy of the coarse inverse), "flexible"
  * (flexible CG outer iteration), "fix_semidefinite_operators", "keep_galerkin_structure" (1: the
  * Galerkin products keep their structure and an update with an operator of the same structure
  * recomputes values only), "rand_seed" (power-method start vectors), "use_graphs" (1: a solve is

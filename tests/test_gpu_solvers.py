@@ -239,3 +239,24 @@ def test_cholesky_solver_and_not_spd(ctx):
     with pytest.raises(U.UgpuError) as e:
         U.CholeskySolver(ctx).update(U.SparseMatrix(ctx, Aneg))
     assert e.value.code == -4
+
+
+@pytest.mark.parametrize("coarse_fp32", [0, 1])
+def test_mixed_coarse_solve_precision(ctx, oracle, coarse_fp32):
+    """The mixed V-cycle's coarse solve runs in FP64 (FP64 inverse and accumulation, FP32 vectors)
+    by default; coarse_fp32 = 1 applies an FP32 copy of the inverse.  Both reach 1e-8 (FP64
+    residual) and the FP64 oracle solution."""
+    A, Ps, b = P.lognormal_mg(48, 4, seed=2)
+    nb = np.linalg.norm(b)
+    Am = oracle.Matrix(A)
+    x64, _ = oracle.cg_solve(Am, b, precond="mg",
+                             mg=oracle.Multigrid(Am, Ps, smoother="jacobi", pre=2, post=2, omega=0.8),
+                             atol=1e-12 * nb)
+    mg = _mg(ctx, Ps, smoother="jacobi", omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+             precision=U.BF16, coarse_fp32=coarse_fp32)
+    s = cg(ctx, mg, atol=1e-8 * nb, flexible=1)
+    x = U.Vector(ctx, n=A.nrows)
+    assert s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+    xg = x.numpy()
+    assert np.linalg.norm(b - A.matvec(xg)) <= 1e-8 * nb
+    assert rel(xg, x64) <= 1e-6

@@ -299,6 +299,39 @@ bool DenseCholesky::factor(const Mat &A) {
     return true;
 }
 
+// x = Ainv * r in FP64 for FP32 vectors (the mixed V-cycle's coarse solve): r converted exactly to
+// FP64, the row sums accumulated in FP64 with the FP64 inverse, x rounded to FP32 once.
+__global__ void __launch_bounds__(kGemvThreads) k_gemv64_f32(const double *M, int64_t n, const float *r, float *x,
+                                                             const int *done, int vec) {
+    if (done && *done) return;
+    __shared__ double part[kGemvThreads / 32];
+    for (int64_t i = blockIdx.x; i < n; i += gridDim.x) {
+        const double *row = M + i * n;
+        double s = 0.0;
+        if (vec) {
+            const double2 *rv = reinterpret_cast<const double2 *>(row);
+            const float2 *xv = reinterpret_cast<const float2 *>(r);
+            for (int64_t c = threadIdx.x; c < n / 2; c += kGemvThreads) {
+                const double2 a = __ldg(rv + c);
+                const float2 b = __ldg(xv + c);
+                s = fma(a.x, f2d_bits(b.x), s);
+                s = fma(a.y, f2d_bits(b.y), s);
+            }
+        } else {
+            for (int64_t c = threadIdx.x; c < n; c += kGemvThreads) s = fma(__ldg(row + c), f2d_bits(__ldg(r + c)), s);
+        }
+        s = warp_sum(s);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            double t = threadIdx.x < kGemvThreads / 32 ? part[threadIdx.x] : 0.0;
+            t = warp_sum(t);
+            if (threadIdx.x == 0) x[i] = d2f_bits(t);
+        }
+        __syncthreads();
+    }
+}
+
 void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int *done) {
     Context &c = *ctx;
     if (n == 0) return;
@@ -309,11 +342,16 @@ void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int 
         const int vec = (n % 2 == 0) && al(Ainv.ptr) && al(rhs);
         k_gemv<double><<<g, kGemvThreads, 0, c.stream>>>(Ainv.as<double>(), n, static_cast<const double *>(rhs),
                                                           static_cast<double *>(x), done, vec);
-    } else if (rdt == UGPU_F32 && xdt == UGPU_F32) {
-        UGPU_CHECK(Ainv32.ptr != nullptr, UGPU_ERR_STATE, "coarse solve: FP32 inverse not prepared");
+    } else if (rdt == UGPU_F32 && xdt == UGPU_F32 && Ainv32.ptr) {
+        // FP32 inverse (only when make_fp32_inverse was called)
         const int vec = (n % 4 == 0) && al(Ainv32.ptr) && al(rhs);
         k_gemv<float><<<g, kGemvThreads, 0, c.stream>>>(Ainv32.as<float>(), n, static_cast<const float *>(rhs),
                                                          static_cast<float *>(x), done, vec);
+    } else if (rdt == UGPU_F32 && xdt == UGPU_F32) {
+        // FP64 solve for FP32 vectors
+        const int vec = (n % 2 == 0) && al(Ainv.ptr) && (reinterpret_cast<uintptr_t>(rhs) & 7u) == 0;
+        k_gemv64_f32<<<g, kGemvThreads, 0, c.stream>>>(Ainv.as<double>(), n, static_cast<const float *>(rhs),
+                                                       static_cast<float *>(x), done, vec);
     } else
         throw Error(UGPU_ERR_UNSUPPORTED, "coarse solve: FP64 or FP32 vectors");
     c.launches++;

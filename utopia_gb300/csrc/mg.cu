@@ -197,6 +197,7 @@ public:
         prm["power_method_max_it"] = 30;
         prm["rand_seed"] = 1;
         prm["mg_type"] = 1;               // V-cycle
+        prm["coarse_fp32"] = 0;           // mixed form: 1 applies an FP32 copy of the coarse inverse
     }
 
     void set_transfers(const std::vector<const Mat *> &P) {
@@ -296,7 +297,9 @@ public:
         }
         UGPU_CHECK(coarse_.factor(*levels_[0].A64), UGPU_ERR_NOT_SPD,
                    "coarse operator is not symmetric positive definite");
-        if (vdt_ == UGPU_F32) coarse_.make_fp32_inverse();
+        // the mixed V-cycle's coarse solve stays FP64 (FP64 inverse, FP64 accumulation) unless
+        // coarse_fp32 asks for the FP32 copy of the inverse
+        if (vdt_ == UGPU_F32 && get("coarse_fp32") != 0) coarse_.make_fp32_inverse();
         const size_t vs = dtype_size(vdt_);
         for (auto &l : levels_) {
             size_t b = vs * std::max<int64_t>(l.n, 1);
