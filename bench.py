@@ -11,13 +11,17 @@ Stop at ||r||_2 <= 1e-8 ||b||_2, checked in FP64.
   * value: wall time of the mixed-precision solve (FP64 flexible CG outer iteration,
     BF16-stored FP32 V-cycle), hierarchy already built, CUDA events on the library's
     stream; lower is better.  The plain FP64 form is timed the same way (fp64_ms).
-  * roofline: the dominant kernel of the solve timed alone with CUDA events.
+  * roofline: the FP64 form's dominant kernel (CG's product fused with (p, Ap)) timed alone
+    with CUDA events, against HBM (two byte models) and against the FP64 pipe.
   * e2e: the same solve through the public C ABI with host buffers: per step b is
     copied from pinned host memory, the solve runs, x is copied back (operator and
     hierarchy resident, as the reference's set-up is untimed too).  cold_path adds the
     operator/transfer upload and the hierarchy set-up.
   * cpu_baseline: the CPU oracle (a restatement of the reference's algorithms) on all
     host cores: one complete FP64 solve of the same problem (hierarchy built untimed).
+
+  * other_workloads: 256^2 CG + Jacobi, 128^3 FP64 MG-PCG (Chebyshev), the 1024^2 obstacle
+    QP (MPRGP, multicolour PGS) and the 128^3 differentiable solve (--no-extra skips them).
 
 --impl reference times only that CPU implementation (rank 0; other ranks exit).
 Multi-GPU: the path is not sharded here (one GPU per box); N ranks run N replicas.
@@ -43,6 +47,9 @@ N_GRID = 192
 LEVELS = 5
 RTOL = 1e-8
 METRIC = "MG-PCG time-to-1e-8 at 192^3 (mixed BF16/FP32 V-cycle in FP64 FCG)"
+# FP64 fused multiply-adds per second of one GB300, measured with a DFMA-bound kernel
+# (1.25 TFLOP/s, about two DFMA per clock per SM); FP64 mma.sync m8n8k4 measured 1.10 TFLOP/s
+FP64_FMA_PEAK = 0.625e12
 
 
 def peaks():
@@ -272,7 +279,7 @@ def run_amg(args):
     print(json.dumps(out), flush=True)
 
 
-def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True):
+def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True, pgs_max_it=None):
     """MPRGP and multicolour projected Gauss-Seidel on the N^2 obstacle problem (5-point
     Laplacian, Gaussian-bump lower bound, seed 3) with b = -1 (scale None, the problem as
     specified) or b = -scale h^2.  Complete solves timed by CUDA events on the library's
@@ -292,7 +299,7 @@ def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True):
     makers = {"mprgp": lambda: U.MPRGP(ctx, atol=atol, rtol=1e-30, max_it=max_it, use_graphs=0 if eager else 1)}
     if pgs:
         makers["pgs_multicolour"] = lambda: U.ProjectedGaussSeidel(
-            ctx, atol=atol, max_it=max_it, projected_gradient_stop=1, use_graphs=0 if eager else 1)
+            ctx, atol=atol, max_it=pgs_max_it or max_it, projected_gradient_stop=1, use_graphs=0 if eager else 1)
     for name, make in makers.items():
         s = make()
         s.set_box_constraints(lbv, ubv)
@@ -315,6 +322,132 @@ def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True):
                "active_fraction": float((xg == lb).mean()), "gpu_launches": int(launches)}
         rec["us_per_iteration"] = rec["ms"] * 1e3 / max(rec["iterations"], 1)
         out[name] = rec
+    return out
+
+
+def extra_workloads(ctx, args, stream):
+    """The other workloads of the path, measured on the same context (one JSON object each):
+    FP64 CG + Jacobi on 256^2 Poisson, FP64 MG-PCG (Chebyshev 3+3) on 128^3 Poisson, the
+    1024^2 obstacle QP (MPRGP, multicolour PGS) and the differentiable solve at 128^3
+    (forward with the mixed MG-PCG, adjoint solve and edge gradient).  Complete solves timed
+    by CUDA events on the library's stream, operators resident; the two CG workloads also
+    run on the oracle (host cores) and report their error against it."""
+    import torch
+    import utopia_gb300 as U
+    from utopia_gb300 import problems as P
+
+    def timed(fn, steps, warm=1):
+        ts = []
+        for i in range(warm + steps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            if i >= warm:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.median(ts))
+
+    out = {}
+    O = None
+    if not args.no_cpu:
+        import oracle as O
+
+        O.build()
+
+    # -- 256^2 Poisson, FP64 CG + Jacobi, rtol 1e-8 --
+    A, b = P.poisson2d_cg(256, 0)
+    nb = float(np.linalg.norm(b))
+    Am, bv, x = U.SparseMatrix(ctx, A), U.Vector(ctx, b), U.Vector(ctx, n=A.nrows)
+    cg = U.ConjugateGradient(ctx, atol=1e-8 * nb)
+    cg.set_preconditioner(U.InvDiagPreconditioner(ctx))
+    cg.update(Am)
+
+    def solve1():
+        x.set(0.0)
+        cg.apply(bv, x)
+
+    ms = timed(solve1, max(args.steps, 3))
+    st = cg.solution_status()
+    rec = {"workload": "FP64 CG + InvDiagPreconditioner, 2D 5-point Poisson 256^2 (n=65536), rtol 1e-8",
+           "ms": ms, "iterations": int(st["iterates"]), "us_per_iteration": ms * 1e3 / max(st["iterates"], 1),
+           "rel_residual_fp64": float(np.linalg.norm(b - A.matvec(x.numpy())) / nb)}
+    if O is not None:
+        Ao = O.Matrix(A)
+        t0 = time.perf_counter()
+        xo, so = O.cg_solve(Ao, b, atol=1e-8 * nb)
+        rec["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+        rec["iterations_minus_oracle"] = int(st["iterates"] - so["iterates"])
+        rec["rel_err_vs_oracle"] = float(np.linalg.norm(x.numpy() - xo) / np.linalg.norm(xo))
+    out["cg_jacobi_poisson2d_256"] = rec
+    del Am, bv, x, cg
+
+    # -- 128^3 Poisson, FP64 MG-PCG, 4 levels, Chebyshev 3+3, rtol 1e-10 --
+    A, Ps, b = P.poisson3d_mg(128, 4, seed=1)
+    nb = float(np.linalg.norm(b))
+    Am, bv, x = U.SparseMatrix(ctx, A), U.Vector(ctx, b), U.Vector(ctx, n=A.nrows)
+    mg = U.Multigrid(ctx, smoother="chebyshev", pre_smoothing_steps=3, post_smoothing_steps=3)
+    mg.set_transfer_operators([U.SparseMatrix(ctx, p) for p in Ps])
+    cg = U.ConjugateGradient(ctx, atol=1e-10 * nb)
+    cg.set_preconditioner(mg)
+    t0 = time.perf_counter()
+    cg.update(Am)
+    ctx.synchronize()
+    setup = (time.perf_counter() - t0) * 1e3
+
+    def solve2():
+        x.set(0.0)
+        cg.apply(bv, x)
+
+    ms = timed(solve2, max(args.steps // 4, 3))
+    st = cg.solution_status()
+    rec = {"workload": "FP64 MG-PCG, 3D 7-point Poisson 128^3 (n=2097152), 4 levels, Chebyshev 3+3, Galerkin "
+                       "RAP, dense Cholesky coarse, rtol 1e-10",
+           "ms": ms, "setup_ms": setup, "iterations": int(st["iterates"]) + 1,
+           "rel_residual_fp64": float(np.linalg.norm(b - A.matvec(x.numpy())) / nb)}
+    if O is not None:
+        Ao = O.Matrix(A)
+        omg = O.Multigrid(Ao, Ps, smoother="chebyshev", pre=3, post=3)
+        t0 = time.perf_counter()
+        xo, so = O.cg_solve(Ao, b, precond="mg", mg=omg, atol=1e-10 * nb)
+        rec["cpu_oracle_ms"] = (time.perf_counter() - t0) * 1e3
+        rec["iterations_minus_oracle"] = int(st["iterates"] - so["iterates"])
+        rec["rel_err_vs_oracle"] = float(np.linalg.norm(x.numpy() - xo) / np.linalg.norm(xo))
+    out["mgpcg_fp64_poisson3d_128"] = rec
+    del Am, bv, x, cg, mg
+
+    # -- 1024^2 obstacle: as specified (b = -1) and with a free boundary (b = -20 h^2) --
+    out["obstacle_1024"] = {
+        "as_specified": qp_measure(ctx, 1024, None, 2),
+        "free_boundary": qp_measure(ctx, 1024, 20.0, 1, pgs_max_it=2000),
+        "note": "PGS on the free-boundary case is capped at 2000 iterations: its per-iteration time is the figure"}
+
+    # -- differentiable solve at 128^3: forward (assembly, hierarchy, mixed MG-PCG to 1e-8),
+    #    backward (adjoint solve with the same hierarchy, edge gradient) --
+    from utopia_gb300.autograd import DifferentiableGraphSolver
+
+    G, theta, b, _ = P.graph_adjoint(128)
+    Ps = P.hierarchy_3d(128, 4)
+    ds = DifferentiableGraphSolver(ctx, G, Ps, precision=U.BF16, rtol=1e-8)
+    th = U.Vector(ctx, theta, dtype=U.F32)
+    bv, x, lam = U.Vector(ctx, b), U.Vector(ctx, n=G.n), U.Vector(ctx, n=G.n)
+    g = U.Vector(ctx, np.random.default_rng(6).standard_normal(G.n))
+    grad = U.Vector(ctx, n=G.E, dtype=U.F32)
+    ms_f = timed(lambda: ds.forward(th, bv, x), 2)
+
+    def backward():
+        ds.adjoint(g, lam)
+        ds.edge_grad(th, lam, x, grad)
+
+    ms_b = timed(backward, 2)
+    out["adjoint_graph_128"] = {
+        "workload": "x = A(theta)^-1 b on the 128^3 7-point graph (6,242,304 edges, FP32 theta), mixed MG-PCG "
+                    "(4 levels, BF16/FP32 V-cycle, FP64 FCG) at rtol 1e-8",
+        "forward_ms": ms_f, "backward_ms": ms_b, "ms": ms_f + ms_b,
+        "forward_iterations": int(ds.status["forward"]["iterates"]) + 1,
+        "adjoint_iterations": int(ds.status["adjoint"]["iterates"]) + 1,
+        "forward_includes": "assembly of A(theta), Galerkin hierarchy and coarse Cholesky, solve",
+        "backward_includes": "adjoint solve with the forward pass's hierarchy, edge-gradient kernel"}
     return out
 
 
@@ -407,6 +540,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--size", type=int, default=N_GRID)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the other workloads (256^2 CG, 128^3 MG-PCG, obstacle QP, adjoint) in the default line")
     ap.add_argument("--profile", action="store_true", help="one warm-up and one timed solve only (for ncu)")
     ap.add_argument("--eager", action="store_true",
                     help="launch every kernel individually instead of one graph per solve (ncu does not "
@@ -547,13 +682,19 @@ def main():
         e.synchronize()
         return s.elapsed_time(e) / reps * 1e-3
 
-    t_spmv = time_kernel(lambda: Am.apply(xr, y))
+    # the FP64 form's dominant kernel is CG's K1, the product fused with (p, Ap): timed as that
+    # launch (the dot left on the device), and the store-only product beside it
+    dotv = U.Vector(ctx, n=1)
+    t_spmv = time_kernel(lambda: Am.apply_dot(xr, y, out=dotv))
+    t_store = time_kernel(lambda: Am.apply(xr, y))
     csr_bytes = nnz * (8 + 4) + 4 * (n + 1) + 2 * n * 8
     sell = Am.sell_info()
     moved_bytes = sell["nstored"] * 8 + 2 * n * 8 + 4 * sell["nslices"] * 3
-    spmv = {"kernel": "k_sell_spmv<double,double,2,EPI_STORE>", "us": t_spmv * 1e6,
+    fp64_ops = sell["nstored"] + n  # one DFMA per stored slot, one per row for the dot
+    spmv = {"kernel": "k_sell_spmv<double,double,2,EPI_STORE,XM0,DOT> (product + (x, y))", "us": t_spmv * 1e6,
+            "store_only_us": t_store * 1e6,
             "csr_model_gbs": csr_bytes / t_spmv / 1e9, "format_bytes_gbs": moved_bytes / t_spmv / 1e9,
-            "csr_model_bytes": csr_bytes, "format_bytes": moved_bytes}
+            "csr_model_bytes": csr_bytes, "format_bytes": moved_bytes, "fp64_fma_per_launch": fp64_ops}
     Am.set_format(U.FORMAT_CSR)
     t_csr = time_kernel(lambda: Am.apply(xr, y))
     Am.set_format(U.FORMAT_SELL)
@@ -564,10 +705,14 @@ def main():
     traffic = 268.8e6 * nnz / 28518400
     roofline = {"bound": "hbm", "achieved": csr_bytes / t_spmv / 1e9, "peak": hbm, "unit": "GB/s",
                 "frac": csr_bytes / t_spmv / 1e9 / hbm, "traffic": traffic,
+                "format_frac": moved_bytes / t_spmv / 1e9 / hbm,
+                "fp64_pipe_frac": fp64_ops / t_spmv / FP64_FMA_PEAK,
                 "kernel": spmv["kernel"], "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
-                "bytes_model": "nnz*(8+4) + 4(n+1) + 2n*8 per launch (CSR model); the diagonal-keyed "
-                               "sliced ELL reads no column indices, format_bytes_gbs is the traffic it moves",
-                "limit": "FP64 pipe (GB300 ~1.6 DFMA/clk/SM; one DFMA per nonzero)"}
+                "bytes_model": "frac: nnz*(8+4) + 4(n+1) + 2n*8 per launch (the CSR model); format_frac: the "
+                               "bytes the diagonal-keyed sliced ELL moves (stored slots x 8 + 2n x 8 + slice "
+                               "headers; no column indices)",
+                "limit": f"FP64 pipe: fp64_pipe_frac of {FP64_FMA_PEAK / 1e9:.0f} G DFMA/s (measured GB300 "
+                         "DFMA throughput, 1.25 TFLOP/s; the FP64 tensor path, DMMA, measured 1.10 TFLOP/s)"}
     # the V-cycle's operator in the mixed form: BF16 values, FP32 vectors
     A16 = Am.cast(U.BF16)
     x16, y16 = U.Vector(ctx, np.ones(n, np.float32), dtype=U.F32), U.Vector(ctx, n=n, dtype=U.F32)
@@ -624,6 +769,10 @@ def main():
     cold_h2d = (A.rowptr.nbytes + A.colidx.nbytes + A.values.nbytes + b.nbytes
                 + sum(p.rowptr.nbytes + p.colidx.nbytes + p.values.nbytes for p in Ps))
 
+    others = None
+    if rank == 0 and not args.no_extra and not args.profile:
+        others = extra_workloads(ctx, args, stream)
+
     cpu = None
     parity = None
     if rank == 0 and not args.no_cpu and not args.profile:
@@ -673,6 +822,7 @@ def main():
                           "includes": "CSR + transfer upload from pageable host arrays, Galerkin hierarchy, "
                                       "coarse Cholesky, solve, download"},
             "cpu_baseline": cpu,
+            "other_workloads": others,
             "clocks": clk.summary(),
             "gpu_launches": int(launches),
         }

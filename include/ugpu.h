@@ -243,6 +243,12 @@ UGPU_API int ugpu_ptap_reuse(const ugpu_mat *A, const ugpu_mat *P, int reuse, ug
 UGPU_API int ugpu_spmv(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y);
 /* y = A x + v (MatMultAdd, utopia_petsc_Matrix.cpp:1400-1404); y may alias v */
 UGPU_API int ugpu_spmv_add(const ugpu_mat *A, const ugpu_vec *x, const ugpu_vec *v, ugpu_vec *y);
+/* y = A x and dot[0] = (x, y) in FP64 from the same kernel (the fused product and dot of CG's
+ * `Ap = A p; alpha = rho / dot(p, Ap)`, utopia_ConjugateGradient_impl.hpp:225-230).  dot: an FP64
+ * vector of at least one entry; the scalar stays on the device (asynchronous, like every vector
+ * operation of the stream).  The dot is a fixed-order two-stage reduction: repeated calls give
+ * identical bits.  A square operator. */
+UGPU_API int ugpu_spmv_dot(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y, ugpu_vec *dot);
 /* Test of the staged product's bounded waits (no counterpart in the reference): y = A x through
  * the shared-memory staged kernel (FP32 / BF16 operator, FP32 vectors) with every wait for a
  * stage's copies limited to spin_cycles (1 .. 1e8) and, in the first CTA's first warp, no copy

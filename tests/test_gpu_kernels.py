@@ -123,13 +123,31 @@ def test_spmv_fp64_matches_oracle(ctx, oracle, name):
     yref = oracle.Matrix(A).matvec(x)
     M = U.SparseMatrix(ctx, A)
     vx, vy = U.Vector(ctx, x), U.Vector(ctx, n=A.nrows)
-    scale = np.abs(A.values) @ np.ones(1) if False else None
     bound = 1e-14 * (np.abs(A.to_scipy()) @ np.abs(x)) + 1e-300
     for fmt in (U.FORMAT_SELL, U.FORMAT_CSR):
         M.set_format(fmt)
         M.apply(vx, vy)
         y = vy.numpy()
         assert np.all(np.abs(y - yref) <= 4 * bound), (name, fmt)
+
+
+@pytest.mark.parametrize("name", ["lap2d", "lap3d", "lognormal"])
+def test_spmv_dot_fused(ctx, name):
+    """y = A x and (x, y) from one kernel: y bit-identical to the plain product's, the dot within
+    1e-13 of numpy's (a different summation order) and identical over repeated calls."""
+    A = MATRICES[name]()
+    x = np.random.default_rng(2).standard_normal(A.ncols)
+    M = U.SparseMatrix(ctx, A)
+    vx, vy, vz = U.Vector(ctx, x), U.Vector(ctx, n=A.nrows), U.Vector(ctx, n=A.nrows)
+    for fmt in (U.FORMAT_SELL, U.FORMAT_CSR):
+        M.set_format(fmt)
+        M.apply(vx, vz)
+        d = M.apply_dot(vx, vy)
+        y = vy.numpy()
+        assert np.array_equal(y, vz.numpy()), (name, fmt)
+        ref = float(x @ y)
+        assert abs(d - ref) <= 1e-13 * (np.abs(x) @ np.abs(y)), (name, fmt)
+        assert M.apply_dot(vx, vy) == d
 
 
 def expected_diagonal_slots(A, S):

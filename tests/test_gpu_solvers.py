@@ -260,3 +260,37 @@ def test_mixed_coarse_solve_precision(ctx, oracle, coarse_fp32):
     xg = x.numpy()
     assert np.linalg.norm(b - A.matvec(xg)) <= 1e-8 * nb
     assert rel(xg, x64) <= 1e-6
+
+
+@pytest.mark.parametrize("smoother,precision,flexible",
+                         [("jacobi", U.F64, 0), ("point_jacobi", U.F64, 0), ("jacobi", U.F32, 1),
+                          ("jacobi", U.BF16, 1)])
+def test_folded_outer_dots(ctx, oracle, smoother, precision, flexible):
+    """fold_dots = 1: the V-cycle's last Jacobi sweep computes CG's (z, r) [and (z, Ap)] while it
+    writes z.  Same iterations as the separate dot kernel (fold_dots = 0), solutions within
+    round-off of each other, the FP64 form within 1e-9 of the oracle, and graph and eager runs
+    bit-identical."""
+    A, Ps, b = P.lognormal_mg(32, 3, seed=2)
+    nb = np.linalg.norm(b)
+    atol = (1e-10 if precision == U.F64 else 1e-8) * nb
+    Am = U.SparseMatrix(ctx, A)
+    out = {}
+    for fold, graphs in ((0, 1), (1, 1), (1, 0)):
+        mg = _mg(ctx, Ps, smoother=smoother, omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+                 precision=precision)
+        s = cg(ctx, mg, atol=atol, flexible=flexible, fold_dots=fold, use_graphs=graphs)
+        x = U.Vector(ctx, n=A.nrows)
+        assert s.solve(Am, U.Vector(ctx, b), x)
+        out[(fold, graphs)] = (x.numpy(), s.solution_status()["iterates"])
+    (x0, i0), (x1, i1), (x2, i2) = out[(0, 1)], out[(1, 1)], out[(1, 0)]
+    assert abs(i1 - i0) <= 1
+    assert i1 == i2 and np.array_equal(x1, x2)
+    assert rel(x1, x0) <= (1e-9 if precision == U.F64 else 1e-6)
+    assert np.linalg.norm(b - A.matvec(x1)) <= atol * 1.0001
+    if precision == U.F64:
+        Ao = oracle.Matrix(A)
+        xo, so = oracle.cg_solve(Ao, b, precond="mg",
+                                 mg=oracle.Multigrid(Ao, Ps, smoother=smoother, pre=2, post=2, omega=0.8),
+                                 atol=atol)
+        assert abs(i1 - so["iterates"]) <= 1
+        assert rel(x1, xo) <= 1e-9

@@ -301,6 +301,16 @@ class SparseMatrix:
     def apply(self, x: Vector, y: Vector):
         self.ctx.check(self.ctx.lib.ugpu_spmv(self.h, x.h, y.h))
 
+    def apply_dot(self, x: Vector, y: Vector, out: Vector | None = None) -> float | None:
+        """y = A x and (x, y) from one kernel.  With out (an FP64 vector), the dot is left in
+        out[0] on the device and nothing is returned; without, it is returned as a float."""
+        if out is not None:
+            self.ctx.check(self.ctx.lib.ugpu_spmv_dot(self.h, x.h, y.h, out.h))
+            return None
+        d = Vector(self.ctx, n=1)
+        self.ctx.check(self.ctx.lib.ugpu_spmv_dot(self.h, x.h, y.h, d.h))
+        return float(d.numpy()[0])
+
     def apply_add(self, x: Vector, v: Vector, y: Vector):
         self.ctx.check(self.ctx.lib.ugpu_spmv_add(self.h, x.h, v.h, y.h))
 

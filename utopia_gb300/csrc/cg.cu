@@ -20,6 +20,9 @@
 //   K2  alpha ; x += alpha p ; r -= alpha Ap ; ||r|| ; z = D^+ r ; (z,r) ; beta ; stop test
 // With a multigrid preconditioner: K0, K1, K2 (without z), the V-cycle, and
 //   K3  (z,r) [and (z,Ap)] ; beta ; max_it test
+// Where the V-cycle ends in a Jacobi / PointJacobi sweep (fold_dots = 1, the default), that
+// sweep computes (z,r) [and (z,Ap)] as it writes z, and K3 shrinks to one thread that
+// closes the iteration: z is not read back.
 // (K0 is not folded into the SpMV: gathering z and p per nonzero doubles the FP64 FMAs of
 // the product, and FP64 FMA throughput, not HBM, then bounds it on GB300.)
 #include <cmath>
@@ -163,6 +166,22 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
     }
 }
 
+// beta and the max_it test from sums = {(z, r) [, (z, Ap)]}
+__device__ __forceinline__ void cg_zclose(CgDev *dev, const double *sums, long long max_it, int flexible) {
+    if (flexible) {
+        // (p_new, r) without a dot over p: p_new = z + beta p and, after r -= alpha Ap,
+        // (p, r) = (p, r)_old - alpha (p, Ap)
+        const double beta = -sums[1] / dev->pAp;
+        dev->beta = beta;
+        dev->pr = sums[0] + beta * (dev->pr - dev->alpha * dev->pAp);
+    } else {
+        dev->beta = sums[0] / dev->rz;
+    }
+    dev->rz = sums[0];
+    if (dev->it >= max_it) cg_stop(dev, UGPU_DIVERGED_MAX_IT, 0);
+    else dev->it += 1;
+}
+
 // K3: (z, r) [and (z, Ap)] of the preconditioned residual; z may arrive in FP32
 // (mixed form).
 template <class ZT>
@@ -210,20 +229,15 @@ __global__ void __launch_bounds__(kBlock) k_cg_zdots(int64_t n, const ZT *__rest
     const int nd = flexible ? 2 : 1;
     block_reduce_store<2>(acc, nd, partials, gridDim.x, blockIdx.x);
     double sums[2];
-    if (finish_last_block(nd, partials, gridDim.x, sums, counter) && threadIdx.x == 0) {
-        if (flexible) {
-            // (p_new, r) without a dot over p: p_new = z + beta p and, after r -= alpha Ap,
-            // (p, r) = (p, r)_old - alpha (p, Ap)
-            const double beta = -sums[1] / dev->pAp;
-            dev->beta = beta;
-            dev->pr = sums[0] + beta * (dev->pr - dev->alpha * dev->pAp);
-        } else {
-            dev->beta = sums[0] / dev->rz;
-        }
-        dev->rz = sums[0];
-        if (dev->it >= max_it) cg_stop(dev, UGPU_DIVERGED_MAX_IT, 0);
-        else dev->it += 1;
-    }
+    if (finish_last_block(nd, partials, gridDim.x, sums, counter) && threadIdx.x == 0)
+        cg_zclose(dev, sums, max_it, flexible);
+}
+
+// K3 when the preconditioner's last kernel computed (z, r) [and (z, Ap)] into sums
+__global__ void k_cg_zfinish(CgDev *dev, const double *sums, long long max_it, int flexible) {
+    if (dev->done) return;
+    const double s[2] = {sums[0], flexible ? sums[1] : 0.0};
+    cg_zclose(dev, s, max_it, flexible);
 }
 
 // K0: p = z + beta p (z in FP64 or, for the mixed form, FP32)
@@ -310,6 +324,7 @@ public:
         prm["reset_initial_guess"] = 0;
         prm["flexible"] = 0;
         prm["use_graphs"] = 1;  // 1: the solve is one graph launch (conditional WHILE node)
+        prm["fold_dots"] = 1;   // 1: the preconditioner's last kernel computes (z,r) [and (z,Ap)]
     }
 
     void set_preconditioner(Solver *p) override {
@@ -341,7 +356,8 @@ public:
             z32_.alloc(sizeof(float) * std::max<int64_t>(n, 1));
         }
         dev_.alloc(sizeof(CgDev));
-        part_.alloc(sizeof(double) * 6 * std::max(kSpmvDotGrid, kRedBlocks));  // 3 regions x 2 dots
+        // 4 regions x 2 dots: K1, K2, K3 (or the folded dots' partials), the folded dots' sums
+        part_.alloc(sizeof(double) * 8 * std::max(kSpmvDotGrid, kRedBlocks));
         cnt_.alloc(sizeof(unsigned int) * 8);
         UGPU_CUDA(cudaMemsetAsync(cnt_.ptr, 0, cnt_.bytes, ctx->stream));
         if (!host_dev_) UGPU_CUDA(cudaMallocHost(&host_dev_, sizeof(CgDev)));
@@ -498,8 +514,24 @@ private:
         }
         if (mode_ != CG_GENERIC) return;
         // z = M r, then K3
-        pc_->pc_enqueue(f32 ? r32_.ptr : r_.ptr, f32 ? z32_.ptr : z_.ptr, &dev->done);
         const long long max_it = (long long)get("max_it");
+        void *z = f32 ? z32_.ptr : z_.ptr;
+        if (get("fold_dots") != 0) {
+            FinalDots fd;
+            fd.a = r_.as<double>();
+            fd.b = flexible_ ? Ap_.as<double>() : nullptr;
+            fd.partials = part + 4 * kSpmvDotGrid;
+            fd.out = part + 6 * kSpmvDotGrid;
+            fd.counter = cnt + 3;
+            if (pc_->pc_enqueue_dots(f32 ? r32_.ptr : r_.ptr, z, &dev->done, fd)) {
+                k_cg_zfinish<<<1, 1, 0, ctx->stream>>>(dev, fd.out, max_it, int(flexible_));
+                ctx->launches++;
+                UGPU_LAUNCH_CHECK();
+                return;
+            }
+        } else {
+            pc_->pc_enqueue(f32 ? r32_.ptr : r_.ptr, z, &dev->done);
+        }
         if (f32)
             k_cg_zdots<float><<<g, kBlock, 0, ctx->stream>>>(n, z32_.as<float>(), r_.as<double>(), Ap_.as<double>(),
                                                              dev, part + 4 * kSpmvDotGrid, cnt + 2, max_it,

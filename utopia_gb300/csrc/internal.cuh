@@ -289,6 +289,13 @@ struct SpmvArgs {
     const void *xalt = nullptr;
     const void *qx = nullptr, *qlb = nullptr, *qub = nullptr;
     unsigned long long *qmin = nullptr;
+    // final dots of the product's output y with FP64 vectors: fout[0] = (y, fa), fout[1] = (y, fb)
+    // (fb may be null), fixed-order two-stage reduction finished by the last CTA (fpart: per-CTA
+    // partials, fcnt: its ticket); set only on Jacobi / PointJacobi sweeps (a preconditioner's
+    // last kernel computing its outer Krylov iteration's dots)
+    const double *fa = nullptr, *fb = nullptr;
+    double *fpart = nullptr, *fout = nullptr;
+    unsigned int *fcnt = nullptr;
     bool use_csr = false;
 };
 void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);

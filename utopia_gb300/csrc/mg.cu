@@ -319,6 +319,23 @@ public:
         cycle(n_levels() - 1, r, z, done);
     }
 
+    // the V-cycle with the outer iteration's dots of z computed by the last fine-level
+    // post-smoothing sweep (Jacobi / PointJacobi smoothing with at least one post sweep and a
+    // coarse level); other configurations run the plain cycle
+    bool pc_enqueue_dots(const void *r, void *z, const int *done, const FinalDots &fd) override {
+        UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
+        if (int(get("smoother")) == 1 || int(get("post_smoothing_steps")) < 1 || n_levels() < 2) {
+            cycle(n_levels() - 1, r, z, done);
+            return false;
+        }
+        fd_ = &fd;
+        fd_used_ = false;
+        cycle(n_levels() - 1, r, z, done);
+        fd_ = nullptr;
+        UGPU_CHECK(fd_used_, UGPU_ERR_INTERNAL, "multigrid: the final dots were not attached");
+        return true;
+    }
+
     // Multigrid::apply as a stand-alone solver (utopia_Multigrid.hpp:162-238)
     void apply(const Vec &rhs, Vec &x) override {
         UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
@@ -585,6 +602,9 @@ private:
         }
     }
 
+    const FinalDots *fd_ = nullptr;  // set while pc_enqueue_dots runs its cycle
+    bool fd_used_ = false;
+
     // ---------------------------------------------------------------- cycle ----
     void spmv(const Mat &A, SpmvArgs a, const int *done) {
         a.vec_dtype = vdt_;
@@ -595,8 +615,9 @@ private:
     // smoothing sweeps of Jacobi / PointJacobi from the iterate in bufs[cur]; returns the
     // buffer index holding the result.  from_zero: the iterate is zero, so the first sweep
     // is x1 = w .* rhs and is folded into the second (its product gathers w .* rhs).
+    // fd: the outer iteration's dots, computed by the last sweep (post-smoothing only)
     int jacobi_sweeps(Level &lv, int sm, const void *rhs, void *bufs[2], int cur, int nu, bool from_zero,
-                      const int *done) {
+                      const int *done, const FinalDots *fd = nullptr) {
         const Mat &Aop = (sm == 2) ? *lv.LU : *lv.A();
         const int epi = (sm == 2) ? EPI_PJACOBI : EPI_JACOBI;
         int s = 0;
@@ -622,6 +643,14 @@ private:
             a.w = lv.w.ptr;
             a.y = bufs[cur ^ 1];
             a.epilogue = epi;
+            if (fd && s == nu - 1) {
+                a.fa = fd->a;
+                a.fb = fd->b;
+                a.fpart = fd->partials;
+                a.fout = fd->out;
+                a.fcnt = fd->counter;
+                fd_used_ = true;
+            }
             spmv(Aop, a, done);
             cur ^= 1;
         }
@@ -728,7 +757,7 @@ private:
         if (sm == 1) {
             chebyshev(lv, r, c, post, false, done);
         } else {
-            cur = jacobi_sweeps(lv, sm, r, bufs, cur, post, false, done);
+            cur = jacobi_sweeps(lv, sm, r, bufs, cur, post, false, done, l == n_levels() - 1 ? fd_ : nullptr);
             UGPU_CHECK(bufs[cur] == c_out, UGPU_ERR_INTERNAL, "multigrid: smoother buffer bookkeeping");
         }
     }

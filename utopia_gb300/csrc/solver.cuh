@@ -57,6 +57,19 @@ struct Solver {
     virtual void pc_enqueue(const void * /*r*/, void * /*z*/, const int * /*done*/) {
         throw Error(UGPU_ERR_UNSUPPORTED, "this solver cannot be used as a preconditioner");
     }
+    // the outer iteration's dots of z = M^{-1} r with FP64 vectors a, b (b may be null), for a
+    // preconditioner that can compute them in the kernel that writes z
+    struct FinalDots {
+        const double *a = nullptr, *b = nullptr;
+        double *partials = nullptr, *out = nullptr;
+        unsigned int *counter = nullptr;
+    };
+    // pc_enqueue, with out[0] = (z, a) [, out[1] = (z, b)] computed by its last kernel; returns false
+    // (and computes no dot) where the preconditioner cannot do that
+    virtual bool pc_enqueue_dots(const void *r, void *z, const int *done, const FinalDots & /*fd*/) {
+        pc_enqueue(r, z, done);
+        return false;
+    }
     virtual void set_box(const Vec *, const Vec *) {
         throw Error(UGPU_ERR_UNSUPPORTED, "this solver takes no box constraints");
     }

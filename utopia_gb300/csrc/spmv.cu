@@ -319,8 +319,28 @@ struct EpiParams {
     const T *xalt;
     const T *qx, *qlb, *qub;
     unsigned long long *qmin;
+    // final dots of y with FP64 vectors (SpmvArgs::fa, fb)
+    const double *fa, *fb;
+    double *fpart, *fout;
+    unsigned int *fcnt;
     int vec_ok;      // every vector pointer above is 16-byte aligned
 };
+
+// y_row's share of the final dots
+template <class T>
+__device__ __forceinline__ void final_dots_row(const EpiParams<T> &e, int64_t row, T y, double &f0, double &f1) {
+    const double yd = cvt<double>(y);
+    f0 = fma(yd, __ldg(e.fa + row), f0);
+    if (e.fb) f1 = fma(yd, __ldg(e.fb + row), f1);
+}
+// the CTA's final-dot partials, finished by the last CTA (every thread of the CTA calls it)
+template <class T>
+__device__ __forceinline__ void final_dots_finish(const EpiParams<T> &e, double f0, double f1) {
+    const int nd = e.fb ? 2 : 1;
+    double a[2] = {f0, f1};
+    block_reduce_store<2>(a, nd, e.fpart, gridDim.x, blockIdx.x);
+    finish_last_block(nd, e.fpart, gridDim.x, e.fout, e.fcnt);
+}
 
 // the MPRGP step bound of one row as an order key (utopia_MPRGP.hpp:289-316, get_alpha_f:
 // min((p > 0) ? (x - l) / p : 1e15, (p < 0) ? (x - u) / p : 1e15)), one division, the
@@ -481,7 +501,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     if constexpr (XM == 1) beta = T(*e.beta_ptr);
     bool qpc = false;
     if constexpr (XM == 3) qpc = *e.qmode != 0;
-    double dacc = 0.0, dacc2 = 0.0;
+    double dacc = 0.0, dacc2 = 0.0, f0 = 0.0, f1 = 0.0;
     unsigned long long qmn = ~0ull;
     // Slices are interleaved over warps (neighbouring warps stream neighbouring slices, which
     // keeps DRAM pages and the x-gathers local).  Each slice's header is one 16-byte load;
@@ -625,6 +645,10 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                                          epi_reads_w<EPI>() ? wr[r] : T(0));
             }
             st16<T, R>(e.y + row0, out);
+            if (e.fa) {
+#pragma unroll
+                for (int r = 0; r < R; ++r) final_dots_row<T>(e, row0 + r, out[r], f0, f1);
+            }
             if constexpr (DOT) {
                 T dr[R];
                 if (e.dv) ld16<T, R>(e.dv + row0, dr);
@@ -651,6 +675,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     }
                     T out = epilogue<T, EPI>(e, row, acc[r], xr);
                     e.y[row] = out;
+                    if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
                     if constexpr (DOT) {
                         dacc = fma(double(xr), double(out), dacc);
                         if (e.dv) dacc2 = fma(double(xr), double(e.dv[row]), dacc2);
@@ -659,6 +684,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
             }
         }
     }
+    if (e.fa) final_dots_finish<T>(e, f0, f1);
     if constexpr (XM == 3) {
         if (qpc) block_atomic_min_u64(qmn, e.qmin);
     }
@@ -837,6 +863,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
     const int64_t nwarps = int64_t(gridDim.x) * kStagedWarps;
     const int cmax = int(m.ncols) - 1;
     const unsigned full = 0xffffffffu;
+    double f0 = 0.0, f1 = 0.0;  // final dots (e.fa) over this thread's rows
 
     if (lane == 0) {
         for (int i = 0; i < nst; ++i) mbar_init(&bar[i], 1);
@@ -1064,7 +1091,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 if constexpr (Nd::w) wr = sww[rl];
                 if constexpr (XM == 2) xr = wr * vr;
                 else if constexpr (Nd::xr) xr = sxr[rl];
-                e.y[row] = epi_row<float, EPI>(acc[r], xr, vr, wr);
+                const float out = epi_row<float, EPI>(acc[r], xr, vr, wr);
+                e.y[row] = out;
+                if (e.fa) final_dots_row<float>(e, row, out, f0, f1);
             }
         }
     };
@@ -1098,6 +1127,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             if (s < ns) mbar_wait_bounded(&bar[(it + j) % nst], uint32_t((it + j) / nst) & 1u, cfg.spin);
         }
     }
+    if (e.fa) final_dots_finish<float>(e, f0, f1);
 }
 
 
@@ -1116,7 +1146,7 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
     if constexpr (XM == 1) beta = T(*e.beta_ptr);
     bool qpc = false;
     if constexpr (XM == 3) qpc = *e.qmode != 0;
-    double dacc = 0.0, dacc2 = 0.0;
+    double dacc = 0.0, dacc2 = 0.0, f0 = 0.0, f1 = 0.0;
     unsigned long long qmn = ~0ull;
     for (int64_t wb = warp0 * RPW; wb < nrows; wb += nwarps * RPW) {
         const int64_t row = wb + lane / G;
@@ -1141,12 +1171,14 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
             }
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
+            if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
             if constexpr (DOT) {
                 dacc = fma(double(xr), double(out), dacc);
                 if (e.dv) dacc2 = fma(double(xr), double(e.dv[row]), dacc2);
             }
         }
     }
+    if (e.fa) final_dots_finish<T>(e, f0, f1);
     if constexpr (XM == 3) {
         if (qpc) block_atomic_min_u64(qmn, e.qmin);
     }
@@ -1187,6 +1219,11 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.qlb = static_cast<const T *>(a.qlb);
     e.qub = static_cast<const T *>(a.qub);
     e.qmin = a.qmin;
+    e.fa = a.fa;
+    e.fb = a.fb;
+    e.fpart = a.fpart;
+    e.fout = a.fout;
+    e.fcnt = a.fcnt;
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
     e.vec_ok = al(a.x) && al(a.p) && al(a.pout) && al(a.v) && al(a.w) && al(a.y) && al(a.dv) && al(a.xalt) &&
                al(a.qx) && al(a.qlb) && al(a.qub);
@@ -1218,7 +1255,7 @@ void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     }
     int64_t want = (s.nslices + kSpmvWarps - 1) / kSpmvWarps;
     int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * per_sm)));
-    if constexpr (DOT) g = std::min(g, kSpmvDotGrid);
+    if (DOT || a.fa) g = std::min(g, kSpmvDotGrid);
     k_sell_spmv<V, T, R, EPI, XM, DOT><<<g, kSpmvWarps * 32, 0, ctx.stream>>>(m, make_epi<T>(a));
 }
 
@@ -1299,7 +1336,8 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
                s.offs.as<int32_t>(), s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols, 1};
     const int64_t want = (s.nslices + kStagedWarps - 1) / kStagedWarps;
-    const int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * best_per_sm)));
+    int g = int(std::max<int64_t>(1, std::min<int64_t>(want, int64_t(ctx.sms) * best_per_sm)));
+    if (a.fa) g = std::min(g, kSpmvDotGrid);
     kern<<<g, kStagedWarps * 32, cta, ctx.stream>>>(m, e, c, ctx.d_kflags());
     return true;
 }
@@ -1326,7 +1364,7 @@ void csr_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     auto go = [&](auto Gc) {
         constexpr int G = decltype(Gc)::value;
         int g = spmv_grid(ctx, 256 / G, A.nrows);
-        if constexpr (DOT) g = std::min(g, kSpmvDotGrid);
+        if (DOT || a.fa) g = std::min(g, kSpmvDotGrid);
         k_csr_spmv<V, T, G, EPI, XM, DOT><<<g, 256, 0, ctx.stream>>>(rp, ci, cv, A.nrows, e);
     };
     if (avg <= 2) go(std::integral_constant<int, 1>{});
@@ -1883,6 +1921,36 @@ int ugpu_spmv(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y) {
     a.vec_dtype = x->impl.dtype;
     a.epilogue = EPI_STORE;
     launch_spmv(*M.ctx, M, a);
+    UGPU_ABI_END(A ? A->impl.ctx : nullptr)
+}
+
+int ugpu_spmv_dot(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec *y, ugpu_vec *dot) {
+    UGPU_ABI_BEGIN
+    UGPU_REQUIRE(A);
+    UGPU_REQUIRE(dot);
+    auto &M = A->impl;
+    check_spmv_vec(M, x ? &x->impl : nullptr, M.ncols, "x");
+    check_spmv_vec(M, y ? &y->impl : nullptr, M.nrows, "y");
+    UGPU_CHECK(M.nrows == M.ncols, UGPU_ERR_ARG, "spmv_dot: square operator");
+    UGPU_CHECK(x->impl.dtype == y->impl.dtype, UGPU_ERR_ARG, "x and y dtypes differ");
+    UGPU_CHECK(x->impl.buf.ptr != y->impl.buf.ptr, UGPU_ERR_ARG, "y must not alias x");
+    UGPU_CHECK(dot->impl.dtype == UGPU_F64 && dot->impl.n >= 1, UGPU_ERR_ARG, "spmv_dot: an FP64 dot vector");
+    UGPU_CHECK(dot->impl.buf.ptr != x->impl.buf.ptr && dot->impl.buf.ptr != y->impl.buf.ptr, UGPU_ERR_ARG,
+               "spmv_dot: the dot vector must not alias x or y");
+    Context &ctx = *M.ctx;
+    if (M.nrows == 0) {
+        UGPU_CUDA(cudaMemsetAsync(dot->impl.buf.ptr, 0, sizeof(double), ctx.stream));
+    } else {
+        SpmvArgs a;
+        a.x = x->impl.buf.ptr;
+        a.y = y->impl.buf.ptr;
+        a.vec_dtype = x->impl.dtype;
+        a.epilogue = EPI_STORE;
+        a.dot_partials = ctx.d_partials();
+        a.dot_out = dot->impl.as<double>();
+        a.dot_counter = ctx.d_counters() + 8;
+        launch_spmv(ctx, M, a);
+    }
     UGPU_ABI_END(A ? A->impl.ctx : nullptr)
 }
 
