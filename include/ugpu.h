@@ -132,6 +132,11 @@ UGPU_API int ugpu_synchronize(ugpu_ctx *ctx);
 UGPU_API int ugpu_launch_count(const ugpu_ctx *ctx, int64_t *out);
 /* the context's CUDA stream (cudaStream_t) for callers that interleave their own work */
 UGPU_API int ugpu_stream(const ugpu_ctx *ctx, void **out);
+/* FP64 arithmetic rate of the context's GPU, measured (no counterpart in the reference: the
+ * denominator of FP64-pipe fractions).  kind 0: FMA chains on every thread (DFMA); kind 1: the
+ * FP64 tensor path (mma.sync m8n8k4).  *flops_per_s: the best of three timed launches of about
+ * 10 ms each, after one warm-up, on the context's stream (synchronising). */
+UGPU_API int ugpu_fp64_rate(ugpu_ctx *ctx, int kind, double *flops_per_s);
 
 /* ---------------------------------------------------------------- vectors ---- */
 /* Replaces PetscVector construction/zeros/values/wrap

@@ -442,3 +442,12 @@ def test_update_values_refreshes_the_spmv_layout(ctx, dtype, name):
     M.apply(x, y1)
     ref.apply(x, y2)
     np.testing.assert_array_equal(y1.numpy(), y2.numpy())
+
+
+def test_fp64_rate_measurement(ctx):
+    """The FP64 rates the benchmark divides by: DFMA chains and the FP64 mma.sync path, both in
+    the range a GB300 can deliver (about 1.2 TFLOP/s; the check only rejects nonsense)."""
+    dfma, dmma = ctx.fp64_rate("dfma"), ctx.fp64_rate("dmma")
+    print(f"FP64 DFMA {dfma / 1e12:.3f} TFLOP/s, DMMA m8n8k4 {dmma / 1e12:.3f} TFLOP/s")
+    assert 0.2e12 < dfma < 5e12
+    assert 0.2e12 < dmma < 5e12

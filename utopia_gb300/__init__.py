@@ -59,6 +59,12 @@ class Context:
         self.check(self.lib.ugpu_launch_count(self.h, C.byref(v)))
         return v.value
 
+    def fp64_rate(self, kind: str = "dfma") -> float:
+        """Measured FP64 FLOP/s of this GPU: "dfma" (FMA chains) or "dmma" (FP64 mma.sync)."""
+        v = C.c_double()
+        self.check(self.lib.ugpu_fp64_rate(self.h, {"dfma": 0, "dmma": 1}[kind], C.byref(v)))
+        return v.value
+
     @property
     def stream(self) -> int:
         v = C.c_void_p()

@@ -99,6 +99,7 @@ SIGNATURES = {
     "ugpu_ptap_reuse": [_vp, _vp, _int, _pp],
     "ugpu_spmv": [_vp, _vp, _vp],
     "ugpu_spmv_add": [_vp, _vp, _vp, _vp],
+    "ugpu_fp64_rate": [_vp, _int, C.POINTER(C.c_double)],
     "ugpu_spmv_dot": [_vp, _vp, _vp, _vp],
     "ugpu_residual": [_vp, _vp, _vp, _vp],
     "ugpu_jacobi_sweep": [_vp, _vp, _vp, _d, _vp],

@@ -91,6 +91,51 @@ __device__ __forceinline__ double block_sum(double v) {
     return t;
 }
 
+// The two-stage reduction of block_reduce_store + finish_last_block over a caller-provided
+// shared scratch of kRedScratchDoubles doubles (for kernels whose shared memory is all sized at
+// launch): the CTA's nd <= 2 sums go to partials[k*G + blk]; the last CTA to finish sums the G
+// partials of each slot in a fixed order into out[k] and rearms the counter.
+constexpr int kRedScratchDoubles = 2 * 32 + 32 + 2;
+__device__ __forceinline__ void block_reduce_finish_in(double a0, double a1, int nd, double *partials, int G,
+                                                       double *out, unsigned int *counter, double *sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    double *wsum = sh;            // [2][32]
+    double *tsum = sh + 64;       // [32]
+    int *last = reinterpret_cast<int *>(sh + 96);
+    a0 = warp_sum(a0);
+    a1 = warp_sum(a1);
+    if (lane == 0) {
+        wsum[w] = a0;
+        wsum[32 + w] = a1;
+    }
+    __syncthreads();
+    if (w == 0) {
+        for (int k = 0; k < nd; ++k) {
+            double v = (lane < nw) ? wsum[32 * k + lane] : 0.0;
+            v = warp_sum(v);
+            if (lane == 0) partials[size_t(k) * G + blockIdx.x] = v;
+        }
+    }
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) *last = (atomicAdd(counter, 1u) == unsigned(G) - 1u) ? 1 : 0;
+    __syncthreads();
+    if (!*last) return;
+    __threadfence();
+    for (int k = 0; k < nd; ++k) {
+        double s = 0.0;
+        for (int j = threadIdx.x; j < G; j += blockDim.x) s += __ldcg(partials + size_t(k) * G + j);
+        s = warp_sum(s);
+        __syncthreads();
+        if (lane == 0) tsum[w] = s;
+        __syncthreads();
+        double t = (lane < nw) ? tsum[lane] : 0.0;
+        t = warp_sum(t);
+        if (threadIdx.x == 0) out[k] = t;
+    }
+    if (threadIdx.x == 0) *counter = 0u;
+}
+
 __device__ __forceinline__ double block_reduce_min(double v) {
     __shared__ double sh[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;

@@ -268,11 +268,13 @@ __global__ void k_qp_init(QpDev *d) {
 }
 
 // ------------------------------------------------------------------ PGS -------------
-// multicolour projected sweep over the rows of one colour
+// multicolour projected sweep over the rows of one colour: c_i = clamp(dinv_i s_i, lo_i, hi_i) with
+// s_i = r_i - sum_{j != i} a_ij c_j and the step bounds lo = lb - x, hi = ub - x of the current
+// iterate (computed once per step); the clamp compares on the integer pipes
 __global__ void __launch_bounds__(kBlock) k_pgs_colour(const int32_t *rows, int64_t nrows_c, const int32_t *rp,
                                                       const int32_t *ci, const double *cv, const double *r,
-                                                      const double *dinv, const double *x, const double *lb,
-                                                      const double *ub, double *c, const int *done) {
+                                                      const double *dinv, const double *lo, const double *hi,
+                                                      double *c, const int *done) {
     if (*done) return;
     QP_LOOP(q, nrows_c) {
         const int32_t i = rows[q];
@@ -281,8 +283,24 @@ __global__ void __launch_bounds__(kBlock) k_pgs_colour(const int32_t *rows, int6
             const int32_t j = ci[k];
             if (j != i) s -= cv[k] * c[j];
         }
+        // fmax(fmin(v, hi), lo)
+        double v = dinv[i] * s;
+        const double h = hi[i], l = lo[i];
+        v = dlt(h, v) ? h : v;
+        v = dlt(v, l) ? l : v;
+        c[i] = v;
+    }
+}
+
+// the step bounds lo = lb - x, hi = ub - x (smoothing steps; the solver's steps get them from
+// the projected-gradient kernel)
+__global__ void __launch_bounds__(kBlock) k_pgs_bounds(int64_t n, const double *x, const double *lb,
+                                                      const double *ub, double *lo, double *hi, const int *done) {
+    if (*done) return;
+    QP_LOOP(i, n) {
         const double xi = x[i];
-        c[i] = fmax(fmin(dinv[i] * s, ub[i] - xi), lb[i] - xi);
+        lo[i] = lb[i] - xi;
+        hi[i] = ub[i] - xi;
     }
 }
 
@@ -325,16 +343,21 @@ __global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, con
     }
 }
 
-// projected-gradient norm || P(x - g) - x || with g = -r (r = b - A x); optional stop test
+// projected-gradient norm || P(x - g) - x || with g = -r (r = b - A x); optional stop test; the
+// step's bounds lo = lb - x, hi = ub - x
 __global__ void __launch_bounds__(kBlock) k_pgs_pgnorm(int64_t n, const double *x, const double *r, const double *lb,
-                                                      const double *ub, PgsDev *dev, double *partials,
-                                                      unsigned int *counter, double atol, int pg_stop) {
+                                                      const double *ub, double *lo, double *hi, PgsDev *dev,
+                                                      double *partials, unsigned int *counter, double atol,
+                                                      int pg_stop) {
     if (dev->done) return;
     double acc = 0;
     QP_LOOP(i, n) {
         const double xi = x[i];
-        const double d = proj(lb[i], ub[i], xi + r[i]) - xi;
+        const double l = lb[i], u = ub[i];
+        const double d = proj(l, u, xi + r[i]) - xi;
         acc = fma(d, d, acc);
+        lo[i] = l - xi;
+        hi[i] = u - xi;
     }
     double a[1] = {acc};
     block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
@@ -692,7 +715,7 @@ public:
         dinv_.alloc(sizeof(double) * std::max<int64_t>(n, 1));
         k_recip<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, M.diag.as<double>(), dinv_.as<double>());
         ctx->launches++;
-        for (Buffer *v : {&r_, &c_}) v->alloc(sizeof(double) * std::max<int64_t>(n, 1));
+        for (Buffer *v : {&r_, &c_, &lo_, &hi_}) v->alloc(sizeof(double) * std::max<int64_t>(n, 1));
         dev_.alloc(sizeof(PgsDev));
         part_.alloc(sizeof(double) * 2 * kRedBlocks);
         cnt_.alloc(sizeof(unsigned int) * 4);
@@ -748,7 +771,7 @@ public:
     }
 
 private:
-    Buffer dinv_, r_, c_, dev_, part_, cnt_, rows_;
+    Buffer dinv_, r_, c_, lo_, hi_, dev_, part_, cnt_, rows_;
     std::vector<int64_t> colour_off_;
     PgsDev *host_ = nullptr;
     DeviceLoop loop_;
@@ -800,6 +823,27 @@ private:
         UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
     }
 
+    // The colour passes of one step: n_local_sweeps forward sweeps over the colours, each followed
+    // by a backward one when symmetric.  A pass over colour k reads only the corrections of the
+    // other colours, so a pass that repeats the one before it (the turn of a symmetric sweep, the
+    // start of the next sweep) recomputes the same values and is dropped; empty colours too.
+    std::vector<int> colour_passes() const {
+        const int sweeps = int(get("n_local_sweeps"));
+        const bool sym = get("use_symmetric_sweep") != 0;
+        std::vector<int> seq;
+        auto push = [&](int c) {
+            if (colour_count[c] == 0) return;
+            if (!seq.empty() && seq.back() == c) return;
+            seq.push_back(c);
+        };
+        for (int il = 0; il < sweeps; ++il) {
+            for (int c = 0; c < ncolours; ++c) push(c);
+            if (sym)
+                for (int c = ncolours - 1; c >= 0; --c) push(c);
+        }
+        return seq;
+    }
+
     // ProjectedGaussSeidel::step (utopia_ProjectedGaussSeidel.hpp:197-318), multicolour
     // smoothing: no projected-gradient norm and no stopping test
     void step(const double *b, double *x, const double *lb, const double *ub, bool smoothing) {
@@ -817,26 +861,22 @@ private:
             launch_spmv(*ctx, *op, a);
         }
         if (!smoothing) {
-            k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, r_.as<double>(), lb, ub, dev,
-                                                                     part_.as<double>(), cnt_.as<unsigned int>() + 0,
-                                                                     get("atol"), pg_stop);
-            ctx->launches++;
+            k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
+                n, x, r_.as<double>(), lb, ub, lo_.as<double>(), hi_.as<double>(), dev, part_.as<double>(),
+                cnt_.as<unsigned int>() + 0, get("atol"), pg_stop);
+        } else {
+            k_pgs_bounds<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, x, lb, ub, lo_.as<double>(),
+                                                                           hi_.as<double>(), &dev->done);
         }
+        ctx->launches++;
         enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
-        const int sweeps = int(get("n_local_sweeps"));
-        const bool sym = get("use_symmetric_sweep") != 0;
-        auto colour_pass = [&](int c) {
-            int64_t m = colour_count[c];
-            if (!m) return;
+        for (int c : colour_passes()) {
+            const int64_t m = colour_count[c];
             k_pgs_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
                 rows_.as<int32_t>() + colour_off_[c], m, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
-                op->vals.as<double>(), r_.as<double>(), dinv_.as<double>(), x, lb, ub, c_.as<double>(), &dev->done);
+                op->vals.as<double>(), r_.as<double>(), dinv_.as<double>(), lo_.as<double>(), hi_.as<double>(),
+                c_.as<double>(), &dev->done);
             ctx->launches++;
-        };
-        for (int il = 0; il < sweeps; ++il) {
-            for (int c = 0; c < ncolours; ++c) colour_pass(c);
-            if (sym)
-                for (int c = ncolours - 1; c >= 0; --c) colour_pass(c);
         }
         k_pgs_finish<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, c_.as<double>(), dev,
                                                                  part_.as<double>() + kRedBlocks,

@@ -732,6 +732,7 @@ struct StagedCfg {
     uint32_t o_x, o_x2, o_xr, o_v, o_w, o_a;  // byte offsets inside a stage (o_a: anchors)
     int xcap;              // floats of one window region
     int xglobal;           // x is gathered from global memory (windows too wide to stage)
+    uint32_t red_off;      // byte offset of the final dots' reduction scratch (after the warps' rings)
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -1127,7 +1128,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             if (s < ns) mbar_wait_bounded(&bar[(it + j) % nst], uint32_t((it + j) / nst) & 1u, cfg.spin);
         }
     }
-    if (e.fa) final_dots_finish<float>(e, f0, f1);
+    if (e.fa)
+        block_reduce_finish_in(f0, f1, e.fb ? 2 : 1, e.fpart, gridDim.x, e.fout, e.fcnt,
+                               reinterpret_cast<double *>(smem + cfg.red_off));
 }
 
 
@@ -1309,8 +1312,10 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     // (about 64 KB per SM covers the HBM latency-bandwidth product).
     int best_nst = 0, best_per_sm = 0;
     long long best_score = 0;
+    // the final dots' reduction scratch, after the warps' rings (folded dots only)
+    const uint32_t red_bytes = a.fa ? uint32_t(round128(sizeof(double) * kRedScratchDoubles)) : 0u;
     for (int nst = kStagedMaxStages; nst >= 2; --nst) {
-        const uint32_t cta = kStagedWarps * (c.hdr_bytes + uint32_t(nst) * c.stage_bytes);
+        const uint32_t cta = kStagedWarps * (c.hdr_bytes + uint32_t(nst) * c.stage_bytes) + red_bytes;
         if (cta > 227u * 1024u) continue;
         int per_sm = 0;
         UGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStagedWarps * 32, cta));
@@ -1332,7 +1337,8 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     c.spin = ctx.staged_test_spin > 0 ? ctx.staged_test_spin : kStagedSpinCycles;
     c.withhold = ctx.staged_test_spin > 0 ? 1 : 0;
     c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
-    const uint32_t cta = kStagedWarps * c.warp_bytes;
+    c.red_off = kStagedWarps * c.warp_bytes;
+    const uint32_t cta = c.red_off + red_bytes;
     SellView m{s.hdr.as<int4>(), s.slice_ptr.as<int64_t>(), s.slice_w.as<int32_t>(), s.slice_aux.as<int64_t>(),
                s.offs.as<int32_t>(), s.cols.as<int32_t>(), s.vals.ptr, s.nslices, A.nrows, A.ncols, 1};
     const int64_t want = (s.nslices + kStagedWarps - 1) / kStagedWarps;
