@@ -352,6 +352,36 @@ __device__ __forceinline__ unsigned long long qp_alpha_f_key(double x, double p,
     const unsigned long long hk = qp_key(h), big = qp_key(1e15);
     return hk < big ? hk : big;
 }
+// A bracket [lo, hi] of qp_alpha_f_key's h = (x - l) / p (p > 0) or (x - u) / p (p < 0) from a
+// single-precision quotient, as order keys: the key of the double-precision h lies inside.  The
+// operands are truncated to binary32 (relative error < 2^-23 each) and divided by the fast
+// reciprocal (2 ulp), so the quotient is within 2^-20 of h; the bracket widens it by 2^-16.
+// p = 0 rows bound at 1e15 and get no bracket (lo = hi = ~0); rows whose operands are zero or
+// outside 2^-60 .. 2^60 in magnitude get lo = 0, hi = ~0 (always evaluated exactly).
+__device__ __forceinline__ void qp_alpha_f_bracket(double x, double p, double l, double u, unsigned long long &lo,
+                                                   unsigned long long &hi) {
+    const long long pk = dkey(p);
+    if (pk == 0) {
+        lo = hi = ~0ull;
+        return;
+    }
+    const double a = x - (pk > 0 ? l : u);
+    const uint64_t ba = (uint64_t)__double_as_longlong(a), bp = (uint64_t)__double_as_longlong(p);
+    const uint32_t ea = uint32_t(ba >> 52) & 0x7ffu, ep = uint32_t(bp >> 52) & 0x7ffu;
+    if (ea - 963u > 120u || ep - 963u > 120u) {  // exponents outside 2^-60 .. 2^60
+        lo = 0ull;
+        hi = ~0ull;
+        return;
+    }
+    auto trunc32 = [](uint64_t b, uint32_t e) {
+        return __uint_as_float((uint32_t(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
+                               uint32_t((b & 0xfffffffffffffull) >> 29));
+    };
+    const float q = __fdividef(trunc32(ba, ea), trunc32(bp, ep));
+    const float q1 = q * (1.0f - 0x1p-16f), q2 = q * (1.0f + 0x1p-16f);
+    lo = qp_key(f2d_bits(fminf(q1, q2)));
+    hi = qp_key(f2d_bits(fmaxf(q1, q2)));
+}
 __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -360,6 +390,34 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
     }
     return v;
 }
+// The exact step bounds of a lane's R rows that can still be the minimum (whole warp, converged):
+// rows whose bracket starts above the least of the warp's bracket ends, of this thread's minimum
+// so far and of the grid's running minimum *gmin cannot be the minimum and skip the division.
+// Every value the bound takes is the key of an exactly evaluated row (or 1e15, the cap every
+// row's bound has), so the minimum is the one all rows' exact keys give.  Improvements go to
+// *gmin at once, so that later slices filter against them.
+template <int R>
+__device__ __forceinline__ void qp_alpha_f_select(const double (&x)[R], const double (&p)[R], const double (&l)[R],
+                                                  const double (&u)[R], const unsigned long long (&lo)[R],
+                                                  unsigned long long hmin, unsigned long long *gmin,
+                                                  unsigned long long &qmn) {
+    hmin = warp_min_u64(hmin);
+    const unsigned long long g = *reinterpret_cast<volatile const unsigned long long *>(gmin);
+    unsigned long long b = hmin < qmn ? hmin : qmn;
+    b = g < b ? g : b;
+    unsigned long long found = ~0ull;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+        if (lo[r] <= b) {
+            const unsigned long long k = qp_alpha_f_key(x[r], p[r], l[r], u[r]);
+            found = k < found ? k : found;
+        }
+    }
+    qmn = found < qmn ? found : qmn;
+    found = warp_min_u64(found);
+    if ((threadIdx.x & 31) == 0 && found < g) atomicMin(gmin, found);
+}
+
 // CTA minimum of the keys, folded into *out with one atomicMin (every thread of the CTA calls it)
 __device__ __forceinline__ void block_atomic_min_u64(unsigned long long v, unsigned long long *out) {
     __shared__ unsigned long long sh[32];
@@ -502,7 +560,8 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
     bool qpc = false;
     if constexpr (XM == 3) qpc = *e.qmode != 0;
     double dacc = 0.0, dacc2 = 0.0, f0 = 0.0, f1 = 0.0;
-    unsigned long long qmn = ~0ull;
+    // QP step bound: every row's bound is at most 1e15 (n >= 1), so the minimum starts there
+    unsigned long long qmn = XM == 3 ? qp_key(1e15) : ~0ull;
     // Slices are interleaved over warps (neighbouring warps stream neighbouring slices, which
     // keeps DRAM pages and the x-gathers local).  Each slice's header is one 16-byte load;
     // headers are fetched two slices ahead and diagonal offsets one slice ahead, so a slice
@@ -597,6 +656,11 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
             }
         }
         constexpr bool kVecEpi = EPI != EPI_CHEB && EPI != EPI_CHEB0;
+        // QP step bound operands of the lane's rows and their brackets (XM == 3)
+        double qx_[R], qp_[R], ql_[R], qu_[R];
+        unsigned long long qlo_[R], qhmin = ~0ull;
+#pragma unroll
+        for (int r = 0; r < R; ++r) qlo_[r] = ~0ull;
         if (kVecEpi && e.vec_ok && !m.il && row0 + R <= m.nrows) {
             // a lane's R rows are consecutive: its epilogue vectors are 16-byte loads
             T xr[R], vr[R], wr[R], out[R];
@@ -623,9 +687,13 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                         ld16<T, R>(e.qub + row0, u);
 #pragma unroll
                         for (int r = 0; r < R; ++r) {
-                            const unsigned long long k = qp_alpha_f_key(double(xx[r]), double(xr[r]), double(l[r]),
-                                                                        double(u[r]));
-                            qmn = k < qmn ? k : qmn;
+                            qx_[r] = double(xx[r]);
+                            qp_[r] = double(xr[r]);
+                            ql_[r] = double(l[r]);
+                            qu_[r] = double(u[r]);
+                            unsigned long long hi;
+                            qp_alpha_f_bracket(qx_[r], qp_[r], ql_[r], qu_[r], qlo_[r], hi);
+                            qhmin = hi < qhmin ? hi : qhmin;
                         }
                     } else {
                         ld16<T, R>(e.xalt + row0, xr);
@@ -668,9 +736,13 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     if constexpr (XM == 1) e.pout[row] = xr;
                     if constexpr (XM == 3) {
                         if (qpc) {
-                            const unsigned long long k = qp_alpha_f_key(double(e.qx[row]), double(xr),
-                                                                        double(e.qlb[row]), double(e.qub[row]));
-                            qmn = k < qmn ? k : qmn;
+                            qx_[r] = double(e.qx[row]);
+                            qp_[r] = double(xr);
+                            ql_[r] = double(e.qlb[row]);
+                            qu_[r] = double(e.qub[row]);
+                            unsigned long long hi;
+                            qp_alpha_f_bracket(qx_[r], qp_[r], ql_[r], qu_[r], qlo_[r], hi);
+                            qhmin = hi < qhmin ? hi : qhmin;
                         }
                     }
                     T out = epilogue<T, EPI>(e, row, acc[r], xr);
@@ -682,6 +754,9 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     }
                 }
             }
+        }
+        if constexpr (XM == 3) {
+            if (qpc) qp_alpha_f_select<R>(qx_, qp_, ql_, qu_, qlo_, qhmin, e.qmin, qmn);
         }
     }
     if (e.fa) final_dots_finish<T>(e, f0, f1);
@@ -1105,20 +1180,24 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (s < ns) issue(s, i, meta_of(load_hdr(s)));
     }
     int4 hq = load_hdr(warp0 + int64_t(nst) * nwarps);
-    int it = 0;
+    int it = 0, st = 0;
+    uint32_t phase = 0;  // parity of the stage's current use: flips each pass around the ring
     bool ok = true;
     for (int64_t s = warp0; s < ns; s += nwarps, ++it) {
-        const int st = it % nst;
         const int64_t s_next = s + int64_t(nst) * nwarps;
         const Meta mt = meta_of(hq);  // in flight while this slice is computed
         hq = load_hdr(s_next + nwarps);
-        if (!mbar_wait_bounded(&bar[st], uint32_t(it / nst) & 1u, cfg.spin)) {
+        if (!mbar_wait_bounded(&bar[st], phase, cfg.spin)) {
             ok = false;
             break;
         }
         compute(s, st);
         __syncwarp();
         if (s_next < ns) issue(s_next, st, mt);
+        if (++st == nst) {
+            st = 0;
+            phase ^= 1u;
+        }
     }
     if (!ok) {
         // record the failure and let the copies still in flight land before the CTA exits
