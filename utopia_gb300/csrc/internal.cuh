@@ -187,6 +187,9 @@ struct Sell {
     // the shared-memory staged kernel); otherwise lane l owns rows l R + r at position l R + r
     bool interleaved = false;
     int xwin_max = 0;   // interleaved: most x-window floats one slice stages (staged kernel's grouping)
+    Buffer tmpl_id;     // interleaved: int32[nslices] window template of an interior diagonal slice, or -1
+    Buffer tmpl;        // the templates (layout in spmv.cu)
+    int ntmpl = 0;
     Buffer keys;        // int32[nslices * kMaxDiagSlots] slice keys of the analysis (values-only refresh)
 };
 

@@ -4,6 +4,7 @@
 // (utopia/backend/petsc/utopia_petsc_Matrix.cpp:1358), MatMultAdd (:1400-1404),
 // Eval_Residual (utopia/utopia_core/eval/utopia_Eval_Residual.hpp:19-38), the Jacobi
 // sweep (utopia/solvers/smoothers/utopia_Jacobi.hpp:131-141), MatGetDiagonal (:756).
+#include <map>
 #include <algorithm>
 #include <climits>
 #include <cstring>
@@ -793,8 +794,16 @@ constexpr int kStagedGap = 16;       // offsets at most this far apart share one
 constexpr int kStagedXBudget = 2048; // most x-window floats per slice that are staged
 constexpr int kStagedMinWarps = 8;   // fewest resident warps per SM the staged kernel runs with
 constexpr bool kStagedGlobalX = false;  // run operators with wider windows here (x through the caches)
-constexpr int kStagedDesc = 66;      // ints per stage descriptor: w, pad, off[32], xb[32]
+constexpr int kStagedDesc = 68;      // ints per stage descriptor: w, flags, off[32], xb[32], x-row offset, pad
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
+// Window templates.  An interior diagonal slice (no gather of its rows leaves [0, ncols)) stages
+// x windows whose layout relative to its first row depends on its offset list alone, so slices
+// with the same offsets share one template, built with the layout: int4[0] = {w, windows, floats
+// staged, window offset of the slot with offset 0 (or INT_MIN)}; int4[1..9) = the slots' window
+// offsets (32 ints); int4[9 + g] = {first float of window g relative to the slice's first row,
+// floats, offset in the stage's window region, 0}.  The issue step then reads its copies and
+// descriptors instead of grouping the offsets itself.
+constexpr int kTmplInt4 = 9 + kStagedMaxWidth;
 
 struct StagedCfg {
     long long spin;        // cycles a wait for a stage's copies may take before the kernel gives up
@@ -808,6 +817,8 @@ struct StagedCfg {
     int xcap;              // floats of one window region
     int xglobal;           // x is gathered from global memory (windows too wide to stage)
     uint32_t red_off;      // byte offset of the final dots' reduction scratch (after the warps' rings)
+    const int *tmpl_id;    // per slice: its window template, or -1 (see StagedTemplate)
+    const int4 *tmpl;      // kTmplInt4 int4 per template
 };
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -957,13 +968,22 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         int aux;
         int anch;   // anchored slice
         int amin, amax;
+        int tid;    // window template (interior diagonal slices), or -1
     };
-    auto load_hdr = [&](int64_t s) -> int4 {
-        return s < ns ? __ldg(reinterpret_cast<const int4 *>(m.hdr) + s) : make_int4(0, 0, 0, 0);
+    struct Hdr {
+        int4 q;
+        int tid;
     };
-    auto meta_of = [&](const int4 &q) -> Meta {
+    auto load_hdr = [&](int64_t s) -> Hdr {
+        if (s >= ns) return Hdr{make_int4(0, 0, 0, 0), -1};
+        return Hdr{__ldg(reinterpret_cast<const int4 *>(m.hdr) + s), cfg.tmpl_id ? __ldg(cfg.tmpl_id + s) : -1};
+    };
+    auto meta_of = [&](const Hdr &hq) -> Meta {
+        const int4 q = hq.q;
         const int anch = ANCH && q.z >= kAnchoredTag;
-        Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), anch ? q.z - kAnchoredTag : q.z, 0, q.w, anch, 0, 0};
+        Meta mt{(int64_t(uint32_t(q.y)) << 32) | uint32_t(q.x), anch ? q.z - kAnchoredTag : q.z, 0, q.w, anch, 0, 0,
+                hq.tid};
+        if (mt.tid >= 0) return mt;  // the template holds the slice's copies and descriptors
         const int32_t *kp = anch ? m.cols + q.w + S : m.offs + q.w;
         if (lane < mt.w) mt.off = __ldg(kp + lane);
         if (anch) {
@@ -980,6 +1000,43 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const int w = mt.w;
         const int r0 = int(s * S);
         const int rows = int(min(int64_t(S), m.nrows - int64_t(r0)));
+        if (mt.tid >= 0) {
+            // interior diagonal slice with a window template (windows staged, never x from global)
+            const int4 *T = cfg.tmpl + size_t(mt.tid) * kTmplInt4;
+            const int4 t0 = __ldg(T);  // {w, windows, floats, x-row offset}
+            const bool xr_win = Nd::xr && t0.w != INT_MIN;
+            if (lane < w) d[34 + lane] = __ldg(reinterpret_cast<const int *>(T + 1) + lane);
+            if (lane == 0) {
+                d[0] = w;
+                d[1] = 1 | (xr_win ? 4 : 0);
+                d[66] = t0.w;
+            }
+            const uint32_t vbytes = uint32_t(w) * S * uint32_t(sizeof(V));
+            const uint32_t rbytes = uint32_t(rows) * 4u;
+            uint32_t total = vbytes + uint32_t(t0.z) * 4u * (XM == 2 ? 2u : 1u);
+            if (Nd::xr && !xr_win) total += rbytes;
+            if (Nd::v) total += rbytes;
+            if (Nd::w) total += rbytes;
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (lane == 0) mbar_arrive_expect_tx(&bar[st], total);
+            __syncwarp();
+            if (cfg.withhold && blockIdx.x == 0 && wib == 0 && s == warp0) return;
+            if (lane == 0 && vbytes) bulk_g2s(sg, vals + mt.base, vbytes, &bar[st]);
+            if (lane < t0.y) {
+                const int4 wd = __ldg(T + 9 + lane);  // {first float - r0, floats, window offset}
+                if constexpr (XM == 2) {
+                    bulk_g2s(sg + cfg.o_x + 4u * wd.z, e.w + r0 + wd.x, 4u * wd.y, &bar[st]);
+                    bulk_g2s(sg + cfg.o_x2 + 4u * wd.z, e.v + r0 + wd.x, 4u * wd.y, &bar[st]);
+                } else {
+                    bulk_g2s(sg + cfg.o_x + 4u * wd.z, e.x + r0 + wd.x, 4u * wd.y, &bar[st]);
+                }
+            }
+            if (Nd::xr && !xr_win && lane == 1) bulk_g2s(sg + cfg.o_xr, e.x + r0, rbytes, &bar[st]);
+            if (Nd::v && lane == 2) bulk_g2s(sg + cfg.o_v, e.v + r0, rbytes, &bar[st]);
+            if (Nd::w && lane == 3) bulk_g2s(sg + cfg.o_w, e.w + r0, rbytes, &bar[st]);
+            return;
+        }
         const int offk = mt.off;
         const int prev = __shfl_up_sync(full, offk, 1);
         const bool start = !cfg.xglobal && lane < w && (lane == 0 || offk - prev > kStagedGap);
@@ -1068,7 +1125,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         float acc[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) acc[r] = 0.f;
-        const int flags = ANCH ? d[1] : (d[1] & 1);
+        const int flags = ANCH ? (d[1] & 3) : (d[1] & 1);
+        const bool xr_win = Nd::xr && (d[1] & 4);  // the row's own x from the window (template slices)
+        const int xr_off = d[66];
         const int *sa = reinterpret_cast<const int *>(sg + cfg.o_a);
         if (ANCH && cfg.xglobal) {
             // values (and anchors) staged, x gathered through L1 / L2
@@ -1166,7 +1225,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 if constexpr (Nd::v) vr = svv[rl];
                 if constexpr (Nd::w) wr = sww[rl];
                 if constexpr (XM == 2) xr = wr * vr;
-                else if constexpr (Nd::xr) xr = sxr[rl];
+                else if constexpr (Nd::xr) xr = xr_win ? sx[rl + xr_off] : sxr[rl];
                 const float out = epi_row<float, EPI>(acc[r], xr, vr, wr);
                 e.y[row] = out;
                 if (e.fa) final_dots_row<float>(e, row, out, f0, f1);
@@ -1179,7 +1238,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const int64_t s = warp0 + int64_t(i) * nwarps;
         if (s < ns) issue(s, i, meta_of(load_hdr(s)));
     }
-    int4 hq = load_hdr(warp0 + int64_t(nst) * nwarps);
+    Hdr hq = load_hdr(warp0 + int64_t(nst) * nwarps);
     int it = 0, st = 0;
     uint32_t phase = 0;  // parity of the stage's current use: flips each pass around the ring
     bool ok = true;
@@ -1362,6 +1421,9 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     // gather latency better, so such operators go there.
     c.xglobal = s.xwin_max > kStagedXBudget ? 1 : 0;
     if (c.xglobal && !kStagedGlobalX) return false;
+    const bool tm = s.ntmpl > 0 && !c.xglobal;
+    c.tmpl_id = tm ? s.tmpl_id.as<int>() : nullptr;
+    c.tmpl = tm ? s.tmpl.as<int4>() : nullptr;
     c.xcap = c.xglobal ? 0 : std::max(4, s.xwin_max);
     const uint32_t vals_b = round128(uint32_t(wcap) * S * uint32_t(sizeof(V)));
     const uint32_t x_b = round128(uint32_t(c.xcap) * 4u);
@@ -1532,6 +1594,66 @@ void dispatch_epi(Context &ctx, const Mat &A, const SpmvArgs &a) {
 // ------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------
+
+// The staged kernel's window templates of an interleaved layout: every interior diagonal slice
+// gets the template of its offset list (the same grouping into windows as the kernel's own issue
+// step: offsets at most kStagedGap apart share a window, rounded out to 16 bytes).
+void build_staged_templates(Mat &A, Sell &s, const std::vector<int32_t> &hw, const std::vector<int64_t> &aux) {
+    Context &ctx = *A.ctx;
+    const int64_t ns = s.nslices;
+    const int S = s.S;
+    std::vector<int32_t> ho(std::max<int64_t>(s.noffs, 1));
+    if (s.noffs)
+        UGPU_CUDA(cudaMemcpyAsync(ho.data(), s.offs.ptr, sizeof(int32_t) * s.noffs, cudaMemcpyDeviceToHost,
+                                  ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+    std::map<std::vector<int32_t>, int> index;
+    std::vector<int4> blocks;
+    std::vector<int32_t> tid(ns, -1);
+    const int64_t cmax = A.ncols - 1;
+    for (int64_t i = 0; i < ns; ++i) {
+        const int w = hw[i];
+        if (w <= 0 || w >= kAnchoredTag || w > kStagedMaxWidth) continue;
+        const int32_t *o = ho.data() + aux[i];
+        const int64_t r0 = i * S;
+        if (r0 + o[0] < 0 || r0 + S - 1 + o[w - 1] > cmax) continue;  // a boundary slice: clamped gathers
+        std::vector<int32_t> key(o, o + w);
+        auto it = index.find(key);
+        if (it == index.end()) {
+            const int t = int(index.size());
+            it = index.emplace(std::move(key), t).first;
+            std::vector<int4> b(kTmplInt4, make_int4(0, 0, 0, 0));
+            int *d34 = reinterpret_cast<int *>(&b[1]);
+            int nwin = 0, woff = 0, xr = INT_MIN;
+            for (int a = 0; a < w;) {
+                int e = a;
+                while (e + 1 < w && o[e + 1] - o[e] <= kStagedGap) ++e;
+                const int lo_r = o[a] & ~3;               // relative to the slice's first row (a multiple of 4)
+                const int len = ((S - 1 + o[e] + 4) & ~3) - lo_r;
+                b[9 + nwin] = make_int4(lo_r, len, woff, 0);
+                for (int k = a; k <= e; ++k) {
+                    d34[k] = o[k] + woff - lo_r;
+                    if (o[k] == 0) xr = d34[k];
+                }
+                woff += len;
+                ++nwin;
+                a = e + 1;
+            }
+            b[0] = make_int4(w, nwin, woff, xr);
+            blocks.insert(blocks.end(), b.begin(), b.end());
+        }
+        tid[i] = it->second;
+    }
+    s.ntmpl = int(index.size());
+    if (s.ntmpl == 0) return;
+    s.tmpl.alloc(sizeof(int4) * blocks.size());
+    s.tmpl_id.alloc(sizeof(int32_t) * ns);
+    UGPU_CUDA(cudaMemcpyAsync(s.tmpl.ptr, blocks.data(), sizeof(int4) * blocks.size(), cudaMemcpyHostToDevice,
+                              ctx.stream));
+    UGPU_CUDA(cudaMemcpyAsync(s.tmpl_id.ptr, tid.data(), sizeof(int32_t) * ns, cudaMemcpyHostToDevice, ctx.stream));
+    UGPU_CUDA(cudaStreamSynchronize(ctx.stream));  // the host vectors must outlive the copies
+}
+
 void build_sell(Mat &A) {
     Context &ctx = *A.ctx;
     auto s = std::make_unique<Sell>();
@@ -1632,6 +1754,7 @@ void build_sell(Mat &A) {
     }
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));  // host vectors above must outlive the copies
     s->xwin_max = h_wmax;
+    if (ns && s->interleaved && h_wmax <= kStagedXBudget) build_staged_templates(A, *s, hw, aux);
     s->keys = std::move(offs_tmp);  // kept: a later values-only refresh re-runs the fill alone
     A.sell = std::move(s);
 }
