@@ -20,9 +20,10 @@
 //   K2  alpha ; x += alpha p ; r -= alpha Ap ; ||r|| ; z = D^+ r ; (z,r) ; beta ; stop test
 // With a multigrid preconditioner: K0, K1, K2 (without z), the V-cycle, and
 //   K3  (z,r) [and (z,Ap)] ; beta ; max_it test
-// Where the V-cycle ends in a Jacobi / PointJacobi sweep (fold_dots = 1, the default), that
-// sweep computes (z,r) [and (z,Ap)] as it writes z, and K3 shrinks to one thread that
-// closes the iteration: z is not read back.
+// Where the V-cycle ends in a Jacobi / PointJacobi sweep and fold_dots = 1, that sweep computes
+// (z,r) [and (z,Ap)] as it writes z, and K3 shrinks to one thread that closes the iteration: z
+// is not read back.  Off by default: measured at 192^3 (mixed form), the BF16 sweep with the two
+// FP64 dots took 96 us against 42 us without them, more than the separate K3 (48 us) it replaces.
 // (K0 is not folded into the SpMV: gathering z and p per nonzero doubles the FP64 FMAs of
 // the product, and FP64 FMA throughput, not HBM, then bounds it on GB300.)
 #include <cmath>
@@ -324,7 +325,7 @@ public:
         prm["reset_initial_guess"] = 0;
         prm["flexible"] = 0;
         prm["use_graphs"] = 1;  // 1: the solve is one graph launch (conditional WHILE node)
-        prm["fold_dots"] = 1;   // 1: the preconditioner's last kernel computes (z,r) [and (z,Ap)]
+        prm["fold_dots"] = 0;   // 1: the preconditioner's last kernel computes (z,r) [and (z,Ap)]
     }
 
     void set_preconditioner(Solver *p) override {

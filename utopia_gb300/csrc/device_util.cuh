@@ -199,21 +199,26 @@ __device__ __forceinline__ bool finish_last_block(int nd, const double *partials
 // selects of the box-constrained solvers run on the integer pipes instead: a double's bit
 // pattern, read as a signed-magnitude integer, orders like the double itself.  Operands are not
 // NaN (bounds, iterates); -0 and +0 compare equal, as in IEEE arithmetic.
-constexpr long long kMag = 0x7fffffffffffffffll;
+// The bit pattern of |d|: the sign is cleared by an integer AND in inline assembly.  Written as
+// C++ (`bits & 0x7fff...`), the compiler recognises the mask as fabs and issues an FP64
+// instruction for it (measured: one DADD per use), which is what these helpers exist to avoid.
+__device__ __forceinline__ long long dmag(double d) {
+    long long r;
+    asm("and.b64 %0, %1, 0x7FFFFFFFFFFFFFFF;" : "=l"(r) : "l"(__double_as_longlong(d)));
+    return r;
+}
 // signed key: a < b <=> dkey(a) < dkey(b) (-0 and +0 share the key 0)
 __device__ __forceinline__ long long dkey(double d) {
     const long long u = __double_as_longlong(d);
-    return u < 0 ? -(u & kMag) : u;
+    return u < 0 ? -dmag(d) : u;
 }
 __device__ __forceinline__ bool dlt(double a, double b) { return dkey(a) < dkey(b); }
 // |d| < t for t > 0 (false for NaN, as the FP comparison)
-__device__ __forceinline__ bool dabs_lt(double d, double t) {
-    return (__double_as_longlong(d) & kMag) < __double_as_longlong(t);
-}
+__device__ __forceinline__ bool dabs_lt(double d, double t) { return dmag(d) < __double_as_longlong(t); }
 // std::min(0.0, g) = (g < 0) ? g : 0.0 and std::max(0.0, g) = (0 < g) ? g : 0.0
 __device__ __forceinline__ double dmin0(double g) {
-    const long long u = __double_as_longlong(g);
-    return (u < 0 && (u & kMag) != 0 && (u & kMag) <= 0x7ff0000000000000ll) ? g : 0.0;
+    const long long u = __double_as_longlong(g), m = dmag(g);
+    return (u < 0 && m != 0 && m <= 0x7ff0000000000000ll) ? g : 0.0;
 }
 __device__ __forceinline__ double dmax0(double g) {
     const long long u = __double_as_longlong(g);
