@@ -294,3 +294,26 @@ def test_folded_outer_dots(ctx, oracle, smoother, precision, flexible):
                                  atol=atol)
         assert abs(i1 - so["iterates"]) <= 1
         assert rel(x1, xo) <= 1e-9
+
+
+@pytest.mark.parametrize("smoother,precision,flexible",
+                         [("jacobi", U.F64, 0), ("point_jacobi", U.F64, 0), ("jacobi", U.BF16, 1)])
+def test_first_jacobi_iterate_from_the_producer(ctx, smoother, precision, flexible):
+    """x1_from_producer = 1: the restriction (coarser levels) and CG's residual update (fine level)
+    write the first Jacobi iterate w .* r beside r, and the pre-smoothing starts from it.  The
+    products are the ones the gathers formed before, so the solve is bit-identical to
+    x1_from_producer = 0, in the graph and eagerly."""
+    A, Ps, b = P.lognormal_mg(32, 3, seed=2)
+    nb = np.linalg.norm(b)
+    Am = U.SparseMatrix(ctx, A)
+    out = []
+    for prod, graphs in ((0, 1), (1, 1), (1, 0)):
+        mg = _mg(ctx, Ps, smoother=smoother, omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+                 precision=precision, x1_from_producer=prod)
+        s = cg(ctx, mg, atol=1e-10 * nb, flexible=flexible, use_graphs=graphs)
+        x = U.Vector(ctx, n=A.nrows)
+        assert s.solve(Am, U.Vector(ctx, b), x)
+        out.append((x.numpy(), s.solution_status()["iterates"]))
+    for xo, it in out[1:]:
+        assert it == out[0][1]
+        assert np.array_equal(xo, out[0][0])

@@ -66,14 +66,19 @@ __device__ __forceinline__ void cg_stop(CgDev *d, int reason, int converged) {
     d->gnorm = d->rnorm;
 }
 
-// K2: alpha, x/r update, ||r||^2 [, z = dinv .* r, (z,r)] [, r32 = (float) r]
+// K2: alpha, x/r update, ||r||^2 [, z = dinv .* r, (z,r)] [, r32 = (float) r] [, x1 = pw .* r (in the
+// preconditioner's precision: its first Jacobi iterate, pc_prescale)]
 template <int MODE, bool R32>
 __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restrict__ x, const double *__restrict__ p,
                                                       double *__restrict__ r, const double *__restrict__ Ap,
                                                       const double *__restrict__ dinv, double *__restrict__ z,
-                                                      float *__restrict__ r32, CgDev *dev, double *partials,
+                                                      float *__restrict__ r32, const void *__restrict__ pw,
+                                                      void *__restrict__ px1, CgDev *dev, double *partials,
                                                       unsigned int *counter, double atol, long long max_it,
                                                       int flexible, int vec) {
+    using PT = typename std::conditional<R32, float, double>::type;
+    const PT *w1 = static_cast<const PT *>(pw);
+    PT *x1 = static_cast<PT *>(px1);
     if (dev->done) return;
     if (MODE == CG_PLAIN && dev->pAp == 0.0) {
         // `if (dot_pq == 0.) { converged = true; break; }`
@@ -103,7 +108,13 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
             z[i] = zi;
             a1 = fma(zi, ri, a1);
         }
-        if constexpr (R32) r32[i] = d2f_bits(ri);
+        if constexpr (R32) {
+            const float rf = d2f_bits(ri);
+            r32[i] = rf;
+            if (x1) x1[i] = w1[i] * rf;
+        } else {
+            if (x1) x1[i] = w1[i] * ri;
+        }
     };
     const int64_t tid = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
     const int64_t nth = int64_t(gridDim.x) * blockDim.x;
@@ -125,7 +136,19 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
                 a1 = fma(z0, r0, a1);
                 a1 = fma(z1, r1, a1);
             }
-            if constexpr (R32) reinterpret_cast<float2 *>(r32)[j] = make_float2(d2f_bits(r0), d2f_bits(r1));
+            if constexpr (R32) {
+                const float2 rf = make_float2(d2f_bits(r0), d2f_bits(r1));
+                reinterpret_cast<float2 *>(r32)[j] = rf;
+                if (x1) {
+                    const float2 wv = reinterpret_cast<const float2 *>(w1)[j];
+                    reinterpret_cast<float2 *>(x1)[j] = make_float2(wv.x * rf.x, wv.y * rf.y);
+                }
+            } else {
+                if (x1) {
+                    const double2 wv = ld2(w1, j);
+                    st2(x1, j, make_double2(wv.x * r0, wv.y * r1));
+                }
+            }
         }
         if ((n & 1) && tid == 0) one(n - 1);
     } else {
@@ -482,6 +505,7 @@ private:
                                                                                        : z_.as<double>(),
                                                                 p_.as<double>(), dev, 1);
         ctx->launches++;
+        bool prescaled = false;  // K2 wrote the preconditioner's first iterate
         // K1: Ap = A p ; (p, Ap) [, (p, r)]
         {
             SpmvArgs a;
@@ -500,11 +524,16 @@ private:
             const double atol = get("atol");
             const long long max_it = (long long)get("max_it");
             const double *dinv = (mode_ == CG_JACOBI) ? static_cast<InvDiag *>(pc_)->d.as<double>() : nullptr;
+            // the preconditioner's first iterate x1 = w .* r, formed here where r is (pc_prescale)
+            const void *pw = nullptr;
+            void *px1 = nullptr;
+            if (mode_ == CG_GENERIC && get("fold_dots") == 0) pc_->pc_prescale(&pw, &px1);
+            prescaled = px1 != nullptr;
 #define UGPU_CG_UPD(M, R)                                                                                          \
     k_cg_update<M, R><<<g, kBlock, 0, ctx->stream>>>(n, static_cast<double *>(x), p_.as<double>(), r_.as<double>(), \
-                                                     Ap_.as<double>(), dinv, z_.as<double>(), r32_.as<float>(), dev,  \
-                                                     part + 2 * kSpmvDotGrid, cnt + 1, atol, max_it, int(flexible_), \
-                                                     vec)
+                                                     Ap_.as<double>(), dinv, z_.as<double>(), r32_.as<float>(), pw,   \
+                                                     px1, dev, part + 2 * kSpmvDotGrid, cnt + 1, atol, max_it,       \
+                                                     int(flexible_), vec)
             if (mode_ == CG_PLAIN) UGPU_CG_UPD(CG_PLAIN, false);
             else if (mode_ == CG_JACOBI) UGPU_CG_UPD(CG_JACOBI, false);
             else if (f32) UGPU_CG_UPD(CG_GENERIC, true);
@@ -517,7 +546,9 @@ private:
         // z = M r, then K3
         const long long max_it = (long long)get("max_it");
         void *z = f32 ? z32_.ptr : z_.ptr;
-        if (get("fold_dots") != 0) {
+        if (prescaled) {
+            pc_->pc_enqueue_prescaled(f32 ? r32_.ptr : r_.ptr, z, &dev->done);
+        } else if (get("fold_dots") != 0) {
             FinalDots fd;
             fd.a = r_.as<double>();
             fd.b = flexible_ ? Ap_.as<double>() : nullptr;

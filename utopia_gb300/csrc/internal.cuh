@@ -299,6 +299,10 @@ struct SpmvArgs {
     const double *fa = nullptr, *fb = nullptr;
     double *fpart = nullptr, *fout = nullptr;
     unsigned int *fcnt = nullptr;
+    // if set: sw_out[row] = sw[row] * y[row] (the next level's first Jacobi iterate w .* b, written by
+    // the restriction that forms b)
+    void *sw_out = nullptr;
+    const void *sw = nullptr;
     bool use_csr = false;
 };
 void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);

@@ -159,6 +159,7 @@ struct Level {
     double emax = 0, emin = 0;
     std::vector<double> cheb_alpha, cheb_beta;
     Buffer r, c, c2, rR, p0, p1, rr;  // work vectors (vector dtype)
+    Buffer x1;  // the first Jacobi iterate w .* r from zero, written by the kernel that forms r
 };
 
 // power-method scratch of one level
@@ -198,6 +199,7 @@ public:
         prm["rand_seed"] = 1;
         prm["mg_type"] = 1;               // V-cycle
         prm["coarse_fp32"] = 0;           // mixed form: 1 applies an FP32 copy of the coarse inverse
+        prm["x1_from_producer"] = 1;      // 1: the kernel forming a level's r also writes w .* r (uses_x1)
     }
 
     void set_transfers(const std::vector<const Mat *> &P) {
@@ -301,9 +303,11 @@ public:
         // coarse_fp32 asks for the FP32 copy of the inverse
         if (vdt_ == UGPU_F32 && get("coarse_fp32") != 0) coarse_.make_fp32_inverse();
         const size_t vs = dtype_size(vdt_);
-        for (auto &l : levels_) {
+        for (size_t k = 0; k < levels_.size(); ++k) {
+            Level &l = levels_[k];
             size_t b = vs * std::max<int64_t>(l.n, 1);
             for (Buffer *q : {&l.r, &l.c, &l.c2, &l.rR, &l.p0, &l.p1, &l.rr}) q->ensure(b);
+            if (uses_x1(int(k))) l.x1.ensure(b);
         }
         f64_r_.ensure(sizeof(double) * std::max<int64_t>(A->nrows, 1));
         f64_z_.ensure(sizeof(double) * std::max<int64_t>(A->nrows, 1));
@@ -317,6 +321,27 @@ public:
     void pc_enqueue(const void *r, void *z, const int *done) override {
         UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
         cycle(n_levels() - 1, r, z, done);
+    }
+
+    // The Jacobi / PointJacobi pre-smoothing from zero starts with x1 = w .* r.  Rather than a
+    // product whose every gather forms w_j r_j, the kernel that forms r writes x1 beside it (the
+    // restriction for the coarser levels, the caller's residual update for the fine one) and the
+    // sweeps start from x1: the same FP32 / FP64 products, so the same iterates.
+    bool uses_x1(int l) const {
+        return l >= 1 && get("x1_from_producer") != 0 && int(get("smoother")) != 1 &&
+               int(get("pre_smoothing_steps")) >= 2;
+    }
+    void pc_prescale(const void **w, void **x1) override {
+        const int top = n_levels() - 1;
+        const bool ok = ready_ && top >= 1 && uses_x1(top) && levels_[size_t(top)].x1.ptr;
+        *w = ok ? levels_[size_t(top)].w.ptr : nullptr;
+        *x1 = ok ? levels_[size_t(top)].x1.ptr : nullptr;
+    }
+    void pc_enqueue_prescaled(const void *r, void *z, const int *done) override {
+        UGPU_CHECK(ready_, UGPU_ERR_STATE, "multigrid: update() first");
+        top_x1_ = true;
+        cycle(n_levels() - 1, r, z, done);
+        top_x1_ = false;
     }
 
     // the V-cycle with the outer iteration's dots of z computed by the last fine-level
@@ -604,6 +629,7 @@ private:
 
     const FinalDots *fd_ = nullptr;  // set while pc_enqueue_dots runs its cycle
     bool fd_used_ = false;
+    bool top_x1_ = false;  // set while pc_enqueue_prescaled runs its cycle: the fine level's x1 is valid
 
     // ---------------------------------------------------------------- cycle ----
     void spmv(const Mat &A, SpmvArgs a, const int *done) {
@@ -616,12 +642,22 @@ private:
     // buffer index holding the result.  from_zero: the iterate is zero, so the first sweep
     // is x1 = w .* rhs and is folded into the second (its product gathers w .* rhs).
     // fd: the outer iteration's dots, computed by the last sweep (post-smoothing only)
+    // x1: the first iterate w .* rhs, already formed (from_zero, nu >= 2)
     int jacobi_sweeps(Level &lv, int sm, const void *rhs, void *bufs[2], int cur, int nu, bool from_zero,
-                      const int *done, const FinalDots *fd = nullptr) {
+                      const int *done, const FinalDots *fd = nullptr, const void *x1 = nullptr) {
         const Mat &Aop = (sm == 2) ? *lv.LU : *lv.A();
         const int epi = (sm == 2) ? EPI_PJACOBI : EPI_JACOBI;
         int s = 0;
-        if (from_zero && nu >= 1) {
+        if (from_zero && nu >= 2 && x1) {
+            SpmvArgs a;  // x2 = x1 + w .* (rhs - A x1)
+            a.x = x1;
+            a.v = rhs;
+            a.w = lv.w.ptr;
+            a.y = bufs[cur];
+            a.epilogue = epi;
+            spmv(Aop, a, done);
+            s = 2;
+        } else if (from_zero && nu >= 1) {
             if (nu == 1) {
                 // Jacobi: x = 0 + w .* (rhs - A*0); PointJacobi: x = w .* (rhs - LU*0)
                 enq_scale_into(*ctx, vdt_, lv.n, lv.w.ptr, rhs, bufs[cur], done);
@@ -722,7 +758,8 @@ private:
             const int swaps = jacobi_swaps(pre, true) + jacobi_swaps(post, false);
             cur = swaps & 1;  // start so that the last sweep lands in c_out
             if (pre <= 0) enq_set(*ctx, vdt_, lv.n, 0.0, bufs[cur], done);
-            cur = jacobi_sweeps(lv, sm, r, bufs, cur, pre, true, done);
+            const bool x1_ok = uses_x1(l) && (l < n_levels() - 1 || top_x1_);
+            cur = jacobi_sweeps(lv, sm, r, bufs, cur, pre, true, done, nullptr, x1_ok ? lv.x1.ptr : nullptr);
             c = bufs[cur];
         }
         // r_R = r - A c ; r_{l-1} = mask .* (R r_R)
@@ -741,6 +778,10 @@ private:
             if (lc.has_mask) {
                 a.w = lc.mask.ptr;
                 a.epilogue = EPI_SCALE;
+            }
+            if (uses_x1(l - 1)) {  // the coarser level's first Jacobi iterate
+                a.sw_out = lc.x1.ptr;
+                a.sw = lc.w.ptr;
             }
             spmv(*t.R(), a, done);
         }

@@ -64,6 +64,15 @@ struct Solver {
         double *partials = nullptr, *out = nullptr;
         unsigned int *counter = nullptr;
     };
+    // A preconditioner whose first step from zero is x1 = w .* r can take x1 from the kernel of its
+    // caller that forms r: *w = the weights (pc_dtype(), fine-level size) and *x1 = the buffer to
+    // write into, or both null when it cannot.
+    virtual void pc_prescale(const void **w, void **x1) {
+        *w = nullptr;
+        *x1 = nullptr;
+    }
+    // pc_enqueue after the caller wrote x1 = w .* r (pc_prescale) for this r
+    virtual void pc_enqueue_prescaled(const void *r, void *z, const int *done) { pc_enqueue(r, z, done); }
     // pc_enqueue, with out[0] = (z, a) [, out[1] = (z, b)] computed by its last kernel; returns false
     // (and computes no dot) where the preconditioner cannot do that
     virtual bool pc_enqueue_dots(const void *r, void *z, const int *done, const FinalDots & /*fd*/) {

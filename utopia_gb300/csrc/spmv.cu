@@ -324,6 +324,9 @@ struct EpiParams {
     const double *fa, *fb;
     double *fpart, *fout;
     unsigned int *fcnt;
+    // sw_out = sw .* y (SpmvArgs::sw_out)
+    T *sw_out;
+    const T *sw;
     int vec_ok;      // every vector pointer above is 16-byte aligned
 };
 
@@ -714,6 +717,13 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                                          epi_reads_w<EPI>() ? wr[r] : T(0));
             }
             st16<T, R>(e.y + row0, out);
+            if (e.sw_out) {
+                T sw[R];
+                ld16<T, R>(e.sw + row0, sw);
+#pragma unroll
+                for (int r = 0; r < R; ++r) sw[r] = sw[r] * out[r];
+                st16<T, R>(e.sw_out + row0, sw);
+            }
             if (e.fa) {
 #pragma unroll
                 for (int r = 0; r < R; ++r) final_dots_row<T>(e, row0 + r, out[r], f0, f1);
@@ -748,6 +758,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     }
                     T out = epilogue<T, EPI>(e, row, acc[r], xr);
                     e.y[row] = out;
+                    if (e.sw_out) e.sw_out[row] = e.sw[row] * out;
                     if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
                     if constexpr (DOT) {
                         dacc = fma(double(xr), double(out), dacc);
@@ -1312,6 +1323,7 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
             }
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
+            if (e.sw_out) e.sw_out[row] = e.sw[row] * out;
             if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
             if constexpr (DOT) {
                 dacc = fma(double(xr), double(out), dacc);
@@ -1360,6 +1372,8 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.qlb = static_cast<const T *>(a.qlb);
     e.qub = static_cast<const T *>(a.qub);
     e.qmin = a.qmin;
+    e.sw_out = static_cast<T *>(a.sw_out);
+    e.sw = static_cast<const T *>(a.sw);
     e.fa = a.fa;
     e.fb = a.fb;
     e.fpart = a.fpart;
@@ -1367,7 +1381,7 @@ EpiParams<T> make_epi(const SpmvArgs &a) {
     e.fcnt = a.fcnt;
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
     e.vec_ok = al(a.x) && al(a.p) && al(a.pout) && al(a.v) && al(a.w) && al(a.y) && al(a.dv) && al(a.xalt) &&
-               al(a.qx) && al(a.qlb) && al(a.qub);
+               al(a.qx) && al(a.qlb) && al(a.qub) && al(a.sw_out) && al(a.sw);
     return e;
 }
 
@@ -1495,6 +1509,7 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
 template <class V, int EPI, int XM>
 bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
+    if (a.sw_out) return false;  // the register and CSR kernels write sw_out
     if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
     if (s.nanch_slices == 0) return staged_launch_t<V, EPI, XM, false>(ctx, A, a);
     if constexpr ((EPI == EPI_ADD || EPI == EPI_STORE) && XM == 0) return staged_launch_t<V, EPI, XM, true>(ctx, A, a);
