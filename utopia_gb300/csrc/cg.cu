@@ -85,8 +85,12 @@ __global__ void __launch_bounds__(kBlock) k_cg_update(int64_t n, double *__restr
         if (blockIdx.x == 0 && threadIdx.x == 0) cg_stop(dev, UGPU_CONVERGED_FNORM_ABS, 1);
         return;
     }
-    const double num = flexible ? dev->pr : dev->rz;
-    const double alpha = num / dev->pAp;
+    // alpha from one thread per CTA (a division per thread would cost the FP64 pipe about 8
+    // operations per thread)
+    __shared__ double s_alpha;
+    if (threadIdx.x == 0) s_alpha = (flexible ? dev->pr : dev->rz) / dev->pAp;
+    __syncthreads();
+    const double alpha = s_alpha;
     if (isinf(alpha) || isnan(alpha)) {
         // `if (std::isinf(alpha) || std::isnan(alpha)) { stop = check_convergence(...); break; }`
         if (blockIdx.x == 0 && threadIdx.x == 0) {

@@ -147,17 +147,59 @@ __device__ __forceinline__ double block_reduce_min(double v) {
     return warp_min(t);
 }
 
+constexpr int pow2_at_least(int k) { return k <= 1 ? 1 : 2 * pow2_at_least((k + 1) / 2); }
+
+// Warp sums of P per-lane values (P a power of two, at most 32) with P - 1 + 5 - log2(P) FP64 adds
+// per lane instead of 5 P: each of the first log2(P) butterfly steps also splits the values
+// between the lane halves (a lane keeps half of what it holds and adds its partner's share of that
+// half), the remaining steps add one value.  The sum of value k ends in the lanes
+// [k 32/P, (k + 1) 32/P).  On GB300 FP64 adds are scarce (about two per clock per SM), and the
+// reductions of kernels with few rows per thread otherwise spend a large part of them here.
+template <int P>
+__device__ __forceinline__ double warp_sum_split(const double (&a)[P]) {
+    double v[P];
+#pragma unroll
+    for (int k = 0; k < P; ++k) v[k] = a[k];
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int m = P, o = 16; m > 1; m >>= 1, o >>= 1) {
+        const bool upper = (lane & o) != 0;
+        const int h = m / 2;
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+            const double send = upper ? v[j] : v[h + j];
+            const double keep = upper ? v[h + j] : v[j];
+            v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+    }
+    double s = v[0];
+#pragma unroll
+    for (int o = 16 / P; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    return s;
+}
+
 // Reduce NK per-thread accumulators over the CTA and store partials[k*G + blk] for k < nd.
 template <int NK>
 __device__ __forceinline__ void block_reduce_store(const double (&acc)[NK], int nd, double *partials, int G,
                                                    int blk) {
-    __shared__ double sh[NK][32];
+    constexpr int P = pow2_at_least(NK);
+    __shared__ double sh[P][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    constexpr int log2P = P >= 32 ? 5 : P >= 16 ? 4 : P >= 8 ? 3 : P >= 4 ? 2 : P >= 2 ? 1 : 0;
+    if (5 * nd > P - 1 + 5 - log2P) {  // the split butterfly adds less than nd separate sums
+        double a[P];
 #pragma unroll
-    for (int k = 0; k < NK; ++k) {
-        if (k < nd) {
-            double v = warp_sum(acc[k]);
-            if (lane == 0) sh[k][w] = v;
+        for (int k = 0; k < P; ++k) a[k] = (k < NK) ? acc[k] : 0.0;
+        const double s = warp_sum_split<P>(a);
+        constexpr int L = 32 / P;  // lanes per value
+        if ((lane & (L - 1)) == 0) sh[lane / L][w] = s;
+    } else {
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+            if (k < nd) {
+                const double v = warp_sum(acc[k]);
+                if (lane == 0) sh[k][w] = v;
+            }
         }
     }
     __syncthreads();

@@ -326,7 +326,8 @@ public:
     // The Jacobi / PointJacobi pre-smoothing from zero starts with x1 = w .* r.  Rather than a
     // product whose every gather forms w_j r_j, the kernel that forms r writes x1 beside it (the
     // restriction for the coarser levels, the caller's residual update for the fine one) and the
-    // sweeps start from x1: the same FP32 / FP64 products, so the same iterates.
+    // sweeps start from the stored x1, as the reference's Jacobi does (in the fused form the
+    // compiler may contract the row's own w_i r_i into the epilogue's FMA: a different rounding).
     bool uses_x1(int l) const {
         return l >= 1 && get("x1_from_producer") != 0 && int(get("smoother")) != 1 &&
                int(get("pre_smoothing_steps")) >= 2;

@@ -133,26 +133,35 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, dou
         }
         return;
     }
-    int step = 0;
-    double alpha;
-    if (cg) {
-        const double alpha_cg = a1 / a0;
-        const double alpha_f = qp_unkey(dev->amin);
-        step = (alpha_cg <= alpha_f) ? 0 : 1;
-        alpha = step == 0 ? alpha_cg : alpha_f;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            dev->alpha_cg = alpha_cg;
-            dev->alpha_f = alpha_f;
-            dev->step = step;
-            dev->gate_exp = step;
-        }
-    } else {
-        alpha = a1 / a0;
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            dev->step = 0;
-            dev->gate_exp = 0;
+    // the step length and branch, from one thread per CTA (an FP64 division per thread would cost
+    // the FP64 pipe about one operation per row)
+    __shared__ double s_alpha;
+    __shared__ int s_step;
+    if (threadIdx.x == 0) {
+        if (cg) {
+            const double alpha_cg = a1 / a0;
+            const double alpha_f = qp_unkey(dev->amin);
+            const int st = (alpha_cg <= alpha_f) ? 0 : 1;
+            s_alpha = st == 0 ? alpha_cg : alpha_f;
+            s_step = st;
+            if (blockIdx.x == 0) {
+                dev->alpha_cg = alpha_cg;
+                dev->alpha_f = alpha_f;
+                dev->step = st;
+                dev->gate_exp = st;
+            }
+        } else {
+            s_alpha = a1 / a0;
+            s_step = 0;
+            if (blockIdx.x == 0) {
+                dev->step = 0;
+                dev->gate_exp = 0;
+            }
         }
     }
+    __syncthreads();
+    const double alpha = s_alpha;
+    const int step = s_step;
     double acc_fq = 0, acc_bb = 0, acc_ff = 0, acc_gg = 0;
     QP_LOOP(i, n) {
         const double l = lb[i], u = ub[i], xi = x[i], gi = g[i], qi = q[i];
