@@ -346,6 +346,52 @@ __global__ void __launch_bounds__(256) k_gemv64_warp(const double *M, int64_t n,
     }
 }
 
+// The same product for coarse levels whose right-hand side fits shared memory: r is converted to
+// FP64 once per CTA into shared memory, and each row is split over four warps (two rows per CTA),
+// so every lane has only a few independent 16-byte row loads and the grid keeps enough of them
+// in flight to stream the inverse at HBM rate.
+constexpr int kGemvSmemMax = 96 * 1024;  // bytes of r staged per CTA
+template <class VT>
+__global__ void __launch_bounds__(256) k_gemv64_split(const double *M, int64_t n, const VT *r, VT *x,
+                                                      const int *done, int vec) {
+    extern __shared__ __align__(16) double sr[];  // r in FP64
+    __shared__ double part[8];
+    if (done && *done) return;
+    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) sr[j] = cvt<double>(r[j]);
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int rl = warp >> 2, q = warp & 3;  // row of the pair, quarter of the row
+    for (int64_t i0 = 2 * int64_t(blockIdx.x); i0 < n; i0 += 2 * int64_t(gridDim.x)) {
+        const int64_t i = i0 + rl;
+        double s0 = 0.0, s1 = 0.0;
+        if (i < n) {
+            const double *row = M + i * n;
+            if (vec) {  // n even, rows 16-byte aligned: pairs [q n2 / 4, (q + 1) n2 / 4)
+                const int64_t n2 = n >> 1, c0 = q * n2 / 4, c1 = (q + 1) * n2 / 4;
+                const double2 *rv = reinterpret_cast<const double2 *>(row);
+                const double2 *xv = reinterpret_cast<const double2 *>(sr);
+#pragma unroll 4
+                for (int64_t c = c0 + lane; c < c1; c += 32) {
+                    const double2 a = __ldg(rv + c), b = xv[c];
+                    s0 = fma(a.x, b.x, s0);
+                    s1 = fma(a.y, b.y, s1);
+                }
+            } else {
+                const int64_t c0 = q * n / 4, c1 = (q + 1) * n / 4;
+                for (int64_t c = c0 + lane; c < c1; c += 32) s0 = fma(__ldg(row + c), sr[c], s0);
+            }
+        }
+        const double s = warp_sum(s0 + s1);
+        if (lane == 0) part[warp] = s;
+        __syncthreads();
+        if (threadIdx.x < 2 && i0 + threadIdx.x < n) {
+            const double *pp = part + 4 * threadIdx.x;
+            x[i0 + threadIdx.x] = cvt<VT>((pp[0] + pp[1]) + (pp[2] + pp[3]));
+        }
+        __syncthreads();
+    }
+}
+
 void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int *done) {
     Context &c = *ctx;
     if (n == 0) return;
@@ -353,6 +399,36 @@ void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int 
     g = int(std::min<int64_t>(std::max<int64_t>(n, 1), int64_t(c.sms) * 8));
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };
     const int gw = int(std::min<int64_t>((n + 7) / 8, int64_t(c.sms) * 8));  // a warp per row, 8 per CTA
+    const bool split = (rdt == xdt) && (rdt == UGPU_F64 || (rdt == UGPU_F32 && !Ainv32.ptr)) &&
+                       size_t(n) * sizeof(double) <= size_t(kGemvSmemMax);
+    if (split) {
+        const int gs = int(std::min<int64_t>((n + 1) / 2, int64_t(c.sms) * 8));  // two rows per CTA
+        const size_t smem = size_t(n) * sizeof(double);
+        const int vec = (n % 2 == 0) && al(Ainv.ptr);
+        if (rdt == UGPU_F64) {
+            static bool attr = false;
+            if (!attr) {
+                UGPU_CUDA(cudaFuncSetAttribute(k_gemv64_split<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               kGemvSmemMax));
+                attr = true;
+            }
+            k_gemv64_split<double><<<gs, 256, smem, c.stream>>>(Ainv.as<double>(), n,
+                                                                static_cast<const double *>(rhs),
+                                                                static_cast<double *>(x), done, vec);
+        } else {
+            static bool attr = false;
+            if (!attr) {
+                UGPU_CUDA(cudaFuncSetAttribute(k_gemv64_split<float>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               kGemvSmemMax));
+                attr = true;
+            }
+            k_gemv64_split<float><<<gs, 256, smem, c.stream>>>(Ainv.as<double>(), n, static_cast<const float *>(rhs),
+                                                               static_cast<float *>(x), done, vec);
+        }
+        c.launches++;
+        UGPU_LAUNCH_CHECK();
+        return;
+    }
     if (rdt == UGPU_F64 && xdt == UGPU_F64) {
         const int vec = (n % 2 == 0) && al(Ainv.ptr) && al(rhs);
         k_gemv64_warp<double><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n, static_cast<const double *>(rhs),
