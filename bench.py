@@ -176,7 +176,8 @@ def run_reference(args):
 
 def run_spmv_only(args):
     """The kernels of the roofline and of the V-cycle's fine sweeps, launched in a fixed order:
-    FP64 y = A x (x2), FP32 y = A x (x2), BF16 Jacobi sweep (x2), on the lognormal operator."""
+    FP64 y = A x (x2), FP32 y = A x (x2), BF16 y = A x (x2), BF16 Jacobi sweep (x2), on the
+    lognormal operator."""
     import utopia_gb300 as U
     from utopia_gb300 import problems as P
 
@@ -194,6 +195,8 @@ def run_spmv_only(args):
         M.apply(x64, y64)
     for _ in range(2):
         M32.apply(x32, y32)
+    for _ in range(2):
+        M16.apply(x32, y32)
     for _ in range(2):
         M16.jacobi_sweep(b32, x32, 0.8, y32)
     ctx.synchronize()

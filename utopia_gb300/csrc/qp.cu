@@ -301,6 +301,58 @@ __global__ void __launch_bounds__(kBlock) k_pgs_colour(const int32_t *rows, int6
     }
 }
 
+// The same sweep over a colour-sliced layout: the rows of one colour in ascending order, their
+// off-diagonal entries slot-major (entry k of the colour's row q at k m + q: every slot is one
+// coalesced load over the colour's rows), padded with (the row itself, 0), which subtracts an
+// exact zero; the diagonal inverses compacted per colour.  Same operations in the same order as
+// k_pgs_colour.
+__global__ void __launch_bounds__(kBlock) k_pgs_colour_sliced(const int32_t *rows, int64_t m, int w,
+                                                             const int32_t *cols, const double *vals,
+                                                             const double *dinv_c, const double *r,
+                                                             const double *lo, const double *hi, double *c,
+                                                             const int *done) {
+    if (*done) return;
+    QP_LOOP(q, m) {
+        const int32_t i = rows[q];
+        double s = r[i];
+        for (int k = 0; k < w; ++k) s -= vals[k * m + q] * c[cols[k * m + q]];
+        double v = dinv_c[q] * s;
+        const double h = hi[i], l = lo[i];
+        v = dlt(h, v) ? h : v;
+        v = dlt(v, l) ? l : v;
+        c[i] = v;
+    }
+}
+
+__global__ void k_pgs_max_row(const int32_t *rp, int64_t n, unsigned int *mx) {
+    unsigned int v = 0;
+    QP_LOOP(i, n) v = max(v, unsigned(rp[i + 1] - rp[i]));
+    v = __reduce_max_sync(0xffffffffu, v);
+    if ((threadIdx.x & 31) == 0) atomicMax(mx, v);
+}
+
+// the colour-sliced layout of one colour (k_pgs_colour_sliced), from the CSR rows (w at least the
+// longest row, so the off-diagonal entries always fit)
+__global__ void k_pgs_slice_colour(const int32_t *rows, int64_t m, int w, const int32_t *rp, const int32_t *ci,
+                                   const double *cv, const double *dinv, int32_t *cols, double *vals,
+                                   double *dinv_c) {
+    QP_LOOP(q, m) {
+        const int32_t i = rows[q];
+        int k = 0;
+        for (int32_t e = rp[i]; e < rp[i + 1]; ++e) {
+            if (ci[e] == i) continue;
+            cols[k * m + q] = ci[e];
+            vals[k * m + q] = cv[e];
+            ++k;
+        }
+        for (; k < w; ++k) {
+            cols[k * m + q] = i;
+            vals[k * m + q] = 0.0;
+        }
+        dinv_c[q] = dinv[i];
+    }
+}
+
 // the step bounds lo = lb - x, hi = ub - x (smoothing steps; the solver's steps get them from
 // the projected-gradient kernel)
 __global__ void __launch_bounds__(kBlock) k_pgs_bounds(int64_t n, const double *x, const double *lb,
@@ -781,6 +833,9 @@ public:
 
 private:
     Buffer dinv_, r_, c_, lo_, hi_, dev_, part_, cnt_, rows_;
+    bool sliced_ = false;  // the colour passes read the colour-sliced layout
+    int sliced_w_ = 0;
+    Buffer slice_cols_, slice_vals_, dinv_c_;
     std::vector<int64_t> colour_off_;
     PgsDev *host_ = nullptr;
     DeviceLoop loop_;
@@ -830,6 +885,41 @@ private:
             colour_off_[c + 1] = colour_off_[c] + cnt;
         }
         UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        // colour-sliced copies of the rows (off-diagonal entries slot-major per colour), when the
+        // widest row keeps the padding small
+        unsigned int hmax = 0;
+        if (n) {
+            Buffer mx;
+            mx.alloc(sizeof(unsigned int));
+            UGPU_CUDA(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned int), ctx->stream));
+            k_pgs_max_row<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(op->rowptr.as<int32_t>(), n,
+                                                                            mx.as<unsigned int>());
+            ctx->launches++;
+            UGPU_CUDA(cudaMemcpyAsync(&hmax, mx.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx->stream));
+        }
+        sliced_w_ = int(std::max(hmax, 1u));
+        sliced_ = n > 0 && hmax <= 32;
+        slice_cols_.release();
+        slice_vals_.release();
+        if (sliced_) {
+            const size_t slots = size_t(sliced_w_) * size_t(n);
+            slice_cols_.alloc(sizeof(int32_t) * slots);
+            slice_vals_.alloc(sizeof(double) * slots);
+            dinv_c_.alloc(sizeof(double) * size_t(n));
+            for (int c = 0; c < ncolours; ++c) {
+                const int64_t m = colour_count[c];
+                if (!m) continue;
+                const size_t base = size_t(sliced_w_) * size_t(colour_off_[c]);
+                k_pgs_slice_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
+                    rows_.as<int32_t>() + colour_off_[c], m, sliced_w_, op->rowptr.as<int32_t>(),
+                    op->colidx.as<int32_t>(), op->vals.as<double>(), dinv_.as<double>(),
+                    slice_cols_.as<int32_t>() + base, slice_vals_.as<double>() + base,
+                    dinv_c_.as<double>() + colour_off_[c]);
+                ctx->launches++;
+            }
+            UGPU_LAUNCH_CHECK();
+        }
     }
 
     // The colour passes of one step: n_local_sweeps forward sweeps over the colours, each followed
@@ -881,10 +971,18 @@ private:
         enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
         for (int c : colour_passes()) {
             const int64_t m = colour_count[c];
-            k_pgs_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
-                rows_.as<int32_t>() + colour_off_[c], m, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
-                op->vals.as<double>(), r_.as<double>(), dinv_.as<double>(), lo_.as<double>(), hi_.as<double>(),
-                c_.as<double>(), &dev->done);
+            if (sliced_) {
+                const size_t base = size_t(sliced_w_) * size_t(colour_off_[c]);
+                k_pgs_colour_sliced<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
+                    rows_.as<int32_t>() + colour_off_[c], m, sliced_w_, slice_cols_.as<int32_t>() + base,
+                    slice_vals_.as<double>() + base, dinv_c_.as<double>() + colour_off_[c], r_.as<double>(),
+                    lo_.as<double>(), hi_.as<double>(), c_.as<double>(), &dev->done);
+            } else {
+                k_pgs_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
+                    rows_.as<int32_t>() + colour_off_[c], m, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
+                    op->vals.as<double>(), r_.as<double>(), dinv_.as<double>(), lo_.as<double>(),
+                    hi_.as<double>(), c_.as<double>(), &dev->done);
+            }
             ctx->launches++;
         }
         k_pgs_finish<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(n, x, c_.as<double>(), dev,
