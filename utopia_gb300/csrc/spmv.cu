@@ -356,12 +356,15 @@ __device__ __forceinline__ unsigned long long qp_alpha_f_key(double x, double p,
     const unsigned long long hk = qp_key(h), big = qp_key(1e15);
     return hk < big ? hk : big;
 }
-// A bracket [lo, hi] of qp_alpha_f_key's h = (x - l) / p (p > 0) or (x - u) / p (p < 0) from a
-// single-precision quotient, as order keys: the key of the double-precision h lies inside.  The
-// operands are truncated to binary32 (relative error < 2^-23 each) and divided by the fast
-// reciprocal (2 ulp), so the quotient is within 2^-20 of h; the bracket widens it by 2^-16.
-// p = 0 rows bound at 1e15 and get no bracket (lo = hi = ~0); rows whose operands are zero or
-// outside 2^-60 .. 2^60 in magnitude get lo = 0, hi = ~0 (always evaluated exactly).
+// A bracket [lo, hi] of qp_alpha_f_key's h = (x - l) / p (p > 0) or (x - u) / p (p < 0) from
+// single-precision arithmetic alone, as order keys: the key of the double-precision h lies
+// inside.  x, the bound b and p are truncated to binary32 (relative error < 2^-23 each); the
+// difference x - b is used only where it does not cancel (|x| + |b| <= 8 |x - b|, so it is within
+// 2^-20), and the quotient by the fast reciprocal (2 ulp) stays within 2^-19; the bracket widens it
+// by 2^-16.  Rows with p = 0, and rows whose bound is at infinity on the side p moves towards
+// (|b| >= 2^61, |p| < 2^10: h > 2^50 > 1e15), bound at the cap 1e15 and get no bracket
+// (lo = hi = ~0); rows outside these cases (operands outside 2^-60 .. 2^60, cancellation) get
+// lo = 0, hi = ~0: they are always evaluated exactly.
 __device__ __forceinline__ void qp_alpha_f_bracket(double x, double p, double l, double u, unsigned long long &lo,
                                                    unsigned long long &hi) {
     const long long pk = dkey(p);
@@ -369,19 +372,31 @@ __device__ __forceinline__ void qp_alpha_f_bracket(double x, double p, double l,
         lo = hi = ~0ull;
         return;
     }
-    const double a = x - (pk > 0 ? l : u);
-    const uint64_t ba = (uint64_t)__double_as_longlong(a), bp = (uint64_t)__double_as_longlong(p);
-    const uint32_t ea = uint32_t(ba >> 52) & 0x7ffu, ep = uint32_t(bp >> 52) & 0x7ffu;
-    if (ea - 963u > 120u || ep - 963u > 120u) {  // exponents outside 2^-60 .. 2^60
-        lo = 0ull;
-        hi = ~0ull;
+    const double b = pk > 0 ? l : u;
+    const uint64_t bx = (uint64_t)__double_as_longlong(x), bb = (uint64_t)__double_as_longlong(b),
+                   bp = (uint64_t)__double_as_longlong(p);
+    const uint32_t ex = uint32_t(bx >> 52) & 0x7ffu, eb = uint32_t(bb >> 52) & 0x7ffu,
+                   ep = uint32_t(bp >> 52) & 0x7ffu;
+    lo = 0ull;  // by default: evaluated exactly
+    hi = ~0ull;
+    const bool x_ok = ex - 963u <= 120u || (bx << 1) == 0;  // 2^-60 <= |x| < 2^61, or zero
+    const bool b_ok = eb - 963u <= 120u || (bb << 1) == 0;
+    if (ep - 963u > 120u || !x_ok) return;
+    if (!b_ok) {
+        // b beyond 2^61 on the far side (b < 0 for p > 0, b > 0 for p < 0): h > 2^60 / 2^10
+        const bool far = (pk > 0) == ((bb >> 63) != 0);
+        if (eb >= 1084u && eb != 2047u && ep < 1033u && far) lo = hi = ~0ull;
         return;
     }
-    auto trunc32 = [](uint64_t b, uint32_t e) {
-        return __uint_as_float((uint32_t(b >> 32) & 0x80000000u) | ((e - 896u) << 23) |
-                               uint32_t((b & 0xfffffffffffffull) >> 29));
+    auto trunc32 = [](uint64_t v, uint32_t e) {
+        if ((v << 1) == 0) return __uint_as_float(uint32_t(v >> 32) & 0x80000000u);
+        return __uint_as_float((uint32_t(v >> 32) & 0x80000000u) | ((e - 896u) << 23) |
+                               uint32_t((v & 0xfffffffffffffull) >> 29));
     };
-    const float q = __fdividef(trunc32(ba, ea), trunc32(bp, ep));
+    const float xf = trunc32(bx, ex), bf = trunc32(bb, eb);
+    const float af = xf - bf;
+    if (!(fabsf(xf) + fabsf(bf) <= 8.0f * fabsf(af))) return;  // x - b cancels: evaluated exactly
+    const float q = __fdividef(af, trunc32(bp, ep));
     const float q1 = q * (1.0f - 0x1p-16f), q2 = q * (1.0f + 0x1p-16f);
     lo = qp_key(f2d_bits(fminf(q1, q2)));
     hi = qp_key(f2d_bits(fmaxf(q1, q2)));
