@@ -261,6 +261,8 @@ enum SpmvEpilogue : int {
     EPI_PJACOBI = 6,    // y = w .* (v - A x)                 (PointJacobi sweep with LU = A - D)
     EPI_CHEB = 7,       // Chebyshev3level step: vout += s0*(A x); y = -vout + s1*x; x2 += s3*x; x2 += s2*y
     EPI_CHEB0 = 8,      // Chebyshev3level start: vout = A x - v; y = -vout
+    EPI_STORE_SW = 9,   // y = A x;       sw_out = sw .* y    (restriction writing the next level's w .* b)
+    EPI_SCALE_SW = 10,  // y = w .* (A x); sw_out = sw .* y   (the same with a mask)
 };
 
 struct SpmvArgs {
@@ -299,8 +301,8 @@ struct SpmvArgs {
     const double *fa = nullptr, *fb = nullptr;
     double *fpart = nullptr, *fout = nullptr;
     unsigned int *fcnt = nullptr;
-    // if set: sw_out[row] = sw[row] * y[row] (the next level's first Jacobi iterate w .* b, written by
-    // the restriction that forms b)
+    // EPI_STORE_SW / EPI_SCALE_SW: sw_out[row] = sw[row] * y[row] (the next level's first Jacobi
+    // iterate w .* b, written by the restriction that forms b)
     void *sw_out = nullptr;
     const void *sw = nullptr;
     bool use_csr = false;

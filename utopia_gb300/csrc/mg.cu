@@ -759,7 +759,7 @@ private:
             const int swaps = jacobi_swaps(pre, true) + jacobi_swaps(post, false);
             cur = swaps & 1;  // start so that the last sweep lands in c_out
             if (pre <= 0) enq_set(*ctx, vdt_, lv.n, 0.0, bufs[cur], done);
-            const bool x1_ok = uses_x1(l) && (l < n_levels() - 1 || top_x1_);
+            const bool x1_ok = uses_x1(l) && lv.x1.ptr && (l < n_levels() - 1 || top_x1_);
             cur = jacobi_sweeps(lv, sm, r, bufs, cur, pre, true, done, nullptr, x1_ok ? lv.x1.ptr : nullptr);
             c = bufs[cur];
         }
@@ -780,9 +780,10 @@ private:
                 a.w = lc.mask.ptr;
                 a.epilogue = EPI_SCALE;
             }
-            if (uses_x1(l - 1)) {  // the coarser level's first Jacobi iterate
+            if (uses_x1(l - 1) && lc.x1.ptr) {  // the coarser level's first Jacobi iterate
                 a.sw_out = lc.x1.ptr;
                 a.sw = lc.w.ptr;
+                a.epilogue = lc.has_mask ? EPI_SCALE_SW : EPI_STORE_SW;
             }
             spmv(*t.R(), a, done);
         }

@@ -415,9 +415,9 @@ __device__ __forceinline__ unsigned long long warp_min_u64(unsigned long long v)
 // Every value the bound takes is the key of an exactly evaluated row (or 1e15, the cap every
 // row's bound has), so the minimum is the one all rows' exact keys give.  Improvements go to
 // *gmin at once, so that later slices filter against them.
-template <int R>
-__device__ __forceinline__ void qp_alpha_f_select(const double (&x)[R], const double (&p)[R], const double (&l)[R],
-                                                  const double (&u)[R], const unsigned long long (&lo)[R],
+template <int R, class T>
+__device__ __forceinline__ void qp_alpha_f_select(const EpiParams<T> &e, const int64_t (&row)[R],
+                                                  const double (&p)[R], const unsigned long long (&lo)[R],
                                                   unsigned long long hmin, unsigned long long *gmin,
                                                   unsigned long long &qmn) {
     hmin = warp_min_u64(hmin);
@@ -427,8 +427,9 @@ __device__ __forceinline__ void qp_alpha_f_select(const double (&x)[R], const do
     unsigned long long found = ~0ull;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
-        if (lo[r] <= b) {
-            const unsigned long long k = qp_alpha_f_key(x[r], p[r], l[r], u[r]);
+        if (lo[r] <= b) {  // a candidate: its operands again from the caches (few rows per warp)
+            const int64_t i = row[r];
+            const unsigned long long k = qp_alpha_f_key(double(e.qx[i]), p[r], double(e.qlb[i]), double(e.qub[i]));
             found = k < found ? k : found;
         }
     }
@@ -495,7 +496,12 @@ constexpr bool epi_reads_v() {
 }
 template <int EPI>
 constexpr bool epi_reads_w() {
-    return EPI == EPI_JACOBI || EPI == EPI_SCALE || EPI == EPI_PJACOBI;
+    return EPI == EPI_JACOBI || EPI == EPI_SCALE || EPI == EPI_PJACOBI || EPI == EPI_SCALE_SW;
+}
+// epilogues that also write sw_out = sw .* y (compiled only into those instantiations)
+template <int EPI>
+constexpr bool epi_writes_sw() {
+    return EPI == EPI_STORE_SW || EPI == EPI_SCALE_SW;
 }
 template <int EPI, int XM, bool DOT>
 constexpr bool epi_reads_x() {
@@ -509,7 +515,7 @@ __device__ __forceinline__ T epi_row(T acc, T xrow, T vrow, T wrow) {
     if constexpr (EPI == EPI_RESIDUAL) return vrow - acc;
     if constexpr (EPI == EPI_SUB) return acc - vrow;
     if constexpr (EPI == EPI_JACOBI) return xrow + wrow * (vrow - acc);
-    if constexpr (EPI == EPI_SCALE) return wrow * acc;
+    if constexpr (EPI == EPI_SCALE || EPI == EPI_SCALE_SW) return wrow * acc;
     if constexpr (EPI == EPI_PJACOBI) return wrow * (vrow - acc);
     return acc;
 }
@@ -675,11 +681,16 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
             }
         }
         constexpr bool kVecEpi = EPI != EPI_CHEB && EPI != EPI_CHEB0;
-        // QP step bound operands of the lane's rows and their brackets (XM == 3)
-        double qx_[R], qp_[R], ql_[R], qu_[R];
+        // QP step bound: the lane's rows, their p and their brackets (XM == 3)
+        double qp_[R];
+        int64_t qrow_[R];
         unsigned long long qlo_[R], qhmin = ~0ull;
 #pragma unroll
-        for (int r = 0; r < R; ++r) qlo_[r] = ~0ull;
+        for (int r = 0; r < R; ++r) {
+            qlo_[r] = ~0ull;
+            qp_[r] = 0.0;
+            qrow_[r] = 0;
+        }
         if (kVecEpi && e.vec_ok && !m.il && row0 + R <= m.nrows) {
             // a lane's R rows are consecutive: its epilogue vectors are 16-byte loads
             T xr[R], vr[R], wr[R], out[R];
@@ -706,12 +717,10 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                         ld16<T, R>(e.qub + row0, u);
 #pragma unroll
                         for (int r = 0; r < R; ++r) {
-                            qx_[r] = double(xx[r]);
+                            qrow_[r] = row0 + r;
                             qp_[r] = double(xr[r]);
-                            ql_[r] = double(l[r]);
-                            qu_[r] = double(u[r]);
                             unsigned long long hi;
-                            qp_alpha_f_bracket(qx_[r], qp_[r], ql_[r], qu_[r], qlo_[r], hi);
+                            qp_alpha_f_bracket(double(xx[r]), qp_[r], double(l[r]), double(u[r]), qlo_[r], hi);
                             qhmin = hi < qhmin ? hi : qhmin;
                         }
                     } else {
@@ -732,7 +741,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                                          epi_reads_w<EPI>() ? wr[r] : T(0));
             }
             st16<T, R>(e.y + row0, out);
-            if (e.sw_out) {
+            if constexpr (epi_writes_sw<EPI>()) {
                 T sw[R];
                 ld16<T, R>(e.sw + row0, sw);
 #pragma unroll
@@ -762,18 +771,17 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
                     if constexpr (XM == 1) e.pout[row] = xr;
                     if constexpr (XM == 3) {
                         if (qpc) {
-                            qx_[r] = double(e.qx[row]);
+                            qrow_[r] = row;
                             qp_[r] = double(xr);
-                            ql_[r] = double(e.qlb[row]);
-                            qu_[r] = double(e.qub[row]);
                             unsigned long long hi;
-                            qp_alpha_f_bracket(qx_[r], qp_[r], ql_[r], qu_[r], qlo_[r], hi);
+                            qp_alpha_f_bracket(double(e.qx[row]), qp_[r], double(e.qlb[row]), double(e.qub[row]),
+                                               qlo_[r], hi);
                             qhmin = hi < qhmin ? hi : qhmin;
                         }
                     }
                     T out = epilogue<T, EPI>(e, row, acc[r], xr);
                     e.y[row] = out;
-                    if (e.sw_out) e.sw_out[row] = e.sw[row] * out;
+                    if constexpr (epi_writes_sw<EPI>()) e.sw_out[row] = e.sw[row] * out;
                     if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
                     if constexpr (DOT) {
                         dacc = fma(double(xr), double(out), dacc);
@@ -783,7 +791,7 @@ __global__ void UGPU_SELL_BOUNDS k_sell_spmv(SellView m, EpiParams<T> e) {
             }
         }
         if constexpr (XM == 3) {
-            if (qpc) qp_alpha_f_select<R>(qx_, qp_, ql_, qu_, qlo_, qhmin, e.qmin, qmn);
+            if (qpc) qp_alpha_f_select<R, T>(e, qrow_, qp_, qlo_, qhmin, e.qmin, qmn);
         }
     }
     if (e.fa) final_dots_finish<T>(e, f0, f1);
@@ -1338,7 +1346,7 @@ __global__ void __launch_bounds__(256) k_csr_spmv(const int32_t *__restrict__ rp
             }
             T out = epilogue<T, EPI>(e, row, acc, xr);
             e.y[row] = out;
-            if (e.sw_out) e.sw_out[row] = e.sw[row] * out;
+            if constexpr (epi_writes_sw<EPI>()) e.sw_out[row] = e.sw[row] * out;
             if (e.fa) final_dots_row<T>(e, row, out, f0, f1);
             if constexpr (DOT) {
                 dacc = fma(double(xr), double(out), dacc);
@@ -1524,7 +1532,6 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
 template <class V, int EPI, int XM>
 bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
-    if (a.sw_out) return false;  // the register and CSR kernels write sw_out
     if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
     if (s.nanch_slices == 0) return staged_launch_t<V, EPI, XM, false>(ctx, A, a);
     if constexpr ((EPI == EPI_ADD || EPI == EPI_STORE) && XM == 0) return staged_launch_t<V, EPI, XM, true>(ctx, A, a);
@@ -1558,7 +1565,7 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
         constexpr int R = std::is_same<V, double>::value ? 2 : 4;
         UGPU_CHECK(A.sell->R == R, UGPU_ERR_INTERNAL, "sliced-ELL rows-per-thread mismatch");
         if constexpr (std::is_same<T, float>::value && !std::is_same<V, double>::value && !DOT &&
-                      (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0) {
+                      (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0 && !epi_writes_sw<EPI>()) {
             if (staged_launch<V, EPI, XM>(ctx, A, a)) return;
         }
         // transfer-like operators (not all slices diagonal) with fewer than two slices per SM: in
@@ -1614,6 +1621,12 @@ void dispatch_epi(Context &ctx, const Mat &A, const SpmvArgs &a) {
         UGPU_EPI_CASE(EPI_SCALE)
         UGPU_EPI_CASE(EPI_CHEB)
         UGPU_EPI_CASE(EPI_CHEB0)
+        case EPI_STORE_SW:
+        case EPI_SCALE_SW:
+            UGPU_CHECK(xm == 0 && !dot && a.sw_out && a.sw, UGPU_ERR_INTERNAL, "sw epilogues: plain input, sw and sw_out");
+            if (a.epilogue == EPI_STORE_SW) dispatch_fmt<V, T, EPI_STORE_SW, 0, false>(ctx, A, a);
+            else dispatch_fmt<V, T, EPI_SCALE_SW, 0, false>(ctx, A, a);
+            break;
         default: throw Error(UGPU_ERR_ARG, "unknown SpMV epilogue");
     }
 #undef UGPU_EPI_CASE
