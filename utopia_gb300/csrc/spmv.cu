@@ -828,14 +828,7 @@ constexpr int kStagedGap = 16;       // offsets at most this far apart share one
 constexpr int kStagedXBudget = 2048; // most x-window floats per slice that are staged
 constexpr int kStagedMinWarps = 8;   // fewest resident warps per SM the staged kernel runs with
 constexpr bool kStagedGlobalX = false;  // run operators with wider windows here (x through the caches)
-constexpr int kStagedDesc = 72;      // ints per stage descriptor: w, flags, off[32], xb[32], x-row offset,
-                                     // the far slots (two), pad
-// Far groups: a window group of a single offset at least kStagedFarOffset from the row (a stencil's
-// neighbour planes) is not staged -- its slot gathers through the caches, coalesced over the warp's
-// rows -- for the first kStagedMaxFar such groups of a diagonal slice.  Their windows would add a
-// slice-wide copy each to every stage; without them the ring is smaller and more warps are resident.
-constexpr int kStagedFarOffset = 1024;
-constexpr int kStagedMaxFar = 2;
+constexpr int kStagedDesc = 68;      // ints per stage descriptor: w, flags, off[32], xb[32], x-row offset, pad
 constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up a wait after this
 // Window templates.  An interior diagonal slice (no gather of its rows leaves [0, ncols)) stages
 // x windows whose layout relative to its first row depends on its offset list alone, so slices
@@ -844,7 +837,7 @@ constexpr long long kStagedSpinCycles = 2000000000ll;  // ~1 s at 2 GHz: give up
 // offsets (32 ints); int4[9 + g] = {first float of window g relative to the slice's first row,
 // floats, offset in the stage's window region, 0}.  The issue step then reads its copies and
 // descriptors instead of grouping the offsets itself.
-constexpr int kTmplInt4 = 9 + kStagedMaxWidth + 1;  // + {far slot 0, far slot 1, 0, 0} (-1: none)
+constexpr int kTmplInt4 = 9 + kStagedMaxWidth;
 
 struct StagedCfg {
     long long spin;        // cycles a wait for a stage's copies may take before the kernel gives up
@@ -911,17 +904,11 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 // Floats of x that the staged kernel copies for slice s (offsets off[0..w) ascending): one
 // window per group of offsets at most kStagedGap apart, each covering the group's clamped
 // gathers rounded out to 16 bytes.  Same arithmetic as the kernel's issue step.
-__device__ __forceinline__ int staged_window_floats(const int32_t *off, int w, int gmin, int gmax, int cmax,
-                                                    bool diag) {
-    int total = 0, nfar = 0;
+__device__ __forceinline__ int staged_window_floats(const int32_t *off, int w, int gmin, int gmax, int cmax) {
+    int total = 0;
     for (int a = 0; a < w;) {
         int b = a;
         while (b + 1 < w && off[b + 1] - off[b] <= kStagedGap) ++b;
-        if (diag && b == a && abs(off[a]) >= kStagedFarOffset && nfar < kStagedMaxFar) {  // a far group
-            ++nfar;
-            a = b + 1;
-            continue;
-        }
         const int lo = min(max(gmin + off[a], 0), cmax);
         const int hi = min(max(gmax + off[b], 0), cmax);
         total += ((hi + 4) & ~3) - (lo & ~3);
@@ -939,9 +926,9 @@ __global__ void k_sell_window_max(const int4 *hdr, const int32_t *offs, const in
         if (q.z >= kAnchoredTag) {
             const int w = q.z - kAnchoredTag;
             const int32_t *kp = cols + q.w + S;
-            if (w > 0) best = max(best, staged_window_floats(kp, w, kp[w], kp[w + 1], int(ncols) - 1, false));
+            if (w > 0) best = max(best, staged_window_floats(kp, w, kp[w], kp[w + 1], int(ncols) - 1));
         } else if (q.z > 0) {
-            best = max(best, staged_window_floats(offs + q.w, q.z, r0, r0 + S - 1, int(ncols) - 1, true));
+            best = max(best, staged_window_floats(offs + q.w, q.z, r0, r0 + S - 1, int(ncols) - 1));
         }
     }
     best = max(best, __reduce_max_sync(0xffffffffu, best));
@@ -1054,12 +1041,9 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             const bool xr_win = Nd::xr && t0.w != INT_MIN;
             if (lane < w) d[34 + lane] = __ldg(reinterpret_cast<const int *>(T + 1) + lane);
             if (lane == 0) {
-                const int4 tf = __ldg(T + 9 + kStagedMaxWidth);  // far slots (their d34: the raw offset)
                 d[0] = w;
                 d[1] = 1 | (xr_win ? 4 : 0);
                 d[66] = t0.w;
-                d[67] = tf.x;
-                d[68] = tf.y;
             }
             const uint32_t vbytes = uint32_t(w) * S * uint32_t(sizeof(V));
             const uint32_t rbytes = uint32_t(rows) * 4u;
@@ -1099,14 +1083,8 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         // anchor (anchored slice), gbase in [gmin, gmax]
         const int gmin = mt.anch ? mt.amin : r0;
         const int gmax = mt.anch ? mt.amax : r0 + S - 1;
-        // far groups (diagonal slices): single-offset groups far from the row, the first kStagedMaxFar
-        const bool farc = start && !mt.anch && last == lane && abs(offk) >= kStagedFarOffset;
-        unsigned fm = __ballot_sync(full, farc);
-        const unsigned fm0 = fm & (0u - fm);          // lowest
-        const unsigned fm1 = (fm & ~fm0) & (0u - (fm & ~fm0));  // second lowest
-        const bool far_slot = ((fm0 | fm1) >> lane) & 1u;
         int len = 0, lo_r = 0;
-        if (start && !far_slot) {
+        if (start) {
             // clamped columns of the group's gathers lie in [lo, hi]; the window covers it
             // rounded out to 16 bytes (ncols is a multiple of 4, so it stays inside x)
             const int lo = min(max(gmin + offk, 0), cmax);
@@ -1134,14 +1112,11 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         const bool interior = w > 0 && gmin + off_lo >= 0 && gmax + off_hi <= cmax;
         if (lane < w) {
             d[2 + lane] = offk;
-            // far slots gather through the caches: their descriptor is the raw offset
-            d[34 + lane] = far_slot ? offk : (interior ? (mt.anch ? 0 : r0) + offk + xb : xb);
+            d[34 + lane] = interior ? (mt.anch ? 0 : r0) + offk + xb : xb;
         }
         if (lane == 0) {
             d[0] = w;
             d[1] = (interior ? 1 : 0) | (mt.anch ? 2 : 0);
-            d[67] = fm0 ? __ffs(fm0) - 1 : -1;
-            d[68] = fm1 ? __ffs(fm1) - 1 : -1;
         }
         const uint32_t vbytes = uint32_t(w) * S * uint32_t(sizeof(V));
         const uint32_t rbytes = uint32_t(rows) * 4u;
@@ -1158,7 +1133,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         // stage is in flight; its wait runs out)
         if (cfg.withhold && blockIdx.x == 0 && wib == 0 && s == warp0) return;
         if (lane == 0 && vbytes) bulk_g2s(sg, vals + mt.base, vbytes, &bar[st]);
-        if (start && !far_slot) {
+        if (start) {
             if constexpr (XM == 2) {
                 bulk_g2s(sg + cfg.o_x + 4u * woff, e.w + lo_r, 4u * len, &bar[st]);
                 bulk_g2s(sg + cfg.o_x2 + 4u * woff, e.v + lo_r, 4u * len, &bar[st]);
@@ -1172,11 +1147,6 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         if (ANCH && mt.anch && lane == 4) bulk_g2s(sg + cfg.o_a, m.cols + mt.aux, S * 4u, &bar[st]);
     };
 
-    // x of column c through the caches (far slots)
-    auto xg = [&](int c) -> float {
-        if constexpr (XM == 2) return __ldg(e.w + c) * __ldg(e.v + c);
-        else return __ldg(e.x + c);
-    };
     // the product and epilogue of slice s from stage st
     auto compute = [&](int64_t s, int st) {
         const unsigned char *sg = stage0 + size_t(st) * cfg.stage_bytes;
@@ -1237,15 +1207,8 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 }
             }
         } else if (flags == 1) {
-            // diagonal, interior; the far slots' x through the caches, loaded first
+            // diagonal, interior
             const float *xl = sx + lane;
-            const int f0 = d[67], f1 = d[68];
-            float xa[R], xc[R];
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                xa[r] = f0 >= 0 ? xg(r0 + lane + 32 * r + d[34 + f0]) : 0.f;
-                xc[r] = f1 >= 0 ? xg(r0 + lane + 32 * r + d[34 + f1]) : 0.f;
-            }
 #pragma unroll 4
             for (int k = 0; k < w; ++k) {
                 const float *xp = xl + d[34 + k];
@@ -1254,9 +1217,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     float xv;
-                    if (k == f0) xv = xa[r];
-                    else if (k == f1) xv = xc[r];
-                    else if constexpr (XM == 2) xv = xp[32 * r] * xp[32 * r + (sx2 - sx)];
+                    if constexpr (XM == 2) xv = xp[32 * r] * xp[32 * r + (sx2 - sx)];
                     else xv = xp[32 * r];
                     acc[r] = fmaf(v[r], xv, acc[r]);
                 }
@@ -1270,21 +1231,18 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
 #pragma unroll
                 for (int r = 0; r < R; ++r) gb[r] = r0 + lane + 32 * r;
             }
-            const int f0 = d[67], f1 = d[68];  // -1 for anchored slices
 #pragma unroll 4
             for (int k = 0; k < w; ++k) {
                 const int off = d[2 + k];
                 const int xb = d[34 + k];
-                const bool far = k == f0 || k == f1;
                 float v[R];
                 smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
-                    const int cg = min(max(gb[r] + off, 0), cmax);
+                    const int c = min(max(gb[r] + off, 0), cmax) + xb;
                     float xv;
-                    if (far) xv = xg(cg);
-                    else if constexpr (XM == 2) xv = sx[cg + xb] * sx2[cg + xb];
-                    else xv = sx[cg + xb];
+                    if constexpr (XM == 2) xv = sx[c] * sx2[c];
+                    else xv = sx[c];
                     acc[r] = fmaf(v[r], xv, acc[r]);
                 }
             }
@@ -1520,8 +1478,7 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     c.o_a = o;
     if (s.nanch_slices) o += S * 4;
     c.stage_bytes = round128(o);
-    // a warp's header: the barriers (room for kStagedMaxStages) and one descriptor per stage
-    auto hdr_of = [](int nst) { return round128(8u * kStagedMaxStages + 4u * kStagedDesc * uint32_t(nst)); };
+    c.hdr_bytes = round128(8u * kStagedMaxStages + 4u * kStagedDesc * kStagedMaxStages);
     auto kern = k_sell_staged<V, EPI, XM, ANCH>;
     static bool attr = false;
     if (!attr) {
@@ -1536,7 +1493,7 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     // the final dots' reduction scratch, after the warps' rings (folded dots only)
     const uint32_t red_bytes = a.fa ? uint32_t(round128(sizeof(double) * kRedScratchDoubles)) : 0u;
     for (int nst = kStagedMaxStages; nst >= 2; --nst) {
-        const uint32_t cta = kStagedWarps * (hdr_of(nst) + uint32_t(nst) * c.stage_bytes) + red_bytes;
+        const uint32_t cta = kStagedWarps * (c.hdr_bytes + uint32_t(nst) * c.stage_bytes) + red_bytes;
         if (cta > 227u * 1024u) continue;
         int per_sm = 0;
         UGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStagedWarps * 32, cta));
@@ -1555,7 +1512,6 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (best_nst == 0) return false;
     if (best_per_sm * kStagedWarps < kStagedMinWarps && s.nslices >= 16 * int64_t(ctx.sms)) return false;
     c.nst = best_nst;
-    c.hdr_bytes = hdr_of(best_nst);
     c.spin = ctx.staged_test_spin > 0 ? ctx.staged_test_spin : kStagedSpinCycles;
     c.withhold = ctx.staged_test_spin > 0 ? 1 : 0;
     c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
@@ -1711,18 +1667,10 @@ void build_staged_templates(Mat &A, Sell &s, const std::vector<int32_t> &hw, con
             it = index.emplace(std::move(key), t).first;
             std::vector<int4> b(kTmplInt4, make_int4(0, 0, 0, 0));
             int *d34 = reinterpret_cast<int *>(&b[1]);
-            int nwin = 0, woff = 0, xr = INT_MIN, nfar = 0;
-            int far[kStagedMaxFar];
-            for (int &f : far) f = -1;
+            int nwin = 0, woff = 0, xr = INT_MIN;
             for (int a = 0; a < w;) {
                 int e = a;
                 while (e + 1 < w && o[e + 1] - o[e] <= kStagedGap) ++e;
-                if (e == a && std::abs(o[a]) >= kStagedFarOffset && nfar < kStagedMaxFar) {
-                    far[nfar++] = a;  // a far group: gathered through the caches, descriptor = the offset
-                    d34[a] = o[a];
-                    a = e + 1;
-                    continue;
-                }
                 const int lo_r = o[a] & ~3;               // relative to the slice's first row (a multiple of 4)
                 const int len = ((S - 1 + o[e] + 4) & ~3) - lo_r;
                 b[9 + nwin] = make_int4(lo_r, len, woff, 0);
@@ -1735,7 +1683,6 @@ void build_staged_templates(Mat &A, Sell &s, const std::vector<int32_t> &hw, con
                 a = e + 1;
             }
             b[0] = make_int4(w, nwin, woff, xr);
-            b[9 + kStagedMaxWidth] = make_int4(far[0], far[1], 0, 0);
             blocks.insert(blocks.end(), b.begin(), b.end());
         }
         tid[i] = it->second;
