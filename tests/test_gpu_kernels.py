@@ -186,7 +186,7 @@ def test_staged_kernel_matches_register_kernel(ctx, dtype):
     shared-memory staged kernel when every vector is 16-byte aligned; a vector 4 bytes into
     its allocation sends the same call to the register kernel.  Both sum each row over the
     same slots in the same order, so the product, residual, add and Jacobi forms agree bit
-    for bit: on the 7-point fine operator (24^3), its 27-point Galerkin coarse operator, the
+    for bit: on the 7-point fine operator (24^3 and 48^3), its 27-point Galerkin coarse operator, the
     trilinear interpolation P (anchored, x windows staged) and R = P^T (anchored; its x
     windows are too wide to stage, so both calls take the register kernel).  The transfers are
     taken at 108^3 -> 54^3 so that both have more
@@ -202,7 +202,9 @@ def test_staged_kernel_matches_register_kernel(ctx, dtype):
     Rm = U.SparseMatrix(ctx, P.CSR.from_scipy(Rsp))
     assert Rm.sell_info()["nslices"] > 8 * torch_sms()
     rng = np.random.default_rng(11)
-    for M, square in ((M64, True), (M64.ptap(P24), True), (Pm, False), (Rm, False)):
+    # 48^3: neighbour planes 2304 rows away (their windows staged like the others)
+    M48 = U.SparseMatrix(ctx, P.lognormal_diffusion_3d(48, 5)[0])
+    for M, square in ((M64, True), (M48, True), (M64.ptap(P24), True), (Pm, False), (Rm, False)):
         Mx = M.cast(dtype)
         assert Mx.sell_interleaved()
         n, m = M.nrows, M.ncols
