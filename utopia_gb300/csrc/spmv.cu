@@ -284,39 +284,14 @@ struct VecLoad<__nv_bfloat16, 4> {
     }
 };
 
-template <>
-struct VecLoad<float, 8> {
-    __device__ __forceinline__ static void load(const float *p, float (&v)[8]) {
-        const float4 a = __ldcs(reinterpret_cast<const float4 *>(p)), b = __ldcs(reinterpret_cast<const float4 *>(p) + 1);
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
-    }
-};
-template <>
-struct VecLoad<__nv_bfloat16, 8> {
-    __device__ __forceinline__ static void load(const __nv_bfloat16 *p, float (&v)[8]) {
-        const uint4 t = __ldcs(reinterpret_cast<const uint4 *>(p));
-        const uint32_t u[4] = {t.x, t.y, t.z, t.w};
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u[q]));
-            v[2 * q] = f.x;
-            v[2 * q + 1] = f.y;
-        }
-    }
-};
-
 template <int R>
 __device__ __forceinline__ void load_cols(const int32_t *p, int32_t (&c)[R]) {
     if constexpr (R == 2) {
         int2 t = __ldcs(reinterpret_cast<const int2 *>(p));
         c[0] = t.x; c[1] = t.y;
     } else {
-#pragma unroll
-        for (int q = 0; q < R / 4; ++q) {
-            const int4 t = __ldcs(reinterpret_cast<const int4 *>(p) + q);
-            c[4 * q] = t.x; c[4 * q + 1] = t.y; c[4 * q + 2] = t.z; c[4 * q + 3] = t.w;
-        }
+        int4 t = __ldcs(reinterpret_cast<const int4 *>(p));
+        c[0] = t.x; c[1] = t.y; c[2] = t.z; c[3] = t.w;
     }
 }
 
@@ -960,41 +935,25 @@ __global__ void k_sell_window_max(const int4 *hdr, const int32_t *offs, const in
     if ((threadIdx.x & 31) == 0) atomicMax(out, best);
 }
 
-// a lane's R values of one slot from the stage (R = 4: 16 / 8 bytes; R = 8: 32 / 16 bytes)
-template <class V, int R>
-__device__ __forceinline__ void smem_vals(const V *p, float (&v)[R]) {
-    if constexpr (std::is_same<V, float>::value) {
-#pragma unroll
-        for (int q = 0; q < R / 4; ++q) {
-            const float4 t = reinterpret_cast<const float4 *>(p)[q];
-            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
-        }
-    } else {
-        uint32_t u[R / 2];
-        if constexpr (R == 8) {
-            const uint4 t = *reinterpret_cast<const uint4 *>(p);
-            u[0] = t.x; u[1] = t.y; u[2] = t.z; u[3] = t.w;
-        } else {
-            const uint2 t = *reinterpret_cast<const uint2 *>(p);
-            u[0] = t.x; u[1] = t.y;
-        }
-#pragma unroll
-        for (int q = 0; q < R / 2; ++q) {
-            const float2 f = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&u[q]));
-            v[2 * q] = f.x;
-            v[2 * q + 1] = f.y;
-        }
-    }
+template <class V>
+__device__ __forceinline__ void smem_vals4(const V *p, float (&v)[4]);
+template <>
+__device__ __forceinline__ void smem_vals4<float>(const float *p, float (&v)[4]) {
+    const float4 t = *reinterpret_cast<const float4 *>(p);
+    v[0] = t.x; v[1] = t.y; v[2] = t.z; v[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void smem_vals4<__nv_bfloat16>(const __nv_bfloat16 *p, float (&v)[4]) {
+    const uint2 t = *reinterpret_cast<const uint2 *>(p);
+    const float2 fa = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.x));
+    const float2 fb = __bfloat1622float2(*reinterpret_cast<const __nv_bfloat162 *>(&t.y));
+    v[0] = fa.x; v[1] = fa.y; v[2] = fb.x; v[3] = fb.y;
 }
 
-// a lane's R anchors in a staged slice: rows l + 32 r sit at slot positions R l + r
-template <int R>
-__device__ __forceinline__ void stage_anchors(const int *sa, int lane, int (&a)[R]) {
-#pragma unroll
-    for (int q = 0; q < R / 4; ++q) {
-        const int4 t = *reinterpret_cast<const int4 *>(sa + R * lane + 4 * q);
-        a[4 * q] = t.x; a[4 * q + 1] = t.y; a[4 * q + 2] = t.z; a[4 * q + 3] = t.w;
-    }
+// a lane's four anchors in a staged slice: rows l + 32 r sit at slot positions 4 l + r
+__device__ __forceinline__ void stage_anchors(const int *sa, int lane, int (&a)[4]) {
+    const int4 q = *reinterpret_cast<const int4 *>(sa + 4 * lane);
+    a[0] = q.x; a[1] = q.y; a[2] = q.z; a[3] = q.w;
 }
 
 template <int EPI, int XM>
@@ -1005,12 +964,11 @@ struct StagedNeeds {
 };
 
 // ANCH: the operator has anchored slices (transfers); false compiles the diagonal-only kernel
-// R: rows per lane (4, or 8 for operators of at most 8 entries per row: 256-row slices)
-template <class V, int EPI, int XM, bool ANCH, int R>
+template <class V, int EPI, int XM, bool ANCH>
 __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, EpiParams<float> e, StagedCfg cfg,
                                                                    int *kflag) {
     if ((e.done && *e.done) || (e.gate && !*e.gate)) return;
-    constexpr int S = 32 * R;
+    constexpr int R = 4, S = 32 * R;
     using Nd = StagedNeeds<EPI, XM>;
     extern __shared__ __align__(128) unsigned char smem[];
     const int lane = threadIdx.x & 31;
@@ -1209,7 +1167,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             // values (and anchors) staged, x gathered through L1 / L2
             int gb[R];
             if (flags & 2) {
-                stage_anchors<R>(sa, lane, gb);
+                stage_anchors(sa, lane, gb);
             } else {
 #pragma unroll
                 for (int r = 0; r < R; ++r) gb[r] = r0 + lane + 32 * r;
@@ -1219,7 +1177,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             for (int k = 0; k < w; ++k) {
                 const int off = d[2 + k];
                 float v[R];
-                smem_vals<V, R>(sv + k * S + lane * R, v);
+                smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     int c = gb[r] + off;
@@ -1233,12 +1191,12 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
         } else if (ANCH && flags == 3) {
             // anchored, interior
             int a[R];
-            stage_anchors<R>(sa, lane, a);
+            stage_anchors(sa, lane, a);
 #pragma unroll 4
             for (int k = 0; k < w; ++k) {
                 const int dk = d[34 + k];
                 float v[R];
-                smem_vals<V, R>(sv + k * S + lane * R, v);
+                smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     const int c = a[r] + dk;
@@ -1255,7 +1213,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             for (int k = 0; k < w; ++k) {
                 const float *xp = xl + d[34 + k];
                 float v[R];
-                smem_vals<V, R>(sv + k * S + lane * R, v);
+                smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     float xv;
@@ -1268,7 +1226,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
             // boundary slice: clamp every gather
             int gb[R];
             if (ANCH && (flags & 2)) {
-                stage_anchors<R>(sa, lane, gb);
+                stage_anchors(sa, lane, gb);
             } else {
 #pragma unroll
                 for (int r = 0; r < R; ++r) gb[r] = r0 + lane + 32 * r;
@@ -1278,7 +1236,7 @@ __global__ void __launch_bounds__(kStagedWarps * 32) k_sell_staged(SellView m, E
                 const int off = d[2 + k];
                 const int xb = d[34 + k];
                 float v[R];
-                smem_vals<V, R>(sv + k * S + lane * R, v);
+                smem_vals4<V>(sv + k * S + lane * R, v);
 #pragma unroll
                 for (int r = 0; r < R; ++r) {
                     const int c = min(max(gb[r] + off, 0), cmax) + xb;
@@ -1485,13 +1443,13 @@ void sell_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
 
 inline uint32_t round128(uint32_t b) { return (b + 127u) & ~127u; }
 
-template <class V, int EPI, int XM, bool ANCH, int R>
+template <class V, int EPI, int XM, bool ANCH>
 bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
     const EpiParams<float> e = make_epi<float>(a);
     if (!e.vec_ok) return false;
     using Nd = StagedNeeds<EPI, XM>;
-    constexpr int S = 32 * R;
+    constexpr int S = 128;
     StagedCfg c{};
     const int wcap = std::max(1, s.max_width);
     // x windows wider than the budget (restrictions: anchors two fine points apart under nine
@@ -1520,9 +1478,8 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     c.o_a = o;
     if (s.nanch_slices) o += S * 4;
     c.stage_bytes = round128(o);
-    // a warp's header: the barriers (room for kStagedMaxStages) and one descriptor per stage
-    auto hdr_of = [](int nst) { return round128(8u * kStagedMaxStages + 4u * kStagedDesc * uint32_t(nst)); };
-    auto kern = k_sell_staged<V, EPI, XM, ANCH, R>;
+    c.hdr_bytes = round128(8u * kStagedMaxStages + 4u * kStagedDesc * kStagedMaxStages);
+    auto kern = k_sell_staged<V, EPI, XM, ANCH>;
     static bool attr = false;
     if (!attr) {
         UGPU_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
@@ -1536,7 +1493,7 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     // the final dots' reduction scratch, after the warps' rings (folded dots only)
     const uint32_t red_bytes = a.fa ? uint32_t(round128(sizeof(double) * kRedScratchDoubles)) : 0u;
     for (int nst = kStagedMaxStages; nst >= 2; --nst) {
-        const uint32_t cta = kStagedWarps * (hdr_of(nst) + uint32_t(nst) * c.stage_bytes) + red_bytes;
+        const uint32_t cta = kStagedWarps * (c.hdr_bytes + uint32_t(nst) * c.stage_bytes) + red_bytes;
         if (cta > 227u * 1024u) continue;
         int per_sm = 0;
         UGPU_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kStagedWarps * 32, cta));
@@ -1555,7 +1512,6 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (best_nst == 0) return false;
     if (best_per_sm * kStagedWarps < kStagedMinWarps && s.nslices >= 16 * int64_t(ctx.sms)) return false;
     c.nst = best_nst;
-    c.hdr_bytes = hdr_of(best_nst);
     c.spin = ctx.staged_test_spin > 0 ? ctx.staged_test_spin : kStagedSpinCycles;
     c.withhold = ctx.staged_test_spin > 0 ? 1 : 0;
     c.warp_bytes = c.hdr_bytes + uint32_t(best_nst) * c.stage_bytes;
@@ -1573,12 +1529,12 @@ bool staged_launch_t(Context &ctx, const Mat &A, const SpmvArgs &a) {
 // Launches the staged kernel when the matrix and vectors allow it; false otherwise.  Operators
 // with anchored slices (interpolations) take the anchored variant, built for the product and
 // the prolongation's add form only.
-template <class V, int EPI, int XM, int R>
+template <class V, int EPI, int XM>
 bool staged_launch(Context &ctx, const Mat &A, const SpmvArgs &a) {
     const Sell &s = *A.sell;
     if (!UGPU_SELL_STAGED || !s.interleaved || s.max_width > kStagedMaxWidth || s.nslices == 0) return false;
-    if (s.nanch_slices == 0) return staged_launch_t<V, EPI, XM, false, R>(ctx, A, a);
-    if constexpr ((EPI == EPI_ADD || EPI == EPI_STORE) && XM == 0) return staged_launch_t<V, EPI, XM, true, R>(ctx, A, a);
+    if (s.nanch_slices == 0) return staged_launch_t<V, EPI, XM, false>(ctx, A, a);
+    if constexpr ((EPI == EPI_ADD || EPI == EPI_STORE) && XM == 0) return staged_launch_t<V, EPI, XM, true>(ctx, A, a);
     return false;
 }
 
@@ -1606,24 +1562,11 @@ void dispatch_fmt(Context &ctx, const Mat &A, const SpmvArgs &a) {
     if (a.use_csr || A.format == UGPU_FORMAT_CSR || !A.sell) {
         csr_launch<V, T, EPI, XM, DOT>(ctx, A, a);
     } else {
-        constexpr bool kStageable = std::is_same<T, float>::value && !std::is_same<V, double>::value && !DOT &&
-                                    (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0 &&
-                                    !epi_writes_sw<EPI>();
-        if constexpr (!std::is_same<V, double>::value) {
-            if (A.sell->R == 8) {
-                // 256-row slices (operators of at most 8 entries per row, lane-interleaved): the
-                // staged kernel, or the register kernel (same slot order) where it cannot run
-                if constexpr (kStageable) {
-                    if (staged_launch<V, EPI, XM, 8>(ctx, A, a)) return;
-                }
-                sell_launch<V, T, 8, EPI, XM, DOT>(ctx, A, a);
-                return;
-            }
-        }
         constexpr int R = std::is_same<V, double>::value ? 2 : 4;
         UGPU_CHECK(A.sell->R == R, UGPU_ERR_INTERNAL, "sliced-ELL rows-per-thread mismatch");
-        if constexpr (kStageable) {
-            if (staged_launch<V, EPI, XM, 4>(ctx, A, a)) return;
+        if constexpr (std::is_same<T, float>::value && !std::is_same<V, double>::value && !DOT &&
+                      (XM == 0 || XM == 2) && EPI != EPI_CHEB && EPI != EPI_CHEB0 && !epi_writes_sw<EPI>()) {
+            if (staged_launch<V, EPI, XM>(ctx, A, a)) return;
         }
         // transfer-like operators (not all slices diagonal) with fewer than two slices per SM: in
         // the register kernel one lane per row would serialize each long row's gathers over too
@@ -1754,12 +1697,11 @@ void build_staged_templates(Mat &A, Sell &s, const std::vector<int32_t> &hw, con
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));  // the host vectors must outlive the copies
 }
 
-// The sliced-ELL layout of A with R rows per lane (slices of 32 R rows)
-static std::unique_ptr<Sell> build_sell_with(Mat &A, int R) {
+void build_sell(Mat &A) {
     Context &ctx = *A.ctx;
     auto s = std::make_unique<Sell>();
     const int sval = int(dtype_size(A.vdtype));
-    s->R = R;
+    s->R = (A.vdtype == UGPU_F64) ? 2 : 4;
     s->S = 32 * s->R;
     const int S = s->S;
     s->nslices = (A.nrows + S - 1) / S;
@@ -1857,21 +1799,7 @@ static std::unique_ptr<Sell> build_sell_with(Mat &A, int R) {
     s->xwin_max = h_wmax;
     if (ns && s->interleaved && h_wmax <= kStagedXBudget) build_staged_templates(A, *s, hw, aux);
     s->keys = std::move(offs_tmp);  // kept: a later values-only refresh re-runs the fill alone
-    return s;
-}
-
-// FP64: 2 rows per lane (16-byte value loads).  FP32 / BF16: 4 rows per lane, or 8 (256-row
-// slices) for operators of at most 8 entries per row whose slices all come out keyed and
-// lane-interleaved: the staged kernel's per-slice and per-slot work then serves twice the rows.
-void build_sell(Mat &A) {
-    if (A.vdtype != UGPU_F64 && A.max_row <= 8) {
-        auto s = build_sell_with(A, 8);
-        if (s->interleaved) {
-            A.sell = std::move(s);
-            return;
-        }
-    }
-    A.sell = build_sell_with(A, A.vdtype == UGPU_F64 ? 2 : 4);
+    A.sell = std::move(s);
 }
 
 // The values of A changed, its structure did not: the sliced-ELL values are filled again from
@@ -2061,13 +1989,8 @@ int ugpu_test_staged_wait_timeout(const ugpu_mat *A, const ugpu_vec *x, ugpu_vec
     ctx.staged_test_spin = spin_cycles;
     bool staged = false;
     if (A->impl.sell && A->impl.format == UGPU_FORMAT_SELL) {
-        const bool r8 = A->impl.sell && A->impl.sell->R == 8;
-        if (A->impl.vdtype == UGPU_F32)
-            staged = r8 ? staged_launch<float, EPI_STORE, 0, 8>(ctx, A->impl, a)
-                        : staged_launch<float, EPI_STORE, 0, 4>(ctx, A->impl, a);
-        else
-            staged = r8 ? staged_launch<__nv_bfloat16, EPI_STORE, 0, 8>(ctx, A->impl, a)
-                        : staged_launch<__nv_bfloat16, EPI_STORE, 0, 4>(ctx, A->impl, a);
+        if (A->impl.vdtype == UGPU_F32) staged = staged_launch<float, EPI_STORE, 0>(ctx, A->impl, a);
+        else staged = staged_launch<__nv_bfloat16, EPI_STORE, 0>(ctx, A->impl, a);
     }
     UGPU_LAUNCH_CHECK();
     *launched = staged ? 1 : 0;
