@@ -494,11 +494,7 @@ private:
         CgDev *dev = dev_.as<CgDev>();
         double *part = part_.as<double>();
         unsigned int *cnt = cnt_.as<unsigned int>();
-        // K2 and K3 stream four to six FP64 vectors with one to three FP64 operations per element: up
-        // to kSpmvDotGrid CTAs (the size of their partial regions) keep more loads and FMAs in flight
-        // than the reductions' default grid
-        const int g = int(std::max<int64_t>(1, std::min<int64_t>((n + 2 * kBlock - 1) / (2 * kBlock),
-                                                                 kSpmvDotGrid)));
+        const int g = reduce_grid(n);
         const bool f32 = mode_ == CG_GENERIC && pc_->pc_dtype() == UGPU_F32;
         // K0: p = z + beta p   (plain CG: p = r + beta p)
         // the solver's own vectors are cudaMalloc'd; only x may be caller memory
