@@ -174,3 +174,27 @@ def test_vector_reductions_and_transforms(ctx):
         w = U.Vector(ctx, v)
         assert lib.ugpu_vec_transform(w.h, op, param) == 0
         np.testing.assert_allclose(w.numpy(), f(v), rtol=1e-15)
+
+
+def test_mprgp_graph_and_eager_are_bitwise_equal(ctx, oracle):
+    """The graph form (the iteration under a WHILE node, the expansion tail under an IF node set on
+    the device) and the eager form (every kernel launched, the tail gated inside its kernels) give
+    the same iterates bit for bit on a problem with expansion steps; both match the oracle's
+    active set."""
+    N = 96
+    h = 1.0 / (N + 1)
+    A, b, lb, ub = P.obstacle_qp(N, seed=3, rhs=-10.0 * h * h)
+    atol = 1e-9 * h * h
+    out = {}
+    for graphs in (1, 0):
+        s = U.MPRGP(ctx, atol=atol, rtol=1e-30, max_it=100000, use_graphs=graphs)
+        s.set_box_constraints(U.Vector(ctx, lb), U.Vector(ctx, ub))
+        x = U.Vector(ctx, n=A.nrows)
+        s.solve(U.SparseMatrix(ctx, A), U.Vector(ctx, b), x)
+        out[graphs] = (x.numpy(), s.solution_status())
+    (xg, sg), (xe, se) = out[1], out[0]
+    assert sg["converged"] and se["converged"]
+    assert sg["iterates"] == se["iterates"]
+    assert np.array_equal(xg, xe)
+    xo, so = oracle.mprgp_solve(oracle.Matrix(A), b, lb, ub, atol=atol, rtol=1e-30, max_it=100000)
+    assert np.array_equal(xg == lb, xo == lb)
