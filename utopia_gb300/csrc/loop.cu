@@ -65,50 +65,6 @@ void DeviceLoop::build(Context &ctx, const std::function<void()> &body, const in
     ctx.launches = l0;
 }
 
-// The graph the context's stream is capturing into, or null when it is not capturing.
-cudaGraph_t capturing_graph(Context &ctx) {
-    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
-    cudaGraph_t g = nullptr;
-    UGPU_CUDA(cudaStreamGetCaptureInfo(ctx.stream, &st, nullptr, &g, nullptr, nullptr, nullptr));
-    return st == cudaStreamCaptureStatusActive ? g : nullptr;
-}
-
-// Appends to the capture of the context's stream an IF node on `handle` whose body is what `body`
-// enqueues on the context (captured on `side` into the node's body graph).  The node depends on
-// everything captured before it; what is captured after it depends on the node.
-void capture_if(Context &ctx, cudaGraphConditionalHandle handle, cudaStream_t side,
-                const std::function<void()> &body) {
-    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
-    cudaGraph_t g = nullptr;
-    const cudaGraphNode_t *deps = nullptr;
-    const cudaGraphEdgeData *edges = nullptr;
-    size_t nd = 0;
-    UGPU_CUDA(cudaStreamGetCaptureInfo(ctx.stream, &st, nullptr, &g, &deps, &edges, &nd));
-    UGPU_CHECK(st == cudaStreamCaptureStatusActive, UGPU_ERR_INTERNAL, "capture_if: the stream is not capturing");
-    cudaGraphNodeParams p{};
-    p.type = cudaGraphNodeTypeConditional;
-    p.conditional.handle = handle;
-    p.conditional.type = cudaGraphCondTypeIf;
-    p.conditional.size = 1;
-    cudaGraphNode_t node;
-    UGPU_CUDA(cudaGraphAddNode(&node, g, deps, edges, nd, &p));
-    UGPU_CUDA(cudaStreamUpdateCaptureDependencies(ctx.stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
-    cudaGraph_t bodyg = p.conditional.phGraph_out[0];
-    cudaStream_t main = ctx.stream;
-    UGPU_CUDA(cudaStreamBeginCaptureToGraph(side, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    ctx.stream = side;
-    try {
-        body();
-    } catch (...) {
-        ctx.stream = main;
-        cudaGraph_t tmp;
-        cudaStreamEndCapture(side, &tmp);
-        throw;
-    }
-    ctx.stream = main;
-    UGPU_CUDA(cudaStreamEndCapture(side, &bodyg));
-}
-
 // runs the loop; returns the number of body executions (synchronises)
 int DeviceLoop::run(Context &ctx) {
     UGPU_CHECK(exec, UGPU_ERR_STATE, "device loop not built");

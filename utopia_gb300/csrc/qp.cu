@@ -121,8 +121,7 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, dou
                                                       double *fi, double *beta, const double *q,
                                                       const double *lb, const double *ub, double alpha_bar,
                                                       QpDev *dev, double *partials, unsigned int *counter,
-                                                      double atol, double rtol, long long max_it,
-                                                      cudaGraphConditionalHandle hexp) {
+                                                      double atol, double rtol, long long max_it) {
     if (dev->done) return;
     const int cg = dev->gate_cg;
     const double a0 = dev->qa0, a1 = dev->qa1;
@@ -131,7 +130,6 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, dou
         if (blockIdx.x == 0 && threadIdx.x == 0) {
             qp_stop(dev, UGPU_DIVERGED_INDEFINITE, 1);
             dev->gate_exp = 0;
-            if (hexp) cudaGraphSetConditional(hexp, 0u);
         }
         return;
     }
@@ -151,7 +149,6 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, dou
                 dev->alpha_f = alpha_f;
                 dev->step = st;
                 dev->gate_exp = st;
-                if (hexp) cudaGraphSetConditional(hexp, unsigned(st));  // the expansion tail runs
             }
         } else {
             s_alpha = a1 / a0;
@@ -159,7 +156,6 @@ __global__ void __launch_bounds__(kBlock) k_mprgp_step(int64_t n, double *x, dou
             if (blockIdx.x == 0) {
                 dev->step = 0;
                 dev->gate_exp = 0;
-                if (hexp) cudaGraphSetConditional(hexp, 0u);
             }
         }
     }
@@ -569,8 +565,6 @@ public:
     }
     ~Mprgp() override {
         if (host_) cudaFreeHost(host_);
-        loop_.reset();
-        if (side_) cudaStreamDestroy(side_);
     }
     void set(const std::string &k, double v) override {
         Solver::set(k, v);
@@ -640,7 +634,6 @@ private:
     const double *rhs_ = nullptr;
     DeviceLoop loop_;
     LoopKey key_;
-    cudaStream_t side_ = nullptr;  // captures the expansion tail's IF body
 
     void final_kernel(double *x, const double *lb, const double *ub, int first) {
         const int64_t n = op->nrows;
@@ -687,37 +680,23 @@ private:
             a.done = &dev->done;
             launch_spmv(*ctx, *op, a);
         }
-        // Captured into the solve's graph, the expansion tail sits under an IF node whose condition
-        // the step kernel sets: iterations without an expansion launch neither of its kernels.
-        // Run eagerly, both kernels are launched and return at once (their device gate).
-        cudaGraph_t capg = capturing_graph(*ctx);
-        cudaGraphConditionalHandle hexp = 0;
-        if (capg) {
-            if (!side_) UGPU_CUDA(cudaStreamCreateWithFlags(&side_, cudaStreamNonBlocking));
-            UGPU_CUDA(cudaGraphConditionalHandleCreate(&hexp, capg, 0, cudaGraphCondAssignDefault));
-        }
         k_mprgp_step<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
             n, x, g_.as<double>(), p_.as<double>(), fi_.as<double>(), beta_.as<double>(), Ap_.as<double>(), lb, ub,
-            alpha_bar_, dev, part + 2 * kSpmvDotGrid, cnt + 4, get("atol"), get("rtol"), (long long)get("max_it"),
-            hexp);
+            alpha_bar_, dev, part + 2 * kSpmvDotGrid, cnt + 4, get("atol"), get("rtol"), (long long)get("max_it"));
         ctx->launches++;
         UGPU_LAUNCH_CHECK();
-        auto tail = [&] {
-            {   // g = A x - b   [expansion step only]
-                SpmvArgs a;
-                a.x = x;
-                a.v = rhs_;
-                a.y = g_.ptr;
-                a.vec_dtype = UGPU_F64;
-                a.epilogue = EPI_SUB;
-                a.done = &dev->done;
-                a.gate = &dev->gate_exp;
-                launch_spmv(*ctx, *op, a);
-            }
-            final_kernel(x, lb, ub, 0);
-        };
-        if (capg) capture_if(*ctx, hexp, side_, tail);
-        else tail();
+        {   // g = A x - b   [expansion step only]
+            SpmvArgs a;
+            a.x = x;
+            a.v = rhs_;
+            a.y = g_.ptr;
+            a.vec_dtype = UGPU_F64;
+            a.epilogue = EPI_SUB;
+            a.done = &dev->done;
+            a.gate = &dev->gate_exp;
+            launch_spmv(*ctx, *op, a);
+        }
+        final_kernel(x, lb, ub, 0);
     }
 
     // MPRGP::power_method (utopia_MPRGP.hpp:351-387)

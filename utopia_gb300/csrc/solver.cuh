@@ -127,11 +127,6 @@ struct DeviceLoop {
     int run(Context &ctx);
 };
 
-// stream-capture helpers for conditional work inside a captured loop body (loop.cu)
-cudaGraph_t capturing_graph(Context &ctx);
-void capture_if(Context &ctx, cudaGraphConditionalHandle handle, cudaStream_t side,
-                const std::function<void()> &body);
-
 std::unique_ptr<Solver> make_cg(Context *c);
 std::unique_ptr<Solver> make_multigrid(Context *c);
 std::unique_ptr<Solver> make_invdiag(Context *c);
