@@ -372,8 +372,7 @@ struct PgsDev {
 };
 
 // x += c; ||x_new - x_old||; convergence (stol on the step, or atol on the projected gradient)
-// (c is zeroed behind the read: the next step's correction starts from zero without a pass of its own)
-__global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, double *c, PgsDev *dev,
+__global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, const double *c, PgsDev *dev,
                                                       double *partials, unsigned int *counter, double stol,
                                                       long long max_it, int pg_stop) {
     if (dev->done) return;
@@ -381,7 +380,6 @@ __global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, dou
     QP_LOOP(i, n) {
         const double xo = x[i];
         const double xn = xo + c[i];
-        c[i] = 0.0;
         x[i] = xn;
         const double d = xn - xo;
         acc = fma(d, d, acc);
@@ -799,7 +797,6 @@ public:
         const double *lb, *ub;
         bounds(n, &lb, &ub);
         UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
-        UGPU_CUDA(cudaMemsetAsync(c_.ptr, 0, c_.bytes, ctx->stream));  // each step's correction starts at zero
         run_loop(loop_, key_, {x.data(), lb, ub, rhs.data()}, 0.0,
                  [&] { step(rhs.as<double>(), x.as<double>(), lb, ub, false); }, &dev_.as<PgsDev>()->done, dev_, host_,
                  sizeof(PgsDev));
@@ -824,7 +821,6 @@ public:
         const double *lb, *ub;
         bounds(n, &lb, &ub);
         UGPU_CUDA(cudaMemsetAsync(dev_.ptr, 0, sizeof(PgsDev), ctx->stream));
-        UGPU_CUDA(cudaMemsetAsync(c_.ptr, 0, c_.bytes, ctx->stream));  // each step's correction starts at zero
         for (int s = 0; s < sweeps; ++s) step(rhs.as<double>(), x.as<double>(), lb, ub, true);
     }
 
@@ -972,6 +968,7 @@ private:
                                                                            hi_.as<double>(), &dev->done);
         }
         ctx->launches++;
+        enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
         for (int c : colour_passes()) {
             const int64_t m = colour_count[c];
             if (sliced_) {
