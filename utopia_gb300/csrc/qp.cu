@@ -372,11 +372,13 @@ struct PgsDev {
 };
 
 // x += c; ||x_new - x_old||; convergence (stol on the step, or atol on the projected gradient)
-__global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *x, const double *c, PgsDev *dev,
-                                                      double *partials, unsigned int *counter, double stol,
-                                                      long long max_it, int pg_stop) {
+__global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *__restrict__ x,
+                                                      const double *__restrict__ c, PgsDev *dev, double *partials,
+                                                      unsigned int *counter, double stol, long long max_it,
+                                                      int pg_stop) {
     if (dev->done) return;
     double acc = 0;
+#pragma unroll 4
     QP_LOOP(i, n) {
         const double xo = x[i];
         const double xn = xo + c[i];
