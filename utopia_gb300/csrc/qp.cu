@@ -304,40 +304,48 @@ __global__ void __launch_bounds__(kBlock) k_pgs_colour(const int32_t *rows, int6
 // The same sweep over a colour-sliced layout: the rows of one colour in ascending order, their
 // off-diagonal entries slot-major (entry k of the colour's row q at k m + q: every slot is one
 // coalesced load over the colour's rows), padded with (the row itself, 0), which subtracts an
-// exact zero; the diagonal inverses compacted per colour.  Same operations in the same order as
-// k_pgs_colour.
+// exact zero; the diagonal inverses, r and the step bounds compacted per colour (r_c, lo_c and
+// hi_c start at the colour's first position), so only c is gathered.  Same operations in the same
+// order as k_pgs_colour.
 __global__ void __launch_bounds__(kBlock) k_pgs_colour_sliced(const int32_t *rows, int64_t m, int w,
                                                              const int32_t *cols, const double *vals,
-                                                             const double *dinv_c, const double *r,
-                                                             const double *lo, const double *hi, double *c,
+                                                             const double *dinv_c, const double *r_c,
+                                                             const double *lo_c, const double *hi_c, double *c,
                                                              const int *done) {
     if (*done) return;
     QP_LOOP(q, m) {
         const int32_t i = rows[q];
-        double s = r[i];
+        double s = r_c[q];
         for (int k = 0; k < w; ++k) s -= vals[k * m + q] * c[cols[k * m + q]];
         double v = dinv_c[q] * s;
-        const double h = hi[i], l = lo[i];
+        const double h = hi_c[q], l = lo_c[q];
         v = dlt(h, v) ? h : v;
         v = dlt(v, l) ? l : v;
         c[i] = v;
     }
 }
 
-__global__ void k_pgs_max_row(const int32_t *rp, int64_t n, unsigned int *mx) {
+// the most off-diagonal entries of a row (the colour-sliced layout's width)
+__global__ void k_pgs_max_row(const int32_t *rp, const int32_t *ci, int64_t n, unsigned int *mx) {
     unsigned int v = 0;
-    QP_LOOP(i, n) v = max(v, unsigned(rp[i + 1] - rp[i]));
+    QP_LOOP(i, n) {
+        unsigned int k = 0;
+        for (int32_t e = rp[i]; e < rp[i + 1]; ++e) k += ci[e] != int32_t(i) ? 1u : 0u;
+        v = max(v, k);
+    }
     v = __reduce_max_sync(0xffffffffu, v);
     if ((threadIdx.x & 31) == 0) atomicMax(mx, v);
 }
 
-// the colour-sliced layout of one colour (k_pgs_colour_sliced), from the CSR rows (w at least the
-// longest row, so the off-diagonal entries always fit)
-__global__ void k_pgs_slice_colour(const int32_t *rows, int64_t m, int w, const int32_t *rp, const int32_t *ci,
-                                   const double *cv, const double *dinv, int32_t *cols, double *vals,
-                                   double *dinv_c) {
+// the colour-sliced layout of one colour (k_pgs_colour_sliced), from the CSR rows (w the most
+// off-diagonal entries of a row, so they always fit; shorter rows pad with zero entries), and
+// each row's colour-ordered position
+__global__ void k_pgs_slice_colour(const int32_t *rows, int64_t m, int64_t off, int w, const int32_t *rp,
+                                   const int32_t *ci, const double *cv, const double *dinv, int32_t *cols,
+                                   double *vals, double *dinv_c, int32_t *pos) {
     QP_LOOP(q, m) {
         const int32_t i = rows[q];
+        pos[i] = int32_t(off + q);  // the row's colour-ordered position
         int k = 0;
         for (int32_t e = rp[i]; e < rp[i + 1]; ++e) {
             if (ci[e] == i) continue;
@@ -356,12 +364,15 @@ __global__ void k_pgs_slice_colour(const int32_t *rows, int64_t m, int w, const 
 // the step bounds lo = lb - x, hi = ub - x (smoothing steps; the solver's steps get them from
 // the projected-gradient kernel)
 __global__ void __launch_bounds__(kBlock) k_pgs_bounds(int64_t n, const double *x, const double *lb,
-                                                      const double *ub, double *lo, double *hi, const int *done) {
+                                                      const double *ub, const double *r, double *lo, double *hi,
+                                                      const int32_t *pos, double *r_c, const int *done) {
     if (*done) return;
     QP_LOOP(i, n) {
         const double xi = x[i];
-        lo[i] = lb[i] - xi;
-        hi[i] = ub[i] - xi;
+        const int64_t j = pos ? int64_t(pos[i]) : i;
+        lo[j] = lb[i] - xi;
+        hi[j] = ub[i] - xi;
+        if (pos) r_c[j] = r[i];
     }
 }
 
@@ -408,19 +419,23 @@ __global__ void __launch_bounds__(kBlock) k_pgs_finish(int64_t n, double *__rest
 
 // projected-gradient norm || P(x - g) - x || with g = -r (r = b - A x); optional stop test; the
 // step's bounds lo = lb - x, hi = ub - x
+// (pos: with the colour-sliced layout, lo, hi and a copy of r go to the rows' colour-ordered
+// positions pos[i], where the colour passes read them contiguously; null: natural order, no copy)
 __global__ void __launch_bounds__(kBlock) k_pgs_pgnorm(int64_t n, const double *x, const double *r, const double *lb,
-                                                      const double *ub, double *lo, double *hi, PgsDev *dev,
-                                                      double *partials, unsigned int *counter, double atol,
-                                                      int pg_stop) {
+                                                      const double *ub, double *lo, double *hi, const int32_t *pos,
+                                                      double *r_c, PgsDev *dev, double *partials,
+                                                      unsigned int *counter, double atol, int pg_stop) {
     if (dev->done) return;
     double acc = 0;
     QP_LOOP(i, n) {
         const double xi = x[i];
-        const double l = lb[i], u = ub[i];
-        const double d = proj(l, u, xi + r[i]) - xi;
+        const double l = lb[i], u = ub[i], ri = r[i];
+        const double d = proj(l, u, xi + ri) - xi;
         acc = fma(d, d, acc);
-        lo[i] = l - xi;
-        hi[i] = u - xi;
+        const int64_t j = pos ? int64_t(pos[i]) : i;
+        lo[j] = l - xi;
+        hi[j] = u - xi;
+        if (pos) r_c[j] = ri;
     }
     double a[1] = {acc};
     block_reduce_store<1>(a, 1, partials, gridDim.x, blockIdx.x);
@@ -837,7 +852,7 @@ private:
     Buffer dinv_, r_, c_, lo_, hi_, dev_, part_, cnt_, rows_;
     bool sliced_ = false;  // the colour passes read the colour-sliced layout
     int sliced_w_ = 0;
-    Buffer slice_cols_, slice_vals_, dinv_c_;
+    Buffer slice_cols_, slice_vals_, dinv_c_, pos_, r_c_;  // layout, diagonal inverses, positions, r copy
     std::vector<int64_t> colour_off_;
     PgsDev *host_ = nullptr;
     DeviceLoop loop_;
@@ -894,7 +909,8 @@ private:
             Buffer mx;
             mx.alloc(sizeof(unsigned int));
             UGPU_CUDA(cudaMemsetAsync(mx.ptr, 0, sizeof(unsigned int), ctx->stream));
-            k_pgs_max_row<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(op->rowptr.as<int32_t>(), n,
+            k_pgs_max_row<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(op->rowptr.as<int32_t>(),
+                                                                            op->colidx.as<int32_t>(), n,
                                                                             mx.as<unsigned int>());
             ctx->launches++;
             UGPU_CUDA(cudaMemcpyAsync(&hmax, mx.ptr, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
@@ -909,15 +925,17 @@ private:
             slice_cols_.alloc(sizeof(int32_t) * slots);
             slice_vals_.alloc(sizeof(double) * slots);
             dinv_c_.alloc(sizeof(double) * size_t(n));
+            pos_.alloc(sizeof(int32_t) * size_t(n));
+            r_c_.alloc(sizeof(double) * size_t(n));
             for (int c = 0; c < ncolours; ++c) {
                 const int64_t m = colour_count[c];
                 if (!m) continue;
                 const size_t base = size_t(sliced_w_) * size_t(colour_off_[c]);
                 k_pgs_slice_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
-                    rows_.as<int32_t>() + colour_off_[c], m, sliced_w_, op->rowptr.as<int32_t>(),
+                    rows_.as<int32_t>() + colour_off_[c], m, colour_off_[c], sliced_w_, op->rowptr.as<int32_t>(),
                     op->colidx.as<int32_t>(), op->vals.as<double>(), dinv_.as<double>(),
                     slice_cols_.as<int32_t>() + base, slice_vals_.as<double>() + base,
-                    dinv_c_.as<double>() + colour_off_[c]);
+                    dinv_c_.as<double>() + colour_off_[c], pos_.as<int32_t>());
                 ctx->launches++;
             }
             UGPU_LAUNCH_CHECK();
@@ -963,11 +981,13 @@ private:
         }
         if (!smoothing) {
             k_pgs_pgnorm<<<reduce_grid(n), kBlock, 0, ctx->stream>>>(
-                n, x, r_.as<double>(), lb, ub, lo_.as<double>(), hi_.as<double>(), dev, part_.as<double>(),
+                n, x, r_.as<double>(), lb, ub, lo_.as<double>(), hi_.as<double>(),
+                sliced_ ? pos_.as<int32_t>() : nullptr, r_c_.as<double>(), dev, part_.as<double>(),
                 cnt_.as<unsigned int>() + 0, get("atol"), pg_stop);
         } else {
-            k_pgs_bounds<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(n, x, lb, ub, lo_.as<double>(),
-                                                                           hi_.as<double>(), &dev->done);
+            k_pgs_bounds<<<stream_grid(*ctx, n), kBlock, 0, ctx->stream>>>(
+                n, x, lb, ub, r_.as<double>(), lo_.as<double>(), hi_.as<double>(),
+                sliced_ ? pos_.as<int32_t>() : nullptr, r_c_.as<double>(), &dev->done);
         }
         ctx->launches++;
         enq_set(*ctx, UGPU_F64, n, 0.0, c_.ptr, &dev->done);
@@ -975,10 +995,11 @@ private:
             const int64_t m = colour_count[c];
             if (sliced_) {
                 const size_t base = size_t(sliced_w_) * size_t(colour_off_[c]);
+                const int64_t o = colour_off_[c];
                 k_pgs_colour_sliced<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
-                    rows_.as<int32_t>() + colour_off_[c], m, sliced_w_, slice_cols_.as<int32_t>() + base,
-                    slice_vals_.as<double>() + base, dinv_c_.as<double>() + colour_off_[c], r_.as<double>(),
-                    lo_.as<double>(), hi_.as<double>(), c_.as<double>(), &dev->done);
+                    rows_.as<int32_t>() + o, m, sliced_w_, slice_cols_.as<int32_t>() + base,
+                    slice_vals_.as<double>() + base, dinv_c_.as<double>() + o, r_c_.as<double>() + o,
+                    lo_.as<double>() + o, hi_.as<double>() + o, c_.as<double>(), &dev->done);
             } else {
                 k_pgs_colour<<<stream_grid(*ctx, m), kBlock, 0, ctx->stream>>>(
                     rows_.as<int32_t>() + colour_off_[c], m, op->rowptr.as<int32_t>(), op->colidx.as<int32_t>(),
