@@ -96,6 +96,14 @@ extern "C" {
                                    * ugpu_mg_set_transfer_operators (coarse -> fine; the last one is the fine-level
                                    * transfer truncated on the active set) */
 
+#define UGPU_SOLVER_SHIFTED_PENALTY 11 /* utopia::ShiftedPenaltyQPSolver (penalty/utopia_ShiftedPenaltyQPSolver_impl.hpp:
+                                   * 87-156) with utopia::ShiftedPenalty: the upper bound of ugpu_qp_set_box_constraints
+                                   * is the constraint (a missing one is the largest double, as
+                                   * fill_empty_bounds makes it, and a lower bound is inert); keys penalty_parameter,
+                                   * penalty_parameter_max (0: = penalty_parameter), penalty_parameter_factor,
+                                   * zero_shift_on_reset, linear_rtol, linear_max_it; the inner solver is CG + Jacobi
+                                   * to linear_rtol * ||rhs|| unless one is set through ugpu_solver_set_preconditioner */
+
 /* convergence reasons (utopia/solvers/utopia_ConvergenceReason.hpp) */
 #define UGPU_CONVERGED_FNORM_ABS 2
 #define UGPU_CONVERGED_FNORM_RELATIVE 3
@@ -341,6 +349,17 @@ UGPU_API int ugpu_amg_parent(const ugpu_solver *amg, int level, int32_t *parent,
  * ugpu_mmg_active_set: the active-set indicator (ActiveSet::indicator, 0/1 per fine dof, n
  * entries; may be NULL) and its size after the last update/apply. */
 UGPU_API int ugpu_mmg_active_set(const ugpu_solver *mmg, int32_t *indicator, int64_t *n_active);
+
+/* The shifted-penalty QP solver's optional terms (ShiftedPenaltyQPSolver::set_transform,
+ * set_selection, set_scaling_matrix; utopia_ShiftedPenaltyQPSolver.hpp:17-53, utopia_Penalty.hpp:
+ * 49-55).  Transformation: square T and O of the operator's size; the constraint acts on
+ * O^T (T x), directions map back by T^T (O v) and the penalty Hessian diag(h) by T^T (O^T diag(h) O) T
+ * (the qp_solve app's PrototypeTransformation, utopia/apps/qp_solve/utopia_qp_solve.cpp:68-88).
+ * Selection: the penalty gradient and Hessian are multiplied by it entrywise.  Scaling: S maps both.
+ * NULL clears a term; the solver keeps the pointers (the caller keeps the objects alive). */
+UGPU_API int ugpu_penalty_set_transform(ugpu_solver *s, const ugpu_mat *T, const ugpu_mat *O);
+UGPU_API int ugpu_penalty_set_selection(ugpu_solver *s, const ugpu_vec *selection);
+UGPU_API int ugpu_penalty_set_scaling_matrix(ugpu_solver *s, const ugpu_mat *S);
 
 /* ---------------------------------------------------------------- files ---- */
 /* PETSc binary matrices and vectors (utopia::read / write over MatLoad / VecLoad, used for the

@@ -89,6 +89,8 @@ def lib():
                 "or_agglomerate": (_vp, [_vp, _i64, _d, C.c_int, _vp]),
                 "or_bicgstab_solve": (C.c_int, [_vp, _vp, _vp, C.c_int, _vp, _d, _i64, _vp]),
                 "or_ssn_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _d, _i64, _d, _vp]),
+                "or_penalty_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _vp,
+                                               C.c_int, _d, _i64, _d, _i64, _vp]),
                 "or_mmg_solve": (C.c_int, [_vp, _vp, _vp, _vp, _vp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_int,
                                            C.c_int, C.c_int, C.c_int, _d, _d, C.c_int, _d, _d, _d, _i64, _vp,
                                            _vp, _vp]),
@@ -336,6 +338,28 @@ def ssn_solve(A: Matrix, b, lb=None, ub=None, x0=None, stol=1e-11, max_it=1000, 
     st = Status()
     lib().or_ssn_solve(A.h, _p(b), lbp, ubp, _p(x), stol, max_it, linear_rtol, C.byref(st))
     return x, st.as_dict()
+
+
+def penalty_solve(A: Matrix, b, lb=None, ub=None, x0=None, selection=None, T=None, O=None, S=None,
+                  penalty_parameter=1e4, penalty_parameter_max=None, penalty_parameter_factor=1.5, shift=None,
+                  stol=1e-11, max_it=1000, linear_rtol=1e-12, linear_max_it=10000):
+    """ShiftedPenaltyQPSolver (utopia_ShiftedPenaltyQPSolver_impl.hpp:87-156) with the ShiftedPenalty
+    term; CG + InvDiag inner solves.  penalty_parameter_max None: = penalty_parameter (as read()
+    sets it).  shift: a constraint-space shift to start from (None: zero, the reset default);
+    returns x, status and the final shift."""
+    b = _f64(b)
+    x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+    keep = [None if v is None else _f64(v) for v in (lb, ub, selection)]
+    m = b.size  # T and O are square (the transformation maps R^n to R^n)
+    sh = np.zeros(m) if shift is None else _f64(shift).copy()
+    st = Status()
+    pmax = penalty_parameter if penalty_parameter_max is None else penalty_parameter_max
+    lbp, ubp, selp = [_p(v) if v is not None else None for v in keep]
+    lib().or_penalty_solve(A.h, _p(b), lbp, ubp, _p(x), selp, T.h if T is not None else None, O.h if O is not None else None,
+                           S.h if S is not None else None, penalty_parameter, pmax, penalty_parameter_factor,
+                           _p(sh), 1 if shift is None else 0, stol, max_it, linear_rtol, linear_max_it,
+                           C.byref(st))
+    return x, st.as_dict(), sh
 
 
 def monotone_mg_solve(A: Matrix, b, lb, ub, P_coarse_to_fine, x0=None, colour=None, pre=3, post=3,

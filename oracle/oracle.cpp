@@ -1264,6 +1264,160 @@ int or_ssn_solve(const void *hA, const double *b, const double *lb_in, const dou
     return st->converged;
 }
 
+// ShiftedPenaltyQPSolver::apply (utopia/solvers/nonlinear/constrained/penalty/
+// utopia_ShiftedPenaltyQPSolver_impl.hpp:87-156) with the ShiftedPenalty term
+// (utopia/solvers/nonlinear/constrained/penalty/utopia_ShiftedPenalty.hpp): per iteration
+//   g = A x - b; ShiftedPenalty::update (update_shift_aux, :348-463, then
+//   p = min(p_max, factor p)); c = gradient (penalty_gradient -p dps, :32-50); H_pen = hessian
+//   (active p on the diagonal, :52-75, :181-237); g = -(g + c); H = A + H_pen; c = 0;
+//   solve H c = g; x += c; stop on check_convergence(it, 1, 1, ||c||).
+// The constraint is the upper bound: update() fills a missing one with the largest double
+// (VariableBoundSolverInterface::init_memory, BoxConstraints::fill_empty_bounds), so the
+// upper-bound branch of update_shift_aux (:357-409) always runs and a lower bound is inert.
+// Selection (Penalty::apply_selection, utopia_Penalty.hpp:51-55) multiplies the constraint-space
+// terms; a scaling matrix S maps them (S v); a transformation (T, O) works in the constraint
+// space w = O^T (T x), maps directions back by T^T (O v) and the penalty Hessian by
+// T^T (O^T D O) T (qp_solve app, utopia/apps/qp_solve/utopia_qp_solve.cpp:68-88).
+// T and O are square (n x n).  Inner solves: CG + InvDiag (H is symmetric positive definite) to
+// linear_rtol * ||g||.
+// shift_io: the shift in constraint space, read (unless zero_shift) and written back.
+Csr mat_add(const Csr &A, const Csr &B) {  // MatAXPY(A, 1, B, DIFFERENT_NONZERO_PATTERN)
+    Csr C;
+    C.n = A.n;
+    C.m = A.m;
+    C.rp.assign(A.n + 1, 0);
+    for (int64_t i = 0; i < A.n; ++i) {
+        int32_t a = A.rp[i], b = B.rp[i];
+        while (a < A.rp[i + 1] || b < B.rp[i + 1]) {
+            const int32_t ca = a < A.rp[i + 1] ? A.ci[a] : INT32_MAX;
+            const int32_t cb = b < B.rp[i + 1] ? B.ci[b] : INT32_MAX;
+            if (ca == cb) {
+                C.ci.push_back(ca);
+                C.v.push_back(A.v[a++] + B.v[b++]);
+            } else if (ca < cb) {
+                C.ci.push_back(ca);
+                C.v.push_back(A.v[a++]);
+            } else {
+                C.ci.push_back(cb);
+                C.v.push_back(B.v[b++]);
+            }
+        }
+        C.rp[i + 1] = int32_t(C.ci.size());
+    }
+    return C;
+}
+
+Csr diag_csr(const std::vector<double> &h) {
+    Csr D;
+    D.n = D.m = int64_t(h.size());
+    D.rp.resize(h.size() + 1);
+    D.ci.resize(h.size());
+    for (size_t i = 0; i < h.size(); ++i) {
+        D.rp[i] = int32_t(i);
+        D.ci[i] = int32_t(i);
+    }
+    D.rp[h.size()] = int32_t(h.size());
+    D.v = h;
+    return D;
+}
+
+int or_penalty_solve(const void *hA, const double *b, const double *lb, const double *ub, double *x,
+                     const double *selection, const void *hT, const void *hO, const void *hS, double penalty,
+                     double penalty_max, double factor, double *shift_io, int zero_shift, double stol,
+                     int64_t max_it, double linear_rtol, int64_t linear_max_it, or_status *st) {
+    const Csr &A = *static_cast<const Csr *>(hA);
+    const int64_t n = A.n;
+    const bool trafo = hT && hO;
+    const Csr *T = trafo ? static_cast<const Csr *>(hT) : nullptr;
+    const Csr *O = trafo ? static_cast<const Csr *>(hO) : nullptr;
+    const Csr *S = static_cast<const Csr *>(hS);
+    const int64_t m = n;  // T and O are square: the constraint space has the problem's size
+    (void)lb;
+    std::vector<double> ubfill;
+    if (!ub) {
+        ubfill.assign(n, std::numeric_limits<double>::max());
+        ub = ubfill.data();
+    }
+    Csr Ot, Tt;
+    if (trafo) {
+        Ot = transpose(*O);
+        Tt = transpose(*T);
+    }
+    Params p;
+    p.stol = stol;
+    p.max_it = max_it;
+    *st = or_status{};
+    double pcur = penalty;  // ShiftedPenalty::reset
+    std::vector<double> shift(m, 0.0), active(m), dps(m), w(m), gc(m), h(m), tmp(std::max(n, m)), g(n), c(n);
+    if (!zero_shift) std::copy(shift_io, shift_io + m, shift.begin());
+    int64_t lin_its = 0;
+    bool converged = false;
+    for (int64_t it = 1; it <= max_it; ++it) {
+        residual(A, b, x, g.data());
+        for (int64_t i = 0; i < n; ++i) g[i] = -g[i];  // A x - b
+        // constraint-space position
+        if (trafo) {
+            spmv(*T, x, tmp.data());
+            spmv(Ot, tmp.data(), w.data());
+        } else {
+            std::copy(x, x + n, w.begin());
+        }
+        for (int64_t i = 0; i < m; ++i) {  // update_shift_aux
+            const double di = ub[i] - w[i];
+            double si = shift[i];
+            double d = di + si;
+            const bool a = d <= 0;
+            si = double(a) * d;
+            d = double(a) * (di + si);
+            active[i] = a;
+            shift[i] = si;
+            dps[i] = d;
+        }
+        pcur = std::min(penalty_max, factor * pcur);
+        for (int64_t i = 0; i < m; ++i) {
+            gc[i] = 0.0 - pcur * dps[i];
+            h[i] = active[i] * pcur;
+            if (selection) {
+                gc[i] = selection[i] * gc[i];
+                h[i] = selection[i] * h[i];
+            }
+        }
+        if (S) {
+            spmv(*S, gc.data(), tmp.data());
+            std::copy(tmp.begin(), tmp.begin() + m, gc.begin());
+            spmv(*S, h.data(), tmp.data());
+            std::copy(tmp.begin(), tmp.begin() + m, h.begin());
+        }
+        Csr Hpen;
+        if (trafo) {
+            spmv(*O, gc.data(), tmp.data());
+            spmv(Tt, tmp.data(), c.data());
+            Hpen = ptap(ptap(diag_csr(h), *O), *T);
+        } else {
+            std::copy(gc.begin(), gc.end(), c.begin());
+            Hpen = diag_csr(h);
+        }
+        for (int64_t i = 0; i < n; ++i) g[i] = -(g[i] + c[i]);
+        const Csr H = mat_add(A, Hpen);
+        std::fill(c.begin(), c.end(), 0.0);
+        Params lp;
+        lp.atol = linear_rtol * norm2(n, g.data());
+        lp.max_it = linear_max_it;
+        InvDiag M(H);
+        or_status lst{};
+        pcg(H, g.data(), c.data(), M, lp, lst);
+        lin_its += lst.iterates;
+        for (int64_t i = 0; i < n; ++i) x[i] += c[i];
+        const double norm_c = norm2(n, c.data());
+        converged = check_convergence(p, *st, it, 1, 1, norm_c);
+        if (converged) break;
+    }
+    if (shift_io) std::copy(shift.begin(), shift.end(), shift_io);
+    st->converged = st->reason > 0;
+    st->spmv_count = lin_its;
+    return st->converged;
+}
+
 // MonotoneMultigrid::update/apply/step (utopia/solvers/multilevel/utopia_MonotoneMultigrid.hpp:135-319):
 // pre_smoothing_steps projected Gauss-Seidel steps on the fine level, the active set of
 // ActiveSet::determine (utopia/solvers/nonlinear/constrained/utopia_ActiveSet.hpp:47-84:

@@ -39,7 +39,7 @@ SUPPORT_SOURCES = [
     "utopia_core/console/utopia_Logger.cpp", "utopia_core/utopia_Tracer.cpp",
     "utopia_core/interfaces/utopia_Communicator.cpp", "utopia_core/utopia_BackendInfo.cpp",
 ]
-_MODULES = ["utopia_core", "solvers", "utils", "ui", "interoperability", "differentiable"]
+_MODULES = ["utopia_core", "solvers", "utils", "ui", "interoperability", "differentiable", "backend/polymorphic"]
 
 _lock = threading.Lock()
 _lib = None
@@ -130,6 +130,8 @@ def lib():
                 "ref_cg_solve": (_i32, [_vp, _vp, _vp, _i32, _vp, _d, _d, _d, _i64, _vp]),
                 "ref_mprgp_solve": (_i32, [_vp, _vp, _vp, _vp, _vp, _d, _d, _i64, _vp]),
                 "ref_pgs_solve": (_i32, [_vp, _vp, _vp, _vp, _vp, _d, _i64, _i32, _i32, _vp]),
+                "ref_penalty_solve": (_i32, [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i32, _i32,
+                                             _d, _i64, _d, _i64, _vp]),
             }
             for name, (res, args) in sig.items():
                 f = getattr(L, name)
@@ -240,4 +242,25 @@ def pgs_solve(A: Matrix, b, lb, ub, x0=None, stol=1e-11, max_it=1000, n_local_sw
     if lib().ref_pgs_solve(A.h, _p(b), _p(lb), _p(ub), _p(x), stol, max_it, n_local_sweeps, int(symmetric),
                            C.byref(st)) != 0:
         raise RuntimeError("reference projected Gauss-Seidel failed")
+    return x, st.as_dict()
+
+
+def penalty_solve(A: Matrix, b, lb=None, ub=None, x0=None, selection=None, T=None, O=None, S=None,
+                  penalty_parameter=1e4, penalty_parameter_max=None, penalty_parameter_factor=1.5,
+                  zero_shift_on_reset=True, n_solves=1, stol=1e-11, max_it=1000, linear_rtol=1e-12,
+                  linear_max_it=10000):
+    """The reference's ShiftedPenaltyQPSolver (CG + InvDiag inner solves to linear_rtol ||rhs||);
+    n_solves consecutive solves by one solver object, each from the previous x."""
+    b = _f64(b)
+    lb, ub, selection = (None if v is None else _f64(v) for v in (lb, ub, selection))
+    x = np.zeros_like(b) if x0 is None else _f64(x0).copy()
+    st = Status()
+    pmax = penalty_parameter if penalty_parameter_max is None else penalty_parameter_max
+    rc = lib().ref_penalty_solve(A.h, _p(b), _p(lb), _p(ub), _p(x), _p(selection),
+                                 T.h if T is not None else None, O.h if O is not None else None,
+                                 S.h if S is not None else None, penalty_parameter, pmax, penalty_parameter_factor,
+                                 int(bool(zero_shift_on_reset)), int(n_solves), stol, max_it, linear_rtol,
+                                 linear_max_it, C.byref(st))
+    if rc != 0:
+        raise RuntimeError("reference shifted-penalty solver failed")
     return x, st.as_dict()

@@ -11,6 +11,8 @@
 //   Chebyshev3level + PowerMethod, Jacobi, PointJacobi (utopia/solvers/smoothers/, eigensolvers/)
 //   MPRGP (utopia/solvers/nonlinear/constrained/quadratic_programming/utopia_MPRGP.hpp:57-387)
 //   ProjectedGaussSeidel (.../utopia_ProjectedGaussSeidel.hpp:71-112,197-318)
+//   ShiftedPenaltyQPSolver + ShiftedPenalty (utopia/solvers/nonlinear/constrained/penalty/), with
+//     the qp_solve app's transformation (utopia/apps/qp_solve/utopia_qp_solve.cpp:68-88)
 // The coarse-level direct solver is a dense Cholesky (the reference's tests pass PETSc's
 // Factorization there), with the restated oracle's arithmetic order.
 #include "utopia_ref_backend.hpp"
@@ -25,6 +27,9 @@
 #include "utopia_PointJacobi.hpp"
 #include "utopia_ProjectedGaussSeidel.hpp"
 #include "utopia_TrivialPreconditioners.hpp"
+#include "utopia_ShiftedPenaltyQPSolver_impl.hpp"
+#include "utopia_TransformedBoxConstraints.hpp"
+#include "utopia_InputParameters.hpp"
 
 #include <cstdint>
 #include <cstdlib>
@@ -47,6 +52,23 @@ RefVector make_vec(int64_t n, const double *v) {
     if (v) std::copy(v, v + n, x.data().begin());
     return x;
 }
+
+// ConjugateGradient whose absolute tolerance is rel * ||b|| of each system it solves (a
+// LinearSolver that forwards to the reference's CG, which is final)
+class RelTolCG final : public LinearSolver<RefMatrix, RefVector> {
+public:
+    std::shared_ptr<ConjugateGradient<RefMatrix, RefVector>> cg = std::make_shared<ConjugateGradient<RefMatrix, RefVector>>();
+    double rel = 1e-12;
+    void update(const std::shared_ptr<const RefMatrix> &op) override {
+        LinearSolver<RefMatrix, RefVector>::update(op);
+        cg->update(op);
+    }
+    bool apply(const RefVector &b, RefVector &x) override {
+        cg->atol(rel * norm2(b));
+        return cg->apply(b, x);
+    }
+    RelTolCG *clone() const override { return new RelTolCG(*this); }
+};
 
 }  // namespace
 
@@ -215,6 +237,65 @@ int ref_pgs_solve(const void *hA, const double *b, const double *lb, const doubl
         const bool ok = pgs.solve(*A, bv, xv);
         std::copy(xv.data().begin(), xv.data().end(), x);
         fill_status(pgs.solution_status(), ok, st);
+        return 0;
+    } catch (...) {
+        return -1;
+    }
+}
+
+// ShiftedPenaltyQPSolver with the upper bound (else the lower bound) as its constraint.  Inner
+// solves: the reference's ConjugateGradient + InvDiagPreconditioner stopped at
+// linear_rtol * ||rhs|| of each system (the rule the restated oracle and the GPU solver use).
+// T/O: the transformation (both or neither), S: a scaling matrix, selection: a 0/1 vector (any
+// may be null).  n_solves consecutive solves by the same solver object, each from the previous
+// x (the shift carries over unless zero_shift_on_reset); the status is the last one's.
+int ref_penalty_solve(const void *hA, const double *b, const double *lb, const double *ub, double *x,
+                      const double *selection, const void *hT, const void *hO, const void *hS, double penalty,
+                      double penalty_max, double factor, int zero_shift, int n_solves, double stol, int64_t max_it,
+                      double linear_rtol, int64_t linear_max_it, ref_status *st) {
+    try {
+        auto A = std::make_shared<RefMatrix>(*static_cast<const RefMatrix *>(hA));
+        const int64_t n = A->nrows;
+        RefVector bv = make_vec(n, b), xv = make_vec(n, x);
+        auto lin = std::make_shared<RelTolCG>();
+        lin->rel = linear_rtol;
+        lin->cg->max_it(linear_max_it);
+        lin->cg->set_preconditioner(std::make_shared<InvDiagPreconditioner<RefMatrix, RefVector>>());
+        ShiftedPenaltyQPSolver<RefMatrix, RefVector> qp(lin);
+        auto params = param_list(param("penalty_parameter", penalty), param("penalty_parameter_max", penalty_max),
+                                 param("penalty_parameter_factor", factor),
+                                 param("zero_shift_on_reset", zero_shift != 0));
+        qp.read(params);
+        qp.stol(stol);
+        qp.max_it(max_it);
+        auto l = std::make_shared<RefVector>(make_vec(n, lb));
+        auto u = std::make_shared<RefVector>(make_vec(n, ub));
+        qp.set_box_constraints(BoxConstraints<RefVector>(lb ? l : nullptr, ub ? u : nullptr));
+        if (selection) qp.set_selection(std::make_shared<RefVector>(make_vec(n, selection)));
+        if (hS) qp.set_scaling_matrix(std::make_shared<RefMatrix>(*static_cast<const RefMatrix *>(hS)));
+        RefMatrix T, O;
+        if (hT && hO) {
+            T = *static_cast<const RefMatrix *>(hT);
+            O = *static_cast<const RefMatrix *>(hO);
+            auto tr = std::make_shared<PrototypeTransformation<RefMatrix, RefVector>>();
+            tr->fun_transform_position = [&](const RefVector &in, RefVector &out) {
+                RefVector t = T * in;
+                out = transpose(O) * t;
+            };
+            tr->fun_inverse_transform_direction = [&](const RefVector &in, RefVector &out) {
+                RefVector t = O * in;
+                out = transpose(T) * t;
+            };
+            tr->fun_transform_matrix = [&](const RefMatrix &D, RefMatrix &out) {
+                RefMatrix t = transpose(O) * D * O;
+                out = transpose(T) * t * T;
+            };
+            qp.set_transform(tr);
+        }
+        bool ok = false;
+        for (int k = 0; k < n_solves; ++k) ok = qp.solve(*A, bv, xv);
+        std::copy(xv.data().begin(), xv.data().end(), x);
+        fill_status(qp.solution_status(), ok, st);
         return 0;
     } catch (...) {
         return -1;

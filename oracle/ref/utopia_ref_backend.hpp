@@ -334,6 +334,12 @@ public:
     using Super::Super;
     using BLAS2Matrix<RefMatrix, RefVector>::multiply;
     using BLAS3Matrix<RefMatrix>::multiply;
+    using BLAS3Matrix<RefMatrix>::transpose_multiply;
+    // y = A^T x (MatMultTranspose, PetscMatrix::transpose_multiply, utopia_petsc_Matrix.cpp:1368-1380)
+    void transpose_multiply(const RefVector &x, RefVector &y) const override { gemv(true, 1.0, x, 0.0, y); }
+    void transpose_multiply(const Scalar &alpha, const RefVector &x, RefVector &y) const override {
+        gemv(true, alpha, x, 0.0, y);
+    }
 
     template <class Expr>
     RefMatrix(const Expression<Expr> &expr) {
@@ -556,6 +562,10 @@ public:
                 if (colidx[size_t(k)] == i) vals[size_t(k)] += a;
     }
     void shift_diag(const RefVector &d) {
+        if (empty()) {  // an empty matrix becomes diag(d) (PetscMatrix::shift_diag, utopia_petsc_Matrix.cpp:1783-1789)
+            diag(d);
+            return;
+        }
         for (SizeType i = 0; i < nrows; ++i)
             for (int k = rowptr[size_t(i)]; k < rowptr[size_t(i) + 1]; ++k)
                 if (colidx[size_t(k)] == i) vals[size_t(k)] += d.get(i);

@@ -198,3 +198,140 @@ def test_mprgp_graph_and_eager_are_bitwise_equal(ctx, oracle):
     assert np.array_equal(xg, xe)
     xo, so = oracle.mprgp_solve(oracle.Matrix(A), b, lb, ub, atol=atol, rtol=1e-30, max_it=100000)
     assert np.array_equal(xg == lb, xo == lb)
+
+
+def _penalty_gpu(ctx, A, b, ub=None, lb=None, selection=None, T=None, O=None, S=None, x0=None, solver=None, **prm):
+    s = solver or U.ShiftedPenaltyQPSolver(ctx, **prm)
+    keep = [U.Vector(ctx, v) if v is not None else None for v in (lb, ub, selection)]
+    s.set_box_constraints(keep[0], keep[1])
+    if selection is not None:
+        s.set_selection(keep[2])
+    mats = [U.SparseMatrix(ctx, M) if M is not None else None for M in (T, O, S)]
+    if T is not None:
+        s.set_transform(mats[0], mats[1])
+    if S is not None:
+        s.set_scaling_matrix(mats[2])
+    x = U.Vector(ctx, x0) if x0 is not None else U.Vector(ctx, n=A.nrows)
+    Ad = U.SparseMatrix(ctx, A)
+    s.solve(Ad, U.Vector(ctx, b), x)
+    return x.numpy(), s.solution_status(), s, (keep, mats, Ad)
+
+
+def test_shifted_penalty_reference_test_problem(ctx, oracle):
+    """ShiftedPenaltyQPSolver on the reference's own test problem (utopia_QPSolverTest.cpp:407-424:
+    1D Laplacian, n = 20, upper bound 30, max_it 40 n) through the C ABI: the oracle's iterations
+    and reason, x to 1e-12 and below the bound up to the penalty's residual violation."""
+    A, b, ub = P.qp_test_problem_1d(20)
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, ub=ub, max_it=800)
+    xg, st, _, _ = _penalty_gpu(ctx, A, b, ub=ub, max_it=800)
+    assert st["converged"] and so["converged"]
+    assert st["iterates"] == so["iterates"] and st["reason"] == so["reason"]
+    assert np.linalg.norm(xg - xo) <= 1e-12 * np.linalg.norm(xo)
+    assert xg.max() <= 30.0 + 1e-6 and xg.max() >= 30.0 - 1e-6
+
+
+@pytest.mark.parametrize("variant", ["plain", "selection_scaling", "transformation"])
+def test_shifted_penalty_matches_oracle(ctx, oracle, variant):
+    """128^2 Laplacian with an upper bound (contact under a load), plain, with a 0/1 selection and a
+    diagonal scaling matrix, and with the qp_solve app's transformation (T, O block rotations):
+    same iterations and reason as the oracle (pinned bit for bit to the reference's solver), x to
+    1e-9, and in the plain case the MPRGP minimiser to 1e-6."""
+    N = 128
+    h = 1.0 / (N + 1)
+    A, b, _, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    b = -b
+    n = A.nrows
+    cap = np.full(n, 0.02)
+    rng = np.random.default_rng(1)
+    kw = dict(ub=cap)
+    if variant == "selection_scaling":
+        kw["selection"] = (rng.uniform(size=n) < 0.8).astype(float)
+        import scipy.sparse as sp
+        kw["S"] = P.CSR.from_scipy(sp.diags(rng.uniform(0.5, 2.0, n)).tocsr())
+    if variant == "transformation":
+        kw["T"], kw["O"] = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    okw = {k: (oracle.Matrix(v) if isinstance(v, P.CSR) else v) for k, v in kw.items()}
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, max_it=300, **okw)
+    xg, st, _, _ = _penalty_gpu(ctx, A, b, max_it=300, **kw)
+    assert so["converged"] and st["converged"]
+    assert st["iterates"] == so["iterates"] and st["reason"] == so["reason"]
+    assert np.linalg.norm(xg - xo) <= 1e-9 * np.linalg.norm(xo)
+    if variant == "plain":
+        Am = oracle.Matrix(A)
+        xm, sm = oracle.mprgp_solve(Am, b, np.full(n, -np.finfo(float).max), cap, atol=1e-12, max_it=50000)
+        assert sm["converged"]
+        assert np.linalg.norm(xg - xm) <= 1e-6 * np.linalg.norm(xm)
+
+
+def test_shifted_penalty_lower_bound_is_inert(ctx, oracle):
+    """As in the reference, a lower bound alone is not enforced (the missing upper bound is filled
+    with the largest double and update_shift_aux takes its upper-bound branch): the solve returns
+    the unconstrained minimiser, as the oracle does."""
+    N = 64
+    h = 1.0 / (N + 1)
+    A, b, lb, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, lb=lb, max_it=50)
+    xg, st, _, _ = _penalty_gpu(ctx, A, b, lb=lb, max_it=50)
+    assert st["iterates"] == so["iterates"] == 2
+    assert np.linalg.norm(xg - xo) <= 1e-10 * np.linalg.norm(xo)
+    assert (xg < lb).any()
+
+
+def test_shifted_penalty_warm_shift_and_linear_solver_slot(ctx, oracle):
+    """zero_shift_on_reset 0: the second solve by the same solver starts from the first one's
+    shift (fewer iterations, the oracle's count); a caller-set inner solver (CG + Jacobi at a
+    tighter tolerance) takes the place of the default one."""
+    N = 64
+    h = 1.0 / (N + 1)
+    A, b, _, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    b = -b
+    n = A.nrows
+    cap = np.full(n, 0.02)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    To, Oo = oracle.Matrix(T), oracle.Matrix(O)
+    x1, s1, shift = oracle.penalty_solve(oracle.Matrix(A), b, ub=cap, T=To, O=Oo, max_it=200)
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, x0=x1, ub=cap, T=To, O=Oo, shift=shift, max_it=200)
+    s = U.ShiftedPenaltyQPSolver(ctx, max_it=200, zero_shift_on_reset=0)
+    xg1, st1, s, keep = _penalty_gpu(ctx, A, b, ub=cap, T=T, O=O, solver=s)
+    assert st1["iterates"] == s1["iterates"]
+    xv = U.Vector(ctx, xg1)
+    s.apply(U.Vector(ctx, b), xv)
+    st2 = s.solution_status()
+    assert st2["iterates"] == so["iterates"] < s1["iterates"]
+    assert np.linalg.norm(xv.numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
+    # the inner-solver slot
+    cg = U.ConjugateGradient(ctx, atol=1e-14, max_it=20000)
+    cg.set_preconditioner(U.InvDiagPreconditioner(ctx))
+    s2 = U.ShiftedPenaltyQPSolver(ctx, max_it=200)
+    s2.set_linear_solver(cg)
+    xg, st, _, _ = _penalty_gpu(ctx, A, b, ub=cap, solver=s2)
+    xp, sp_, _ = oracle.penalty_solve(oracle.Matrix(A), b, ub=cap, max_it=200)
+    assert st["converged"]
+    assert np.linalg.norm(xg - xp) <= 1e-8 * np.linalg.norm(xp)
+
+
+def test_qp_solve_shifted_penalty_app(ctx, oracle, tmp_path):
+    """The reference's qp_solve app (QPSolveApp::solve_with_shifted_penalty, utopia_qp_solve.cpp:
+    61-107) on files: A, T, O, rhs, upper_bound, is_contact; the constraint acts on O^T (T x).  The
+    written x is the oracle's shifted-penalty solution with the same transformation."""
+    from utopia_gb300 import qp_solve
+
+    N = 64
+    h = 1.0 / (N + 1)
+    A, b, _, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    b = -b
+    n = A.nrows
+    cap = np.full(n, 0.02)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    for name, m in (("A", A), ("T", T), ("O", O)):
+        U.SparseMatrix(ctx, m).write_petsc(str(tmp_path / name))
+    for name, v in (("rhs", b), ("upper_bound", cap), ("is_contact", np.ones(n))):
+        U.Vector(ctx, v).write_petsc(str(tmp_path / name))
+    out = qp_solve.main(["--dir", str(tmp_path), "--solver", "shifted_penalty", "--max_it", "200",
+                         "--out", str(tmp_path / "out.bin")])
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, ub=cap, T=oracle.Matrix(T), O=oracle.Matrix(O),
+                                     max_it=200)
+    assert out["converged"] and so["converged"] and out["iterations"] == so["iterates"]
+    assert out["violation"] <= 1e-8
+    x = U.read_petsc_vector(ctx, str(tmp_path / "out.bin")).numpy()
+    assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)

@@ -284,3 +284,20 @@ def test_oracle_monotone_multigrid_variants(oracle, levels, csi, smoother):
     assert st["converged"], st
     assert np.abs(x - xs).max() < 1e-10
     np.testing.assert_array_equal(act.astype(bool), xs <= lb + 1e-12)
+
+
+def test_oracle_shifted_penalty_reaches_the_mprgp_minimiser(oracle):
+    """ShiftedPenaltyQPSolver restatement (utopia_ShiftedPenaltyQPSolver_impl.hpp:87-156) with an
+    upper bound: converges to the minimiser MPRGP finds (the shift drives the violation to zero)."""
+    N = 40
+    h = 1.0 / (N + 1)
+    A, b, _, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    b = -b
+    cap = np.full(A.nrows, 0.02)
+    Am = oracle.Matrix(A)
+    x, st, shift = oracle.penalty_solve(Am, b, ub=cap, max_it=200)
+    assert st["converged"] and st["iterates"] < 30
+    xm, sm = oracle.mprgp_solve(Am, b, np.full(A.nrows, -np.finfo(float).max), cap, atol=1e-12, max_it=20000)
+    assert sm["converged"]
+    assert np.linalg.norm(x - xm) <= 1e-6 * np.linalg.norm(xm)
+    assert x.max() <= 0.02 + 1e-8 and (shift < 0).any()

@@ -116,3 +116,55 @@ def test_projected_gauss_seidel_lexicographic(oracle, R):
     assert so["iterates"] == sr["iterates"] and so["reason"] == sr["reason"]
     assert same(xo == lb, xr == lb)
     assert same(xo, xr)
+
+
+def _penalty_cases():
+    N = 32
+    h = 1.0 / (N + 1)
+    A, b, lb, _ = P.obstacle_qp(N, seed=3, rhs=-5 * h * h)
+    n = A.nrows
+    rng = np.random.default_rng(1)
+    sel = (rng.uniform(size=n) < 0.8).astype(float)
+    S = P.CSR.from_scipy(__import__("scipy.sparse", fromlist=["diags"]).diags(rng.uniform(0.5, 2.0, n)).tocsr())
+    cap = np.full(n, 0.02)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    A1, b1, ub1 = P.qp_test_problem_1d(20)
+    return {
+        "qp_test_problem_1d": (A1, b1, dict(ub=ub1, max_it=800)),
+        "upper_bound": (A, -b, dict(ub=cap, max_it=200)),
+        "lower_bound_is_inert": (A, b, dict(lb=lb, max_it=200)),
+        "selection_and_scaling": (A, -b, dict(ub=cap, selection=sel, S=S, max_it=200)),
+        "transformation": (A, -b, dict(ub=cap, T=T, O=O, max_it=200)),
+        "growing_penalty": (A, -b, dict(ub=cap, T=T, O=O, penalty_parameter=1e2, penalty_parameter_max=1e6,
+                                        max_it=200)),
+    }
+
+
+@pytest.mark.parametrize("case", ["qp_test_problem_1d", "upper_bound", "lower_bound_is_inert",
+                                  "selection_and_scaling", "transformation", "growing_penalty"])
+def test_shifted_penalty(oracle, R, case):
+    """ShiftedPenaltyQPSolver + ShiftedPenalty (with the qp_solve app's transformation, a
+    selection and a scaling matrix): iterations, reason and x bit for bit.  The first case is the
+    reference's own test problem (utopia_QPSolverTest.cpp:407-424, QPSolverTestProblem)."""
+    A, b, kw = _penalty_cases()[case]
+
+    def mats(M):
+        return {k: (M(v) if isinstance(v, P.CSR) else v) for k, v in kw.items()}
+
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, **mats(oracle.Matrix))
+    xr, sr = R.penalty_solve(R.Matrix(A), b, **mats(R.Matrix))
+    assert so["iterates"] == sr["iterates"] and so["reason"] == sr["reason"] and so["converged"]
+    assert same(xo, xr)
+
+
+def test_shifted_penalty_keeps_its_shift(oracle, R):
+    """zero_shift_on_reset false: a second solve by the same solver object starts from the
+    previous solve's shift (ShiftedPenalty::reset, utopia_ShiftedPenalty.hpp:552-566)."""
+    A, b, kw = _penalty_cases()["transformation"]
+    T, O = oracle.Matrix(kw["T"]), oracle.Matrix(kw["O"])
+    x1, s1, shift = oracle.penalty_solve(oracle.Matrix(A), b, ub=kw["ub"], T=T, O=O, max_it=200)
+    xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, x0=x1, ub=kw["ub"], T=T, O=O, shift=shift, max_it=200)
+    xr, sr = R.penalty_solve(R.Matrix(A), b, ub=kw["ub"], T=R.Matrix(kw["T"]), O=R.Matrix(kw["O"]),
+                             zero_shift_on_reset=False, n_solves=2, max_it=200)
+    assert so["iterates"] == sr["iterates"] < s1["iterates"]
+    assert same(xo, xr)

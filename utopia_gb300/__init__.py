@@ -516,6 +516,34 @@ class SemismoothNewton(_QPSolver):
         self.ctx.check(self.ctx.lib.ugpu_solver_set_preconditioner(self.h, solver.h))
 
 
+class ShiftedPenaltyQPSolver(_QPSolver):
+    """utopia::ShiftedPenaltyQPSolver with utopia::ShiftedPenalty: the upper bound is enforced by a
+    shifted quadratic penalty, one linear solve per iteration (as in the reference, a lower bound
+    alone is inert: the missing upper bound is filled with the largest double).  Keys
+    penalty_parameter, penalty_parameter_max, penalty_parameter_factor, zero_shift_on_reset,
+    linear_rtol, linear_max_it).  set_linear_solver replaces the default inner CG + Jacobi;
+    set_transform(T, O), set_selection and set_scaling_matrix add the optional terms."""
+
+    KIND = _abi.SOLVER_SHIFTED_PENALTY
+
+    def set_linear_solver(self, solver):
+        self._linear = solver
+        self.ctx.check(self.ctx.lib.ugpu_solver_set_preconditioner(self.h, solver.h))
+
+    def set_transform(self, T: SparseMatrix | None, O: SparseMatrix | None):
+        self._trafo = (T, O)
+        self.ctx.check(self.ctx.lib.ugpu_penalty_set_transform(self.h, T.h if T is not None else None,
+                                                               O.h if O is not None else None))
+
+    def set_selection(self, selection: Vector | None):
+        self._selection = selection
+        self.ctx.check(self.ctx.lib.ugpu_penalty_set_selection(self.h, selection.h if selection is not None else None))
+
+    def set_scaling_matrix(self, S: SparseMatrix | None):
+        self._scaling = S
+        self.ctx.check(self.ctx.lib.ugpu_penalty_set_scaling_matrix(self.h, S.h if S is not None else None))
+
+
 class MPRGP(_QPSolver):
     KIND = _abi.SOLVER_MPRGP
 

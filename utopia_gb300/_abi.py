@@ -23,6 +23,7 @@ SOLVER_AMG = 7
 SOLVER_BICGSTAB = 8
 SOLVER_SSNEWTON = 9
 SOLVER_MONOTONE_MG = 10
+SOLVER_SHIFTED_PENALTY = 11
 
 _lock = threading.Lock()
 _lib = None
@@ -122,6 +123,9 @@ SIGNATURES = {
     "ugpu_pgs_colouring": [_vp, _vp, C.POINTER(_int)],
     "ugpu_amg_parent": [_vp, _int, _vp, C.POINTER(_i64), C.POINTER(_i64)],
     "ugpu_mmg_active_set": [_vp, _vp, C.POINTER(_i64)],
+    "ugpu_penalty_set_transform": [_vp, _vp, _vp],
+    "ugpu_penalty_set_selection": [_vp, _vp],
+    "ugpu_penalty_set_scaling_matrix": [_vp, _vp],
     "ugpu_petsc_read_mat": [_vp, C.c_char_p, _pp],
     "ugpu_petsc_read_vec": [_vp, C.c_char_p, _pp],
     "ugpu_petsc_write_mat": [_vp, C.c_char_p],

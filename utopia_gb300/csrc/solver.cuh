@@ -137,6 +137,7 @@ std::unique_ptr<Solver> make_amg(Context *c);
 std::unique_ptr<Solver> make_bicgstab(Context *c);
 std::unique_ptr<Solver> make_ssnewton(Context *c);
 std::unique_ptr<Solver> make_monotone_mg(Context *c);
+std::unique_ptr<Solver> make_shifted_penalty(Context *c);
 // the multigrid inside an algebraic multigrid solver (any other solver: itself)
 const Solver *amg_multigrid(const Solver *s);
 

@@ -55,6 +55,7 @@ int ugpu_solver_create(ugpu_ctx *ctx, int kind, ugpu_solver **out) {
         case UGPU_SOLVER_BICGSTAB: s->impl = make_bicgstab(c); break;
         case UGPU_SOLVER_SSNEWTON: s->impl = make_ssnewton(c); break;
         case UGPU_SOLVER_MONOTONE_MG: s->impl = make_monotone_mg(c); break;
+        case UGPU_SOLVER_SHIFTED_PENALTY: s->impl = make_shifted_penalty(c); break;
         default: throw Error(UGPU_ERR_ARG, "unknown solver kind");
     }
     *out = s.release();

@@ -374,6 +374,34 @@ def laplacian_1d_dirichlet(n: int) -> CSR:
     return CSR.from_scipy(_sp.csr_matrix((vals, (rows, cols)), shape=(n, n)))
 
 
+def qp_test_problem_1d(n: int = 20):
+    """QPSolverTestProblem::run (utopia/tests/test_problems/utopia_QPSolverTestProblem.hpp:29-97):
+    the 1D Laplacian (-1, 2, -1) with rows 0 and n-1 set to the identity (their off-diagonal entry
+    kept as an explicit zero), rhs 1 with 0 at both ends, upper bound 30; returns A, rhs, ub."""
+    rows, cols, vals = [0, 0, n - 1, n - 1], [0, 1, n - 2, n - 1], [1.0, 0.0, 0.0, 1.0]
+    for i in range(1, n - 1):
+        rows += [i, i, i]
+        cols += [i - 1, i, i + 1]
+        vals += [-1.0, 2.0, -1.0]
+    A = _sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    b = np.ones(n)
+    b[0] = b[-1] = 0.0
+    return CSR.from_scipy(A), b, np.full(n, 30.0)
+
+
+def block_rotation(n: int, seed: int) -> CSR:
+    """An orthogonal sparse matrix: independent 2 x 2 rotations of the pairs (2k, 2k+1) by random
+    angles (the last row the identity when n is odd) -- a stand-in for a contact rotation."""
+    rng = np.random.default_rng(seed)
+    th = rng.uniform(0.0, 2.0 * np.pi, n // 2)
+    c, s = np.cos(th), np.sin(th)
+    i = np.arange(n // 2) * 2
+    rows = np.concatenate([i, i, i + 1, i + 1] + ([np.array([n - 1])] if n % 2 else []))
+    cols = np.concatenate([i, i + 1, i, i + 1] + ([np.array([n - 1])] if n % 2 else []))
+    vals = np.concatenate([c, -s, s, c] + ([np.array([1.0])] if n % 2 else []))
+    return CSR.from_scipy(_sp.csr_matrix((vals, (rows, cols)), shape=(n, n)))
+
+
 def random_spd_graph(n: int, degree: int, seed: int) -> CSR:
     """Weighted graph Laplacian of a random graph plus a small diagonal shift (SPD, unstructured)."""
     rng = np.random.default_rng(seed)

@@ -17,9 +17,18 @@ semismooth_newton; these need no interpolations).  One JSON line on stdout.
     python -m utopia_gb300.qp_solve --dir D [--out x.bin] [--oracle x_ref.bin] [--solver monotone_mg]
         [--n_interpolators 4] [--interp_index_offset 1] [--max_it 40] [--pre 3] [--post 3]
         [--atol 1e-9] [--stol 1e-11] [--active_set_tol 0] [--device 0]
+    python -m utopia_gb300.qp_solve --dir D --solver shifted_penalty [--use_trafo 1] [--out out.bin]
+        [--penalty_parameter 1e4] [--penalty_parameter_max 0] [--penalty_parameter_factor 1.5]
+        [--linear_rtol 1e-12] [--max_it 1000] [--stol 1e-11]
 
-The reference's QR variant (ProjectedGaussSeidelQR with the Q and R factors) and the shifted-penalty
-QP app (ShiftedPenaltyQPSolver) have no counterpart here.
+`--solver shifted_penalty` is the reference's other QP app (QPSolveApp::solve_with_shifted_penalty,
+utopia_qp_solve.cpp:61-107, registered as qp_solve): it reads `A`, `T`, `O`, `rhs`, `upper_bound` and
+`is_contact`, enforces x <= upper_bound in the transformed space O^T (T x) (`--use_trafo 0`: in x
+itself) with the shifted-penalty solver from x = 0 and writes x (default `out.bin`, as the app's
+output_path).
+
+The reference's QR variant (MGQPSolveApp with ProjectedGaussSeidelQR) is unreachable in its app:
+Problem::read keeps a local `use_QR = false`, so Q and R are never read and use_QR_mg() is false.
 """
 from __future__ import annotations
 
@@ -47,16 +56,70 @@ def rotate_system(A, rhs, x, Rot, I_fine):
     return Ar, rr, xr, Ir
 
 
+def shifted_penalty_app(a, path) -> dict:
+    """QPSolveApp::solve_with_shifted_penalty (utopia_qp_solve.cpp:61-107)."""
+    t0 = time.perf_counter()
+    ctx = U.Context(a.device)
+    A = read_matrix(ctx, path("A"))
+    T = read_matrix(ctx, path("T"))
+    O = read_matrix(ctx, path("O"))
+    rhs = read_vector(ctx, path("rhs"))
+    ub = read_vector(ctx, path("upper_bound"))
+    is_contact = read_vector(ctx, path("is_contact"))  # required by Problem::read, unused by the solve
+    n = A.nrows
+    for v, what in ((rhs, "rhs"), (ub, "upper_bound"), (is_contact, "is_contact")):
+        if len(v) != n:
+            raise ValueError(f"{what} has {len(v)} entries, A has {n} rows")
+    t_read = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    solver = U.ShiftedPenaltyQPSolver(ctx, max_it=a.max_it if a.max_it is not None else 1000, stol=a.stol,
+                                      penalty_parameter=a.penalty_parameter,
+                                      penalty_parameter_max=a.penalty_parameter_max,
+                                      penalty_parameter_factor=a.penalty_parameter_factor,
+                                      linear_rtol=a.linear_rtol)
+    if a.use_trafo:
+        solver.set_transform(T, O)
+    solver.set_box_constraints(None, ub)
+    x = U.Vector(ctx, n=n)
+    solver.solve(A, rhs, x)
+    ctx.synchronize()
+    t_solve = time.perf_counter() - t1
+    st = solver.solution_status()
+    xh = x.numpy()
+    w = x
+    if a.use_trafo:  # the constrained quantity O^T (T x)
+        t = U.Vector(ctx, n=n)
+        T.apply(x, t)
+        w = U.Vector(ctx, n=n)
+        O.transpose().apply(t, w)
+    out = {"app": "qp_solve", "solver": "shifted_penalty", "n": n, "nnz": A.nnz, "converged": bool(st["converged"]),
+           "iterations": int(st["iterates"]), "inner_iterations": int(st["spmv_count"]),
+           "violation": float(max(0.0, (w.numpy() - ub.numpy()).max(initial=0.0))),
+           "read_s": t_read, "solve_s": t_solve}
+    if a.oracle:
+        xo = read_vector(ctx, a.oracle).numpy()
+        out["error_vs_oracle"] = float(np.linalg.norm(xh - xo) / max(np.linalg.norm(xo), 1e-300))
+    dest = a.out or "out.bin"
+    (x.write_raw if dest.endswith(".raw") else x.write_petsc)(dest)
+    print(json.dumps(out), flush=True)
+    return out
+
+
 def main(argv=None) -> dict:
     ap = argparse.ArgumentParser(prog="qp_solve", description=__doc__.split("\n")[0])
     ap.add_argument("--dir", required=True)
-    for name in ("A", "rhs", "x", "Rot", "lb", "ub", "I"):
+    for name in ("A", "rhs", "x", "Rot", "lb", "ub", "I", "T", "O", "upper_bound", "is_contact"):
         ap.add_argument("--" + name, default="", help=f"path of {name} (default: <dir>/{name})")
     ap.add_argument("--n_interpolators", type=int, default=4)
     ap.add_argument("--interp_index_offset", type=int, default=1)
     ap.add_argument("--solver", default="monotone_mg",
-                    choices=["monotone_mg", "mprgp", "pgs", "semismooth_newton"])
-    ap.add_argument("--max_it", type=int, default=40)
+                    choices=["monotone_mg", "mprgp", "pgs", "semismooth_newton", "shifted_penalty"])
+    ap.add_argument("--use_trafo", type=int, default=1, help="shifted_penalty: constrain O^T (T x)")
+    ap.add_argument("--penalty_parameter", type=float, default=1e4)
+    ap.add_argument("--penalty_parameter_max", type=float, default=0.0, help="0: = penalty_parameter")
+    ap.add_argument("--penalty_parameter_factor", type=float, default=1.5)
+    ap.add_argument("--linear_rtol", type=float, default=1e-12)
+    ap.add_argument("--max_it", type=int, default=None, help="40 (shifted_penalty: 1000)")
     ap.add_argument("--pre", type=int, default=3)
     ap.add_argument("--post", type=int, default=3)
     ap.add_argument("--smoother", default="chebyshev", choices=list(U.SMOOTHERS))
@@ -71,6 +134,10 @@ def main(argv=None) -> dict:
     def path(name):
         return getattr(a, name) or os.path.join(a.dir, name)
 
+    if a.solver == "shifted_penalty":
+        return shifted_penalty_app(a, path)
+    if a.max_it is None:
+        a.max_it = 40
     t0 = time.perf_counter()
     ctx = U.Context(a.device)
     A = read_matrix(ctx, path("A"))
