@@ -233,7 +233,9 @@ def test_shifted_penalty_reference_test_problem(ctx, oracle):
 @pytest.mark.parametrize("variant", ["plain", "selection_scaling", "transformation"])
 def test_shifted_penalty_matches_oracle(ctx, oracle, variant):
     """128^2 Laplacian with an upper bound (contact under a load), plain, with a 0/1 selection and a
-    diagonal scaling matrix, and with the qp_solve app's transformation (T, O block rotations):
+    diagonal scaling matrix, and with the qp_solve app's transformation (T block rotations, O block
+    reflections: the reference maps the Hessian by T^T O^T D O T and directions by T^T O, which agree
+    for a symmetric O):
     same iterations and reason as the oracle (pinned bit for bit to the reference's solver), x to
     1e-9, and in the plain case the MPRGP minimiser to 1e-6."""
     N = 128
@@ -249,13 +251,18 @@ def test_shifted_penalty_matches_oracle(ctx, oracle, variant):
         import scipy.sparse as sp
         kw["S"] = P.CSR.from_scipy(sp.diags(rng.uniform(0.5, 2.0, n)).tocsr())
     if variant == "transformation":
-        kw["T"], kw["O"] = P.block_rotation(n, 5), P.block_rotation(n, 7)
+        kw["T"], kw["O"] = P.block_rotation(n, 5), P.block_rotation(n, 7, reflection=True)
     okw = {k: (oracle.Matrix(v) if isinstance(v, P.CSR) else v) for k, v in kw.items()}
     xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, max_it=300, **okw)
     xg, st, _, _ = _penalty_gpu(ctx, A, b, max_it=300, **kw)
     assert so["converged"] and st["converged"]
     assert st["iterates"] == so["iterates"] and st["reason"] == so["reason"]
     assert np.linalg.norm(xg - xo) <= 1e-9 * np.linalg.norm(xo)
+    w = xg
+    if variant == "transformation":
+        w = kw["O"].to_scipy().T @ (kw["T"].to_scipy() @ xg)
+    sel = kw["selection"] != 0 if "selection" in kw else np.ones(n, bool)
+    assert (w - cap)[sel].max() <= 1e-12 and (w >= cap - 1e-9).sum() > 100  # a real contact set
     if variant == "plain":
         Am = oracle.Matrix(A)
         xm, sm = oracle.mprgp_solve(Am, b, np.full(n, -np.finfo(float).max), cap, atol=1e-12, max_it=50000)
@@ -287,7 +294,7 @@ def test_shifted_penalty_warm_shift_and_linear_solver_slot(ctx, oracle):
     b = -b
     n = A.nrows
     cap = np.full(n, 0.02)
-    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7, reflection=True)
     To, Oo = oracle.Matrix(T), oracle.Matrix(O)
     x1, s1, shift = oracle.penalty_solve(oracle.Matrix(A), b, ub=cap, T=To, O=Oo, max_it=200)
     xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, x0=x1, ub=cap, T=To, O=Oo, shift=shift, max_it=200)
@@ -322,7 +329,7 @@ def test_qp_solve_shifted_penalty_app(ctx, oracle, tmp_path):
     b = -b
     n = A.nrows
     cap = np.full(n, 0.02)
-    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7, reflection=True)
     for name, m in (("A", A), ("T", T), ("O", O)):
         U.SparseMatrix(ctx, m).write_petsc(str(tmp_path / name))
     for name, v in (("rhs", b), ("upper_bound", cap), ("is_contact", np.ones(n))):
@@ -332,6 +339,6 @@ def test_qp_solve_shifted_penalty_app(ctx, oracle, tmp_path):
     xo, so, _ = oracle.penalty_solve(oracle.Matrix(A), b, ub=cap, T=oracle.Matrix(T), O=oracle.Matrix(O),
                                      max_it=200)
     assert out["converged"] and so["converged"] and out["iterations"] == so["iterates"]
-    assert out["violation"] <= 1e-8
+    assert out["violation"] <= 1e-12
     x = U.read_petsc_vector(ctx, str(tmp_path / "out.bin")).numpy()
     assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)

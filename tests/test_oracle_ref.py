@@ -127,7 +127,7 @@ def _penalty_cases():
     sel = (rng.uniform(size=n) < 0.8).astype(float)
     S = P.CSR.from_scipy(__import__("scipy.sparse", fromlist=["diags"]).diags(rng.uniform(0.5, 2.0, n)).tocsr())
     cap = np.full(n, 0.02)
-    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7)
+    T, O = P.block_rotation(n, 5), P.block_rotation(n, 7, reflection=True)
     A1, b1, ub1 = P.qp_test_problem_1d(20)
     return {
         "qp_test_problem_1d": (A1, b1, dict(ub=ub1, max_it=800)),
@@ -155,6 +155,10 @@ def test_shifted_penalty(oracle, R, case):
     xr, sr = R.penalty_solve(R.Matrix(A), b, **mats(R.Matrix))
     assert so["iterates"] == sr["iterates"] and so["reason"] == sr["reason"] and so["converged"]
     assert same(xo, xr)
+    w = xo if "T" not in kw else kw["O"].to_scipy().T @ (kw["T"].to_scipy() @ xo)
+    if "ub" in kw:  # the constraint holds where it is selected
+        sel = kw["selection"] != 0 if "selection" in kw else np.ones(w.size, bool)
+        assert (w - kw["ub"])[sel].max() <= 1e-10
 
 
 def test_shifted_penalty_keeps_its_shift(oracle, R):

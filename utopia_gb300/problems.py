@@ -389,16 +389,18 @@ def qp_test_problem_1d(n: int = 20):
     return CSR.from_scipy(A), b, np.full(n, 30.0)
 
 
-def block_rotation(n: int, seed: int) -> CSR:
-    """An orthogonal sparse matrix: independent 2 x 2 rotations of the pairs (2k, 2k+1) by random
-    angles (the last row the identity when n is odd) -- a stand-in for a contact rotation."""
+def block_rotation(n: int, seed: int, reflection: bool = False) -> CSR:
+    """An orthogonal sparse matrix: independent 2 x 2 rotations [[c, -s], [s, c]] of the pairs
+    (2k, 2k+1) by random angles, or with reflection=True the symmetric reflections
+    [[c, s], [s, -c]] (the last row the identity when n is odd) -- stand-ins for a contact basis."""
     rng = np.random.default_rng(seed)
     th = rng.uniform(0.0, 2.0 * np.pi, n // 2)
     c, s = np.cos(th), np.sin(th)
     i = np.arange(n // 2) * 2
     rows = np.concatenate([i, i, i + 1, i + 1] + ([np.array([n - 1])] if n % 2 else []))
     cols = np.concatenate([i, i + 1, i, i + 1] + ([np.array([n - 1])] if n % 2 else []))
-    vals = np.concatenate([c, -s, s, c] + ([np.array([1.0])] if n % 2 else []))
+    blocks = [c, s, s, -c] if reflection else [c, -s, s, c]
+    vals = np.concatenate(blocks + ([np.array([1.0])] if n % 2 else []))
     return CSR.from_scipy(_sp.csr_matrix((vals, (rows, cols)), shape=(n, n)))
 
 
