@@ -86,14 +86,18 @@ def test_pinned_host_upload_download(ctx, offset):
 def test_fp64_fp32_conversions_match_ieee(ctx):
     """The device converts FP64 <-> FP32 with integer bit operations (round to nearest even);
     results equal numpy's IEEE conversions bit for bit, on ties, the overflow boundary, the
-    smallest normals, subnormals, signed zeros, infinities, NaNs and random magnitudes."""
+    smallest normals, subnormals (ties included), signed zeros, infinities, NaNs (with their
+    payloads) and random magnitudes."""
     rng = np.random.default_rng(7)
     one = 1.0
     edge = [0.0, -0.0, one, -one, one + 2.0**-24, one + 3 * 2.0**-24, one + 2.0**-24 + 2.0**-52,
             np.float32(3.4028235e38).astype(np.float64), 3.4028235677973366e38, 3.4028235677973362e38, 1e39,
             -1e39, 2.0**-126, 2.0**-126 * (1 - 2.0**-25), 2.0**-127, 1e-45, 1e-300, np.inf, -np.inf,
-            np.nan, 0.1, 1 / 3]
-    rnd = rng.standard_normal(20000) * 10.0 ** rng.integers(-40, 40, 20000)
+            np.nan, 0.1, 1 / 3, 2.0**-149 * 1.5, 2.0**-150, 2.0**-150 * (1 + 2.0**-52), 3 * 2.0**-150,
+            2.0**-149 * 2.5, 2.0**-126 * (1 - 2.0**-24), 2.0**-126 * (1 - 2.0**-23), 5e-324, -5e-324, 2.0**-1022,
+            2.0**-149 * 0.5000001, 2.0**-149 * 0.4999999]
+    rnd = np.concatenate([rng.standard_normal(20000) * 10.0 ** rng.integers(-40, 40, 20000),
+                          rng.uniform(-2.0**-126, 2.0**-126, 20000)])  # the float subnormal range
     d = np.array(edge + list(rnd), dtype=np.float64)
     v64, v32 = U.Vector(ctx, d), U.Vector(ctx, n=d.size, dtype=U.F32)
     v64.copy_to(v32)
@@ -102,6 +106,12 @@ def test_fp64_fp32_conversions_match_ieee(ctx):
     got = v32.numpy()
     ok = (got.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(got) & np.isnan(ref))
     assert ok.all(), d[~ok][:5]
+    # NaN payloads: the top fraction bits kept, the quiet bit set (as numpy's conversion does)
+    nan64 = np.array([0x7ff8000000000001, 0x7ff0000000000001, 0xfff8123456789abc], np.uint64).view(np.float64)
+    n64, n32 = U.Vector(ctx, nan64), U.Vector(ctx, n=3, dtype=U.F32)
+    n64.copy_to(n32)
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(n32.numpy().view(np.uint32), nan64.astype(np.float32).view(np.uint32))
     f = np.concatenate([ref, np.array([1e-40, -1e-44, 1.17549435e-38], np.float32),
                         (rng.standard_normal(20000) * 10.0 ** rng.integers(-44, 38, 20000)).astype(np.float32)])
     w32, w64 = U.Vector(ctx, f, dtype=U.F32), U.Vector(ctx, n=f.size)
@@ -109,6 +119,11 @@ def test_fp64_fp32_conversions_match_ieee(ctx):
     got64, ref64 = w64.numpy(), f.astype(np.float64)
     ok = (got64.view(np.uint64) == ref64.view(np.uint64)) | (np.isnan(got64) & np.isnan(ref64))
     assert ok.all(), f[~ok][:5]
+    nan32 = np.array([0x7fc00001, 0x7f800001, 0xffc12345], np.uint32).view(np.float32)
+    m32, m64 = U.Vector(ctx, nan32, dtype=U.F32), U.Vector(ctx, n=3)
+    m32.copy_to(m64)
+    with np.errstate(invalid="ignore"):
+        assert np.array_equal(m64.numpy().view(np.uint64), nan32.astype(np.float64).view(np.uint64))
 
 
 def test_empty_vector_dot(ctx):

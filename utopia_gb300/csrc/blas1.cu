@@ -105,8 +105,8 @@ __global__ void k_project(int64_t n, const double *lb, const double *ub, double 
 __device__ __forceinline__ double load_any(const void *p, int dt, int64_t i) {
     switch (dt) {
         case UGPU_F64: return static_cast<const double *>(p)[i];
-        case UGPU_F32: return double(static_cast<const float *>(p)[i]);
-        default: return double(__bfloat162float(static_cast<const __nv_bfloat16 *>(p)[i]));
+        case UGPU_F32: return f2d_bits(static_cast<const float *>(p)[i]);
+        default: return f2d_bits(__bfloat162float(static_cast<const __nv_bfloat16 *>(p)[i]));
     }
 }
 

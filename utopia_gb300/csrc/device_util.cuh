@@ -18,31 +18,60 @@ __device__ __forceinline__ D cvt(__nv_bfloat16 v);
 template <>
 __device__ __forceinline__ double cvt<double>(double v) { return v; }
 // Exact IEEE-754 binary32 -> binary64 and round-to-nearest-even binary64 -> binary32 by bit
-// manipulation on the integer pipe.  On GB300 the FP64 pipe (about two operations per clock
-// per SM) also executes the hardware conversions, and it bounds the FP64 vector kernels of
-// the mixed solver; zeros, subnormals, infinities and NaNs take the hardware conversion.
+// manipulation on the integer pipes, every class of input included (zeros, subnormals,
+// infinities, NaNs with their payload, quietened).  On GB300 the FP64 pipe (about two operations
+// per clock per SM) also executes the hardware conversions and bounds the FP64 vector kernels of
+// the mixed solver; a hardware fallback for the rare classes would still be issued for every
+// element once the compiler turns the branch into predicated code, so there is none.
 __device__ __forceinline__ double f2d_bits(float f) {
     const uint32_t u = __float_as_uint(f);
     const uint32_t e = (u >> 23) & 0xffu;
-    if (e - 1u < 254u) {  // normal: rebias the exponent (1023 - 127), widen the mantissa
-        const uint64_t b = (uint64_t(u & 0x80000000u) << 32) | (uint64_t(e + 896u) << 52) |
-                           (uint64_t(u & 0x7fffffu) << 29);
-        return __longlong_as_double((long long)b);
+    const uint32_t m = u & 0x7fffffu;
+    uint32_t de;   // the binary64 exponent field
+    uint64_t dm;   // the binary64 fraction field
+    if (e - 1u < 254u) {  // normal: rebias the exponent (1023 - 127), widen the fraction
+        de = e + 896u;
+        dm = uint64_t(m) << 29;
+    } else if (e == 0xffu) {  // infinity, or NaN (payload kept, quiet bit set)
+        de = 0x7ffu;
+        dm = (uint64_t(m) << 29) | (m ? (1ull << 51) : 0ull);
+    } else if (m == 0u) {  // signed zero
+        de = 0u;
+        dm = 0ull;
+    } else {  // subnormal m 2^-149 = 2^(p-149) (1 + ...), p the leading one's position
+        const uint32_t p = 31u - uint32_t(__clz(m));
+        de = p + 874u;
+        dm = (uint64_t(m) << (52u - p)) & 0xfffffffffffffull;
     }
-    return double(f);
+    return __longlong_as_double((long long)((uint64_t(u & 0x80000000u) << 32) | (uint64_t(de) << 52) | dm));
 }
 __device__ __forceinline__ float d2f_bits(double d) {
     const uint64_t b = (uint64_t)__double_as_longlong(d);
     const uint32_t e = uint32_t(b >> 52) & 0x7ffu;
+    const uint64_t m = b & 0xfffffffffffffull;
+    uint32_t r;
     if (e - 897u < 254u) {  // the result's exponent is a normal float exponent (1..254)
-        const uint64_t m = b & 0xfffffffffffffull;
-        uint32_t r = ((e - 896u) << 23) | uint32_t(m >> 29);  // truncated exponent and mantissa
-        const uint64_t rem = m & 0x1fffffffull;               // the 29 dropped bits
+        r = ((e - 896u) << 23) | uint32_t(m >> 29);  // truncated exponent and fraction
+        const uint64_t rem = m & 0x1fffffffull;      // the 29 dropped bits
         const uint64_t half = 0x10000000ull;
         r += (rem > half || (rem == half && (r & 1u))) ? 1u : 0u;  // a carry may raise the exponent (to inf)
-        return __uint_as_float((uint32_t(b >> 32) & 0x80000000u) | r);
+    } else if (e == 0x7ffu) {  // infinity, or NaN (the payload's top bits, quiet bit set)
+        r = 0x7f800000u | (m ? (0x400000u | uint32_t(m >> 29)) : 0u);
+    } else if (e >= 1151u) {  // |d| >= 2^128: overflow
+        r = 0x7f800000u;
+    } else {  // a float subnormal or zero: k = round(M 2^(e - 926)), M the 53-bit significand
+        const uint64_t M = m | (e ? (1ull << 52) : 0ull);
+        const uint32_t sh = e ? 926u - e : 925u;  // at least 30
+        if (sh >= 64u) {
+            r = 0u;
+        } else {
+            const uint64_t k = M >> sh;
+            const uint64_t rem = M & ((1ull << sh) - 1ull);
+            const uint64_t half = 1ull << (sh - 1u);
+            r = uint32_t(k) + ((rem > half || (rem == half && (k & 1ull))) ? 1u : 0u);
+        }
     }
-    return float(d);
+    return __uint_as_float((uint32_t(b >> 32) & 0x80000000u) | r);
 }
 
 template <>
@@ -56,7 +85,7 @@ __device__ __forceinline__ float cvt<float>(float v) { return v; }
 template <>
 __device__ __forceinline__ __nv_bfloat16 cvt<__nv_bfloat16>(float v) { return __float2bfloat16(v); }
 template <>
-__device__ __forceinline__ double cvt<double>(__nv_bfloat16 v) { return double(__bfloat162float(v)); }
+__device__ __forceinline__ double cvt<double>(__nv_bfloat16 v) { return f2d_bits(__bfloat162float(v)); }
 template <>
 __device__ __forceinline__ float cvt<float>(__nv_bfloat16 v) { return __bfloat162float(v); }
 template <>
