@@ -11,6 +11,7 @@
 // (1728^2 and 4096^2 doubles), instead of two latency-bound triangular sweeps.
 // GB300's FP64 tensor rate is no higher than its FP64 FMA rate, so the set-up uses
 // FP64 FMA tiles.
+#include <functional>
 #include <cmath>
 
 #include "abi_util.cuh"
@@ -155,6 +156,14 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
         }
 }
 
+// A[i][j] = A[j][i] for j > i (the strictly upper triangle from the lower one)
+__global__ void k_mirror_lower(double *A, int64_t n) {
+    for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < n * n; e += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t i = e / n, j = e % n;
+        if (j > i) A[e] = A[j * n + i];
+    }
+}
+
 __global__ void k_zero(double *p, int64_t m) {
     for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m; i += int64_t(gridDim.x) * blockDim.x)
         p[i] = 0.0;
@@ -268,30 +277,42 @@ bool DenseCholesky::factor(const Mat &A) {
     UGPU_CUDA(cudaMemcpyAsync(&hbad, bad.ptr, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     UGPU_CUDA(cudaStreamSynchronize(c.stream));
     if (hbad) return false;
-    // Y = L^-1, block row by block row: Y[bi, 0:r0] = -L_ii^-1 (L[bi, 0:r0] Y[0:r0, 0:r0]); Y_ii = L_ii^-1
+    // Y = L^-1 by recursive halving: inv([[L11, 0], [L21, L22]]) = [[Y11, 0], [-Y22 L21 Y11, Y22]], halves
+    // split at multiples of NB down to the diagonal blocks, whose inverses the factorisation kept.
+    // Every product is a GEMM of half the current size (the top two are n/2 x n/2 x n/2), so the
+    // grid stays full where a block-row sweep (kb x r0 x r0 products) left most SMs idle.
     k_zero<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Y, n * n);
     c.launches++;
-    for (int64_t r0 = 0; r0 < n; r0 += NB) {
-        const int kb = int(std::min<int64_t>(NB, n - r0));
-        const double *Lb = Lip + (r0 / NB) * NB * NB;
-        if (r0 > 0) {
-            dim3 grid(unsigned((r0 + 63) / 64), unsigned((kb + 63) / 64));
-            // T = L[r0:r0+kb, 0:r0] Y[0:r0, 0:r0]  (kb x r0, leading dimension r0)
-            k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(kb, int(r0), int(r0), 1.0, Lp + r0 * n, n, Y, n, 0.0,
-                                                              Tp, r0, false);
-            // Y[r0:r0+kb, 0:r0] = -L_bb^-1 T
-            k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(kb, int(r0), kb, -1.0, Lb, NB, Tp, r0, 0.0, Y + r0 * n,
-                                                              n, false);
-            c.launches += 2;
+    Buffer W;
+    W.alloc(sizeof(double) * size_t(std::max<int64_t>((n / 2 + NB) * (n / 2 + NB), 1)));
+    double *Wp = W.as<double>();
+    std::function<void(int64_t, int64_t)> tri_inv = [&](int64_t r0, int64_t m) {
+        if (m <= NB) {  // one diagonal block (r0 is a multiple of NB)
+            copy_block(Lip + (r0 / NB) * NB * NB, NB, Y + r0 * n + r0, n, int(m), int(m));
+            return;
         }
-        copy_block(Lb, NB, Y + r0 * n + r0, n, kb, kb);
+        const int64_t h = ((m / 2 + NB - 1) / NB) * NB;  // 0 < h < m, a multiple of NB
+        tri_inv(r0, h);
+        tri_inv(r0 + h, m - h);
+        const int64_t m2 = m - h;
+        dim3 grid(unsigned((h + 63) / 64), unsigned((m2 + 63) / 64));
+        // W = L21 Y11  (m2 x h, leading dimension h)
+        k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(int(m2), int(h), int(h), 1.0, Lp + (r0 + h) * n + r0, n,
+                                                          Y + r0 * n + r0, n, 0.0, Wp, h, false);
+        // Y21 = -Y22 W
+        k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(int(m2), int(h), int(m2), -1.0, Y + (r0 + h) * n + r0 + h,
+                                                          n, Wp, h, 0.0, Y + (r0 + h) * n + r0, n, false);
+        c.launches += 2;
         UGPU_LAUNCH_CHECK();
-    }
-    // Ainv = Y^T Y  (stored in L's buffer, then swapped)
+    };
+    tri_inv(0, n);
+    // Ainv = Y^T Y (stored in L's buffer, then swapped): the lower triangle's tiles, then mirrored
+    // (the product is symmetric bit for bit: (i, j) and (j, i) sum the same products in one order)
     {
         dim3 grid(unsigned((n + 63) / 64), unsigned((n + 63) / 64));
-        k_dgemm<true, false><<<grid, 256, 0, c.stream>>>(int(n), int(n), int(n), 1.0, Y, n, Y, n, 0.0, Lp, n, false);
-        c.launches++;
+        k_dgemm<true, false><<<grid, 256, 0, c.stream>>>(int(n), int(n), int(n), 1.0, Y, n, Y, n, 0.0, Lp, n, true);
+        k_mirror_lower<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Lp, n);
+        c.launches += 2;
         UGPU_LAUNCH_CHECK();
     }
     std::swap(L, Ainv);  // Ainv now holds the inverse; L holds L^-1 (kept for diagnostics)

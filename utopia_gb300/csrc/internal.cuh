@@ -315,8 +315,8 @@ void launch_spmv(Context &ctx, const Mat &A, const SpmvArgs &a);
 // what a numeric-only SpGEMM of the same structure needs: per-row product bounds, the rows
 // beyond the warp tiers
 struct SpgemmPlan {
-    Buffer ub, big;
-    int h_nbig = 0;
+    Buffer ub, big, over;  // row bounds, rows beyond the warp tiers, the mid tier's overflow rows
+    int h_nbig = 0, h_nover = 0;
     unsigned long long max_ub = 0;
 };
 // finalize = false: CSR arrays only (no SpMV layout), for intermediates that only feed products

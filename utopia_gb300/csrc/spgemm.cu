@@ -287,6 +287,140 @@ __global__ void __launch_bounds__(WARPS * 32) k_spgemm_warp(int64_t m, int64_t l
     }
 }
 
+// The mid tier: rows of 129..1024 products whose distinct columns number at most 128 (a
+// Galerkin row has a few hundred products landing on a few dozen columns).  Sized by the
+// distinct count, a warp's table is 256 slots and its compaction buffer 128 entries (4.5 KB, 48
+// warps per SM) where sizing by the product count took 36 KB per warp (4 warps per SM).  The
+// symbolic pass tries every such row at that size and sends the rows that exceed 128 distinct
+// columns to a list for the full-size tier; the numeric pass picks the tier by the row's length.
+constexpr int kMidTable = 256, kMidCap = 128, kMidWarps = 8;
+constexpr size_t kMidSmem = (sizeof(int32_t) + sizeof(double)) * size_t(kMidTable + kMidCap) * kMidWarps;
+
+// hash_insert with a bounded probe sequence: -1 when the table is full
+__device__ __forceinline__ int hash_insert_bounded(int32_t *keys, int mask, int32_t c, int *n_unique) {
+    volatile int32_t *vk = keys;
+    uint32_t h = hash_col(c, mask);
+    for (int p = 0; p <= mask; ++p) {
+        const int32_t k = vk[h];
+        if (k == c) return int(h);
+        if (k == -1) {
+            const int32_t old = atomicCAS(&keys[h], -1, c);
+            if (old == -1) {
+                atomicAdd(n_unique, 1);
+                return int(h);
+            }
+            if (old == c) return int(h);
+        }
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// distinct columns of row i of A B with one warp and a table of TS slots, or -1 past cap
+__device__ int row_count_capped(int64_t i, int lane, int TS, int cap, int32_t *keys, int *s_count, int *s_over,
+                                const int32_t *arp, const int32_t *aci, const int32_t *brp, const int32_t *bci) {
+    const int mask = TS - 1;
+    for (int t = lane; t < TS; t += 32) keys[t] = -1;
+    if (lane == 0) {
+        *s_count = 0;
+        *s_over = 0;
+    }
+    __syncwarp();
+    bool over = false;
+    for (int32_t ka = arp[i]; ka < arp[i + 1] && !over; ++ka) {
+        const int32_t j = aci[ka];
+        const int32_t b1 = brp[j + 1];
+        for (int32_t kb = brp[j] + lane; kb < b1; kb += 32) {
+            if (*reinterpret_cast<volatile int *>(s_count) > cap) break;
+            if (hash_insert_bounded(keys, mask, bci[kb], s_count) < 0) {
+                *s_over = 1;
+                break;
+            }
+        }
+        __syncwarp();
+        over = *reinterpret_cast<volatile int *>(s_count) > cap || *reinterpret_cast<volatile int *>(s_over) != 0;
+        __syncwarp();  // every lane reads before any lane inserts again: `over` is warp-uniform
+    }
+    const int c = *reinterpret_cast<volatile int *>(s_count);
+    __syncwarp();
+    return over ? -1 : c;
+}
+
+// symbolic mid tier: rows with kTier1Ub < ub <= kWarpRowsUb counted at the small size; those past
+// kMidCap distinct columns go to over[], rows beyond kWarpRowsUb products to big[] (for the CTA kernels)
+__global__ void __launch_bounds__(kMidWarps * 32) k_spgemm_mid_sym(int64_t m, const int64_t *ub, const int32_t *arp,
+                                                                 const int32_t *aci, const int32_t *brp,
+                                                                 const int32_t *bci, int64_t *cnt, int *over,
+                                                                 int *n_over, int *big, int *n_big) {
+    __shared__ int32_t s_keys[kMidWarps][kMidTable];
+    __shared__ int s_count[kMidWarps], s_over[kMidWarps];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int64_t nw = int64_t(gridDim.x) * kMidWarps;
+    for (int64_t i = int64_t(blockIdx.x) * kMidWarps + w; i < m; i += nw) {
+        const int64_t u = ub[i];
+        if (u <= kTier1Ub) continue;
+        if (u > kWarpRowsUb) {
+            if (lane == 0) big[atomicAdd(n_big, 1)] = int(i);
+            continue;
+        }
+        const int c = row_count_capped(i, lane, kMidTable, kMidCap, s_keys[w], &s_count[w], &s_over[w], arp, aci,
+                                       brp, bci);
+        if (lane == 0) {
+            if (c >= 0) cnt[i] = c;
+            else over[atomicAdd(n_over, 1)] = int(i);
+        }
+    }
+}
+
+// numeric mid tier: rows with kTier1Ub < ub <= kWarpRowsUb and at most kMidCap entries
+template <class V>
+__global__ void __launch_bounds__(kMidWarps * 32) k_spgemm_mid_num(int64_t m, const int64_t *ub, const int32_t *arp,
+                                                                 const int32_t *aci, const V *acv,
+                                                                 const int32_t *brp, const int32_t *bci,
+                                                                 const V *bcv, const int32_t *crp, int32_t *cci,
+                                                                 V *ccv) {
+    extern __shared__ unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *vals = reinterpret_cast<double *>(smem) + size_t(w) * kMidTable;
+    double *lvals = reinterpret_cast<double *>(smem) + size_t(kMidWarps) * kMidTable + size_t(w) * kMidCap;
+    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (kMidTable + kMidCap) * kMidWarps);
+    int32_t *keys = ibase + size_t(w) * kMidTable;
+    int32_t *lkeys = ibase + size_t(kMidWarps) * kMidTable + size_t(w) * kMidCap;
+    __shared__ int s_count[kMidWarps];
+    const int64_t nw = int64_t(gridDim.x) * kMidWarps;
+    for (int64_t i = int64_t(blockIdx.x) * kMidWarps + w; i < m; i += nw) {
+        const int64_t u = ub[i];
+        const int nz = crp[i + 1] - crp[i];
+        if (u <= kTier1Ub || u > kWarpRowsUb || nz > kMidCap) continue;
+        row_product<V, true, false>(i, lane, 32, table_size(nz, kMidTable), keys, vals, lkeys, lvals, &s_count[w],
+                                    arp, aci, acv, brp, bci, bcv, nullptr, crp, cci, ccv);
+    }
+}
+
+// the full-size warp tier over a list of rows (the mid tier's overflow)
+template <class V, bool NUMERIC>
+__global__ void __launch_bounds__(kWarpsPerCta * 32) k_spgemm_warp_list(const int *rows, int nrows, const int64_t *ub,
+                                                                       const int32_t *arp, const int32_t *aci,
+                                                                       const V *acv, const int32_t *brp,
+                                                                       const int32_t *bci, const V *bcv,
+                                                                       int64_t *cnt, const int32_t *crp,
+                                                                       int32_t *cci, V *ccv) {
+    extern __shared__ unsigned char smem[];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    double *vals = reinterpret_cast<double *>(smem) + size_t(w) * kWarpTable;
+    double *lvals = reinterpret_cast<double *>(smem) + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
+    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta);
+    int32_t *keys = ibase + size_t(w) * kWarpTable;
+    int32_t *lkeys = ibase + size_t(kWarpsPerCta) * kWarpTable + size_t(w) * kWarpRowsUb;
+    __shared__ int s_count[kWarpsPerCta];
+    const int nw = gridDim.x * kWarpsPerCta;
+    for (int b = blockIdx.x * kWarpsPerCta + w; b < nrows; b += nw) {
+        const int64_t i = rows[b];
+        row_product<V, NUMERIC, false>(i, lane, 32, table_size(ub[i], kWarpTable), keys, vals, lkeys, lvals,
+                                       &s_count[w], arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    }
+}
+
 template <class V, bool NUMERIC>
 __global__ void __launch_bounds__(kCtaThreads) k_spgemm_cta(const int *big_rows, int n_big, const int64_t *ub,
                                                             const int32_t *arp, const int32_t *aci, const V *acv,
@@ -494,6 +628,10 @@ void spgemm_set_attributes() {
         UGPU_CUDA(cudaFuncSetAttribute(
             k_spgemm_warp<double, true, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>,
             cudaFuncAttributeMaxDynamicSharedMemorySize, int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp_list<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(warp_smem)));
+        UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_warp_list<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(warp_smem)));
         UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        int(cta_smem)));
         UGPU_CUDA(cudaFuncSetAttribute(k_spgemm_cta<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -508,9 +646,12 @@ void spgemm_set_attributes() {
 
 // the warp tiers (rows up to kWarpRowsUb products); tiers above the largest row are skipped.
 // Symbolic (N = false): row counts into cnt, rows beyond the warp tiers listed in big/nbig.
+// Symbolic: the mid tier's overflow rows go to over[] (count in *nover on the device, returned in
+// *h_nover_out); numeric: the list from the symbolic pass (h_nover_in rows).
 template <bool N>
 void launch_warp_tiers(Context &ctx, const Mat &A, const Mat &B, unsigned long long max_ub, const int64_t *ub,
-                       int64_t *cnt, const int32_t *crp, int32_t *cci, double *ccv, int *big, int *nbig) {
+                       int64_t *cnt, const int32_t *crp, int32_t *cci, double *ccv, int *big, int *nbig, int *over,
+                       int *nover, int h_nover_in, int *h_nover_out) {
     const int64_t m = A.nrows;
     if (!m) return;
     const int32_t *arp = A.rowptr.as<int32_t>(), *aci = A.colidx.as<int32_t>();
@@ -530,10 +671,29 @@ void launch_warp_tiers(Context &ctx, const Mat &A, const Mat &B, unsigned long l
         ctx.launches++;
     }
     if (max_ub > (unsigned long long)kTier1Ub) {
-        k_spgemm_warp<double, N, kWarpTable, kWarpRowsUb, kWarpsPerCta, true>
-            <<<grid(kWarpsPerCta, 16), kWarpsPerCta * 32, kWarpSmem, ctx.stream>>>(
-                m, kTier1Ub, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, big, nbig);
+        if constexpr (!N) {
+            k_spgemm_mid_sym<<<grid(kMidWarps, 6), kMidWarps * 32, 0, ctx.stream>>>(m, ub, arp, aci, brp, bci, cnt,
+                                                                                   over, nover, big, nbig);
+        } else {
+            k_spgemm_mid_num<double><<<grid(kMidWarps, 6), kMidWarps * 32, kMidSmem, ctx.stream>>>(
+                m, ub, arp, aci, acv, brp, bci, bcv, crp, cci, ccv);
+        }
         ctx.launches++;
+        UGPU_LAUNCH_CHECK();
+        // the mid tier's overflow rows at the full warp-table size
+        int h_nover = h_nover_in;
+        if constexpr (!N) {
+            UGPU_CUDA(cudaMemcpyAsync(&h_nover, nover, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
+            UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
+            *h_nover_out = h_nover;
+        }
+        if (h_nover > 0) {
+            k_spgemm_warp_list<double, N><<<std::max(1, std::min((h_nover + kWarpsPerCta - 1) / kWarpsPerCta,
+                                                                 ctx.sms * 16)),
+                                            kWarpsPerCta * 32, kWarpSmem, ctx.stream>>>(
+                over, h_nover, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+            ctx.launches++;
+        }
     }
     UGPU_LAUNCH_CHECK();
 }
@@ -565,8 +725,11 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPla
     UGPU_CHECK(A.ncols == B.nrows, UGPU_ERR_ARG, "spgemm: inner dimensions differ");
     UGPU_CHECK(A.vdtype == UGPU_F64 && B.vdtype == UGPU_F64, UGPU_ERR_UNSUPPORTED, "spgemm: FP64 operands");
     const int64_t m = A.nrows;
-    Buffer ub, cnt, crp64, big, nbig;
+    Buffer ub, cnt, crp64, big, nbig, over, nover;
     ub.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
+    over.alloc(sizeof(int) * std::max<int64_t>(m, 1));
+    nover.alloc(sizeof(int));
+    UGPU_CUDA(cudaMemsetAsync(nover.ptr, 0, sizeof(int), ctx.stream));
     cnt.alloc(sizeof(int64_t) * std::max<int64_t>(m, 1));
     crp64.alloc(sizeof(int64_t) * (m + 1));
     big.alloc(sizeof(int) * std::max<int64_t>(m, 1));
@@ -587,8 +750,9 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPla
         UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
     }
     // symbolic
+    int h_nover = 0;
     launch_warp_tiers<false>(ctx, A, B, max_ub, ub.as<int64_t>(), cnt.as<int64_t>(), nullptr, nullptr, nullptr,
-                             big.as<int>(), nbig.as<int>());
+                             big.as<int>(), nbig.as<int>(), over.as<int>(), nover.as<int>(), 0, &h_nover);
     int h_nbig = 0;
     UGPU_CUDA(cudaMemcpyAsync(&h_nbig, nbig.ptr, sizeof(int), cudaMemcpyDeviceToHost, ctx.stream));
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -603,7 +767,8 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPla
     UGPU_LAUNCH_CHECK();
     // numeric
     launch_warp_tiers<true>(ctx, A, B, max_ub, ub.as<int64_t>(), nullptr, C->rowptr.as<int32_t>(),
-                            C->colidx.as<int32_t>(), C->vals.as<double>(), nullptr, nullptr);
+                            C->colidx.as<int32_t>(), C->vals.as<double>(), nullptr, nullptr, over.as<int>(), nullptr,
+                            h_nover, nullptr);
     launch_big_rows<true>(ctx, A, B, max_ub, ub.as<int64_t>(), big.as<int>(), h_nbig, nullptr,
                           C->rowptr.as<int32_t>(), C->colidx.as<int32_t>(), C->vals.as<double>());
     UGPU_CUDA(cudaStreamSynchronize(ctx.stream));
@@ -611,6 +776,8 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPla
         plan->ub = std::move(ub);
         plan->big = std::move(big);
         plan->h_nbig = h_nbig;
+        plan->over = std::move(over);
+        plan->h_nover = h_nover;
         plan->max_ub = max_ub;
     }
     if (finalize) finalize_matrix(*C);
@@ -621,7 +788,8 @@ std::unique_ptr<Mat> spgemm(const Mat &A, const Mat &B, bool finalize, SpgemmPla
 void spgemm_numeric(const Mat &A, const Mat &B, Mat &C, const SpgemmPlan &plan) {
     Context &ctx = *A.ctx;
     launch_warp_tiers<true>(ctx, A, B, plan.max_ub, plan.ub.as<int64_t>(), nullptr, C.rowptr.as<int32_t>(),
-                            C.colidx.as<int32_t>(), C.vals.as<double>(), nullptr, nullptr);
+                            C.colidx.as<int32_t>(), C.vals.as<double>(), nullptr, nullptr,
+                            const_cast<int *>(plan.over.as<int>()), nullptr, plan.h_nover, nullptr);
     launch_big_rows<true>(ctx, A, B, plan.max_ub, plan.ub.as<int64_t>(), plan.big.as<int>(), plan.h_nbig, nullptr,
                           C.rowptr.as<int32_t>(), C.colidx.as<int32_t>(), C.vals.as<double>());
 }

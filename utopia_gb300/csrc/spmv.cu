@@ -71,35 +71,72 @@ constexpr int kAnalyzeThreads = 128;
 // slots as that shape has entries.
 constexpr int kAnchoredTag = 1 << 16;
 
-// Sorted distinct keys of a slice by repeated min-extraction; returns the count, or -1 if
-// more than kMaxDiagSlots (or a key outside int32).  ANCH: key = col - first column.
+// Sorted distinct keys of a slice; returns the count, or -1 if more than kMaxDiagSlots (or a key
+// outside int32).  ANCH: key = col - first column, else col - row.  The keys go into a shared-memory
+// hash set (256 slots: inserts stop counting past kMaxDiagSlots, and at most one insert per thread
+// is in flight beyond that, so the set never fills), then each distinct key is placed by its rank.
+// One pass over the slice's entries, where extracting the minimum key by key took one pass per key.
+constexpr int kKeySlots = 256;
+static_assert(kKeySlots >= kMaxDiagSlots + kAnalyzeThreads, "key set too small");
 template <bool ANCH>
-__device__ int slice_keys(const int32_t *rp, const int32_t *ci, int64_t r0, int64_t r1, int32_t *out,
-                          long long *s_min) {
-    int nd = 0;
-    long long prev = LLONG_MIN;
-    while (true) {
-        if (threadIdx.x == 0) *s_min = LLONG_MAX;
-        __syncthreads();
-        long long m = LLONG_MAX;
-        for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-            const int32_t k0 = rp[r], k1 = rp[r + 1];
-            const long long base = ANCH ? (k1 > k0 ? (long long)ci[k0] : 0ll) : r;
-            for (int32_t k = k0; k < k1; ++k) {
-                long long off = (long long)ci[k] - base;
-                if (off > prev && off < m) m = off;
-            }
-        }
-        atomicMin(s_min, m);
-        __syncthreads();
-        long long mm = *s_min;
-        __syncthreads();
-        if (mm == LLONG_MAX) return nd;
-        if (nd >= kMaxDiagSlots || mm > INT_MAX || mm < INT_MIN) return -1;
-        if (threadIdx.x == 0) out[nd] = int32_t(mm);
-        nd++;
-        prev = mm;
+__device__ int slice_keys(const int32_t *rp, const int32_t *ci, int64_t r0, int64_t r1, int32_t *out) {
+    __shared__ long long s_tab[kKeySlots];
+    __shared__ long long s_key[kMaxDiagSlots];
+    __shared__ int s_cnt, s_bad;
+    const long long kEmpty = LLONG_MAX;
+    for (int i = threadIdx.x; i < kKeySlots; i += blockDim.x) s_tab[i] = kEmpty;
+    if (threadIdx.x == 0) {
+        s_cnt = 0;
+        s_bad = 0;
     }
+    __syncthreads();
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const int32_t k0 = rp[r], k1 = rp[r + 1];
+        const long long base = ANCH ? (k1 > k0 ? (long long)ci[k0] : 0ll) : r;
+        for (int32_t k = k0; k < k1; ++k) {
+            if (*reinterpret_cast<volatile int *>(&s_bad) || *reinterpret_cast<volatile int *>(&s_cnt) > kMaxDiagSlots)
+                break;
+            const long long off = (long long)ci[k] - base;
+            if (off > INT_MAX || off < INT_MIN) {
+                s_bad = 1;
+                break;
+            }
+            unsigned h = (unsigned(off) * 2654435761u) >> 24;  // 8-bit slot index
+            bool placed = false;
+            for (int probe = 0; probe < kKeySlots && !placed; ++probe) {
+                const long long prev = (long long)atomicCAS(reinterpret_cast<unsigned long long *>(&s_tab[h]),
+                                                            (unsigned long long)kEmpty, (unsigned long long)off);
+                if (prev == kEmpty) {  // a new key
+                    if (atomicAdd(&s_cnt, 1) >= kMaxDiagSlots) s_bad = 1;
+                    placed = true;
+                } else if (prev == off) {
+                    placed = true;
+                } else {
+                    h = (h + 1) & (kKeySlots - 1);
+                }
+            }
+            if (!placed) s_bad = 1;  // a full set (excluded by its size; the loop stays bounded)
+        }
+    }
+    __syncthreads();
+    const int bad = s_bad;
+    const int nd = s_cnt;
+    __syncthreads();
+    if (bad) return -1;
+    // compact, then place each key by its rank (keys are distinct)
+    if (threadIdx.x == 0) s_cnt = 0;
+    __syncthreads();
+    for (int i = threadIdx.x; i < kKeySlots; i += blockDim.x)
+        if (s_tab[i] != kEmpty) s_key[atomicAdd(&s_cnt, 1)] = s_tab[i];
+    __syncthreads();
+    for (int t = threadIdx.x; t < nd; t += blockDim.x) {
+        const long long k = s_key[t];
+        int rank = 0;
+        for (int u = 0; u < nd; ++u) rank += s_key[u] < k ? 1 : 0;
+        out[rank] = int32_t(k);
+    }
+    __syncthreads();
+    return nd;
 }
 
 // per slice: kind and width (the cheapest of the three layouts in bytes)
@@ -107,7 +144,6 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_analyze(const int32_t 
                                                                    int S, int64_t nslices, int sval,
                                                                    int32_t *width, int32_t *offs_tmp) {
     __shared__ int s_maxrow;
-    __shared__ long long s_min;
     for (int64_t s = blockIdx.x; s < nslices; s += gridDim.x) {
         int64_t r0 = s * S, r1 = min(n, r0 + S);
         if (threadIdx.x == 0) s_maxrow = 0;
@@ -121,12 +157,12 @@ __global__ void __launch_bounds__(kAnalyzeThreads) k_sell_analyze(const int32_t 
         // bytes: diagonal nd*S*sval + 4nd; anchored na*S*sval + 4na + 4S + 8; explicit maxrow*S*(sval+4)
         const long long expl = (long long)maxrow * S * (sval + 4);
         int32_t *keys = offs_tmp + s * kMaxDiagSlots;
-        const int nd = maxrow <= kMaxDiagSlots ? slice_keys<false>(rp, ci, r0, r1, keys, &s_min) : -1;
+        const int nd = maxrow <= kMaxDiagSlots ? slice_keys<false>(rp, ci, r0, r1, keys) : -1;
         int kind_w = -maxrow;
         if (nd >= 0 && (long long)nd * S * sval + 4ll * nd <= expl) {
             kind_w = nd;
         } else if (maxrow <= kMaxDiagSlots) {
-            const int na = slice_keys<true>(rp, ci, r0, r1, keys, &s_min);
+            const int na = slice_keys<true>(rp, ci, r0, r1, keys);
             if (na >= 0 && (long long)na * S * sval + 4ll * na + 4ll * S + 8 < expl) kind_w = kAnchoredTag + na;
         }
         if (threadIdx.x == 0) width[s] = kind_w;
