@@ -73,21 +73,22 @@ __global__ void __launch_bounds__(256) k_potrf_diag(double *A, int64_t n, int64_
 // inverse of the lower-triangular kb x kb diagonal block of L at (k0, k0), into Li (row-major,
 // leading dimension NB): one thread per column solves L_bb x = e_c by forward substitution
 __global__ void __launch_bounds__(NB) k_trinv_diag(const double *L, int64_t n, int64_t k0, int kb, double *Li) {
-    __shared__ double x[NB][NB + 1];
+    __shared__ double l[NB][NB + 1];  // the block of L, staged once (coalesced rows)
     const int c = threadIdx.x;
     const double *Lb = L + k0 * n + k0;
-    if (c < kb) {
-        for (int i = 0; i < c; ++i) x[i][c] = 0.0;
-        for (int i = c; i < kb; ++i) {
-            double s = (i == c) ? 1.0 : 0.0;
-            for (int q = c; q < i; ++q) s -= Lb[int64_t(i) * n + q] * x[q][c];
-            x[i][c] = s / Lb[int64_t(i) * n + i];
-        }
-    }
+    for (int i = 0; i < kb; ++i)
+        if (c < kb) l[i][c] = Lb[int64_t(i) * n + c];
     __syncthreads();
-    for (int e = threadIdx.x; e < NB * NB; e += blockDim.x) {
-        const int i = e / NB, j = e % NB;
-        Li[e] = (i < kb && j < kb) ? x[i][j] : 0.0;
+    // column c of the inverse, written straight to Li and read back by the same thread
+    double *xc = Li + c;
+    for (int i = 0; i < NB; ++i) {
+        double v = 0.0;
+        if (c < kb && i >= c && i < kb) {
+            double s = (i == c) ? 1.0 : 0.0;
+            for (int q = c; q < i; ++q) s -= l[i][q] * xc[q * NB];
+            v = s / l[i][i];
+        }
+        xc[i * NB] = v;
     }
 }
 

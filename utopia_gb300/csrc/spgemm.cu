@@ -113,20 +113,38 @@ __global__ void k_transpose_scatter(const int32_t *rp, const int32_t *ci, const 
 // sort every row by column (insertion sort; rows of transposed transfer operators are short)
 template <class V>
 __global__ void k_sort_rows(const int64_t *tp, int64_t n, int32_t *tci, V *tcv) {
-    for (int64_t r = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; r < n; r += int64_t(gridDim.x) * blockDim.x) {
-        int64_t a = tp[r], b = tp[r + 1];
-        for (int64_t i = a + 1; i < b; ++i) {
-            int32_t key = tci[i];
-            V val = tcv[i];
-            int64_t j = i - 1;
-            while (j >= a && tci[j] > key) {
-                tci[j + 1] = tci[j];
-                tcv[j + 1] = tcv[j];
-                --j;
+    // a warp per row: rows of at most 32 entries are placed by rank (the keys of a row are
+    // distinct: they are the source rows of one column), longer rows by one lane's insertion sort
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t r = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5; r < n; r += nw) {
+        const int64_t a = tp[r], b = tp[r + 1];
+        const int64_t len = b - a;
+        if (len <= 1) continue;
+        if (len <= 32) {
+            const int32_t key = lane < len ? tci[a + lane] : INT32_MAX;
+            const V val = lane < len ? tcv[a + lane] : V{};
+            int rank = 0;
+            for (int t = 0; t < int(len); ++t) rank += __shfl_sync(0xffffffffu, key, t) < key ? 1 : 0;
+            if (lane < len) {
+                tci[a + rank] = key;
+                tcv[a + rank] = val;
             }
-            tci[j + 1] = key;
-            tcv[j + 1] = val;
+        } else if (lane == 0) {
+            for (int64_t i = a + 1; i < b; ++i) {
+                const int32_t key = tci[i];
+                const V val = tcv[i];
+                int64_t j = i - 1;
+                while (j >= a && tci[j] > key) {
+                    tci[j + 1] = tci[j];
+                    tcv[j + 1] = tcv[j];
+                    --j;
+                }
+                tci[j + 1] = key;
+                tcv[j + 1] = val;
+            }
         }
+        __syncwarp();
     }
 }
 
@@ -597,7 +615,7 @@ std::unique_ptr<Mat> transpose(const Mat &A, bool finalize) {
                 A.rowptr.as<int32_t>(), A.colidx.as<int32_t>(), A.vals.as<V>(), A.nrows, fill.as<int64_t>(),
                 tp64.as<int64_t>(), T->colidx.as<int32_t>(), T->vals.as<V>());
         if (A.ncols)
-            k_sort_rows<V><<<stream_grid(ctx, A.ncols), kBlock, 0, ctx.stream>>>(tp64.as<int64_t>(), A.ncols,
+            k_sort_rows<V><<<stream_grid(ctx, A.ncols * 32), kBlock, 0, ctx.stream>>>(tp64.as<int64_t>(), A.ncols,
                                                                                 T->colidx.as<int32_t>(),
                                                                                 T->vals.as<V>());
         ctx.launches += 2;
