@@ -213,6 +213,7 @@ __global__ void __launch_bounds__(kGemvThreads) k_gemv(const T *M, int64_t n, co
 }  // namespace
 
 void DenseCholesky::make_fp32_inverse() {
+    UGPU_CHECK(!tri, UGPU_ERR_UNSUPPORTED, "coarse solver: no FP32 inverse above the factored-inverse size");
     Ainv32.alloc(sizeof(float) * std::max<int64_t>(n * n, 1));
     if (n) launch_convert(*ctx, Ainv.ptr, UGPU_F64, Ainv32.ptr, UGPU_F32, n * n);
 }
@@ -307,6 +308,15 @@ bool DenseCholesky::factor(const Mat &A) {
         UGPU_LAUNCH_CHECK();
     };
     tri_inv(0, n);
+    tmp_d.ensure(sizeof(double) * size_t(n));
+    tri = n > kDenseTriMin;
+    if (tri) {  // Y in the lower triangle, Y^T in the upper one; L keeps the factor
+        k_mirror_lower<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Y, n);
+        c.launches++;
+        UGPU_LAUNCH_CHECK();
+        UGPU_CUDA(cudaStreamSynchronize(c.stream));
+        return true;
+    }
     // Ainv = Y^T Y (stored in L's buffer, then swapped): the lower triangle's tiles, then mirrored
     // (the product is symmetric bit for bit: (i, j) and (j, i) sum the same products in one order)
     {
@@ -414,9 +424,54 @@ __global__ void __launch_bounds__(256) k_gemv64_split(const double *M, int64_t n
     }
 }
 
+// One triangle of the tri form: out_i = sum over j <= i (LOWER) or j >= i of M[i][j] in_j, a warp per
+// row (row segments are contiguous, the lanes' loads coalesced), four partial sums per lane.
+template <class VI, class VO, bool LOWER>
+__global__ void __launch_bounds__(256) k_gemv64_tri(const double *M, int64_t n, const VI *in, VO *out,
+                                                    const int *done) {
+    if (done && *done) return;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = (int64_t(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t i = (blockIdx.x * int64_t(blockDim.x) + threadIdx.x) >> 5; i < n; i += nw) {
+        const double *row = M + i * n;
+        const int64_t lo = LOWER ? 0 : i, hi = LOWER ? i + 1 : n;
+        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+        int64_t c = lo + lane;
+        for (; c + 96 < hi; c += 128) {
+            s0 = fma(__ldg(row + c), cvt<double>(__ldg(in + c)), s0);
+            s1 = fma(__ldg(row + c + 32), cvt<double>(__ldg(in + c + 32)), s1);
+            s2 = fma(__ldg(row + c + 64), cvt<double>(__ldg(in + c + 64)), s2);
+            s3 = fma(__ldg(row + c + 96), cvt<double>(__ldg(in + c + 96)), s3);
+        }
+        for (; c < hi; c += 32) s0 = fma(__ldg(row + c), cvt<double>(__ldg(in + c)), s0);
+        const double s = warp_sum((s0 + s1) + (s2 + s3));
+        if (lane == 0) out[i] = cvt<VO>(s);
+    }
+}
+
 void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int *done) {
     Context &c = *ctx;
     if (n == 0) return;
+    if (tri) {  // x = Y^T (Y r), the intermediate in FP64
+        UGPU_CHECK((rdt == UGPU_F64 || rdt == UGPU_F32) && rdt == xdt, UGPU_ERR_UNSUPPORTED,
+                   "coarse solve: FP64 or FP32 vectors");
+        const int gw = int(std::min<int64_t>((n + 7) / 8, int64_t(c.sms) * 8));  // a warp per row, 8 per CTA
+        double *t = tmp_d.as<double>();
+        if (rdt == UGPU_F64) {
+            k_gemv64_tri<double, double, true><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n,
+                                                                         static_cast<const double *>(rhs), t, done);
+            k_gemv64_tri<double, double, false><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n, t,
+                                                                          static_cast<double *>(x), done);
+        } else {
+            k_gemv64_tri<float, double, true><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n,
+                                                                        static_cast<const float *>(rhs), t, done);
+            k_gemv64_tri<double, float, false><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n, t,
+                                                                         static_cast<float *>(x), done);
+        }
+        c.launches += 2;
+        UGPU_LAUNCH_CHECK();
+        return;
+    }
     int g = int(std::min<int64_t>((n * 32 + 255) / 256, int64_t(c.sms) * 8));
     g = int(std::min<int64_t>(std::max<int64_t>(n, 1), int64_t(c.sms) * 8));
     auto al = [](const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; };

@@ -336,11 +336,16 @@ std::unique_ptr<Mat> ptap(const Mat &A, const Mat &P);
 std::unique_ptr<Mat> cast_matrix(const Mat &A, int vdtype);
 std::unique_ptr<Mat> make_csr_device(Context &ctx, int64_t nrows, int64_t ncols, int64_t nnz, int vdtype);
 
+constexpr int64_t kDenseTriMin = 4096;  // coarse sizes above which the inverse stays factored (tri)
 struct DenseCholesky {
     Context *ctx = nullptr;
     int64_t n = 0;
     Buffer L;      // n*n FP64, row-major, lower triangle
-    Buffer Ainv;   // n*n FP64 explicit inverse (L^-T L^-1), applied as one GEMV per coarse solve
+    Buffer Ainv;   // n*n FP64 explicit inverse (L^-T L^-1), applied as one GEMV per coarse solve; for n
+                   // above kDenseTriMin instead Y = L^-1 in the lower triangle and Y^T in the upper one
+                   // (tri), applied as two triangular GEMVs: the same FMAs per solve without the n^3
+                   // product Y^T Y at set-up
+    bool tri = false;
     Buffer Ainv32; // its FP32 copy for FP32 vectors (make_fp32_inverse; dropped by factor())
     Buffer tmp_d;  // FP64 rhs/solution staging
     bool factor(const Mat &A);           // returns false if not SPD
