@@ -449,79 +449,27 @@ __global__ void __launch_bounds__(256) k_gemv64_tri(const double *M, int64_t n, 
     }
 }
 
-// The same triangle with the input staged in shared memory (FP64) and each row split over four
-// warps, two rows per CTA, as k_gemv64_split does for the full inverse
-template <class VI, class VO, bool LOWER>
-__global__ void __launch_bounds__(256) k_gemv64_split_tri(const double *M, int64_t n, const VI *in, VO *out,
-                                                          const int *done) {
-    extern __shared__ __align__(16) double sr[];
-    __shared__ double part[8];
-    if (done && *done) return;
-    for (int64_t j = threadIdx.x; j < n; j += blockDim.x) sr[j] = cvt<double>(in[j]);
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rl = warp >> 2, q = warp & 3;
-    for (int64_t i0 = 2 * int64_t(blockIdx.x); i0 < n; i0 += 2 * int64_t(gridDim.x)) {
-        const int64_t i = i0 + rl;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-        if (i < n) {
-            const double *row = M + i * n;
-            const int64_t lo = LOWER ? 0 : i, len = LOWER ? i + 1 : n - i;
-            const int64_t c0 = lo + q * len / 4, c1 = lo + (q + 1) * len / 4;
-            int64_t c = c0 + lane;
-            for (; c + 96 < c1; c += 128) {
-                s0 = fma(__ldg(row + c), sr[c], s0);
-                s1 = fma(__ldg(row + c + 32), sr[c + 32], s1);
-                s2 = fma(__ldg(row + c + 64), sr[c + 64], s2);
-                s3 = fma(__ldg(row + c + 96), sr[c + 96], s3);
-            }
-            for (; c < c1; c += 32) s0 = fma(__ldg(row + c), sr[c], s0);
-        }
-        const double s = warp_sum((s0 + s1) + (s2 + s3));
-        if (lane == 0) part[warp] = s;
-        __syncthreads();
-        if (threadIdx.x < 2 && i0 + threadIdx.x < n) {
-            const double *pp = part + 4 * threadIdx.x;
-            out[i0 + threadIdx.x] = cvt<VO>((pp[0] + pp[1]) + (pp[2] + pp[3]));
-        }
-        __syncthreads();
-    }
-}
-
-template <class VI, class VO, bool LOWER>
-void launch_tri(Context &c, const double *M, int64_t n, const VI *in, VO *out, const int *done) {
-    if (size_t(n) * sizeof(double) <= size_t(kGemvSmemMax)) {
-        static bool attr = false;
-        if (!attr) {
-            UGPU_CUDA(cudaFuncSetAttribute(k_gemv64_split_tri<VI, VO, LOWER>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, kGemvSmemMax));
-            attr = true;
-        }
-        const int gs = int(std::min<int64_t>((n + 1) / 2, int64_t(c.sms) * 8));  // two rows per CTA
-        k_gemv64_split_tri<VI, VO, LOWER><<<gs, 256, size_t(n) * sizeof(double), c.stream>>>(M, n, in, out, done);
-    } else {
-        const int gw = int(std::min<int64_t>((n + 7) / 8, int64_t(c.sms) * 8));  // a warp per row, 8 per CTA
-        k_gemv64_tri<VI, VO, LOWER><<<gw, 256, 0, c.stream>>>(M, n, in, out, done);
-    }
-    c.launches++;
-    UGPU_LAUNCH_CHECK();
-}
-
 void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int *done) {
     Context &c = *ctx;
     if (n == 0) return;
     if (tri) {  // x = Y^T (Y r), the intermediate in FP64
         UGPU_CHECK((rdt == UGPU_F64 || rdt == UGPU_F32) && rdt == xdt, UGPU_ERR_UNSUPPORTED,
                    "coarse solve: FP64 or FP32 vectors");
+        const int gw = int(std::min<int64_t>((n + 7) / 8, int64_t(c.sms) * 8));  // a warp per row, 8 per CTA
         double *t = tmp_d.as<double>();
-        const double *M = Ainv.as<double>();
         if (rdt == UGPU_F64) {
-            launch_tri<double, double, true>(c, M, n, static_cast<const double *>(rhs), t, done);
-            launch_tri<double, double, false>(c, M, n, t, static_cast<double *>(x), done);
+            k_gemv64_tri<double, double, true><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n,
+                                                                         static_cast<const double *>(rhs), t, done);
+            k_gemv64_tri<double, double, false><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n, t,
+                                                                          static_cast<double *>(x), done);
         } else {
-            launch_tri<float, double, true>(c, M, n, static_cast<const float *>(rhs), t, done);
-            launch_tri<double, float, false>(c, M, n, t, static_cast<float *>(x), done);
+            k_gemv64_tri<float, double, true><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n,
+                                                                        static_cast<const float *>(rhs), t, done);
+            k_gemv64_tri<double, float, false><<<gw, 256, 0, c.stream>>>(Ainv.as<double>(), n, t,
+                                                                         static_cast<float *>(x), done);
         }
+        c.launches += 2;
+        UGPU_LAUNCH_CHECK();
         return;
     }
     int g = int(std::min<int64_t>((n * 32 + 255) / 256, int64_t(c.sms) * 8));
