@@ -665,7 +665,7 @@ def main():
     res_plain = float(np.linalg.norm(b - A.matvec(x_plain)) / nb)
     err_mixed_vs_fp64 = float(np.linalg.norm(x_mixed - x_plain) / np.linalg.norm(x_plain))
 
-    # ---- roofline: the FP64 fine-level SpMV, timed alone (CSR byte model of the survey) ----
+    # ---- roofline: the FP64 fine-level SpMV, timed alone (the CSR byte model nnz (8 + 4) + 4 (n + 1) + 2 n 8) ----
     hbm, peak_kind = peaks()
     y = U.Vector(ctx, n=n)
     xr = U.Vector(ctx, np.random.default_rng(0).standard_normal(n))
