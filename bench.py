@@ -23,6 +23,9 @@ Stop at ||r||_2 <= 1e-8 ||b||_2, checked in FP64.
   * other_workloads: 256^2 CG + Jacobi, 128^3 FP64 MG-PCG (Chebyshev), the 1024^2 obstacle
     QP (MPRGP, multicolour PGS) and the 128^3 differentiable solve (--no-extra skips them).
 
+Other modes print their own line and are not the headline: --amg, --mmg, --qp (solvers beside the
+path), --spmv-only, --cg-jacobi, --transfers (profiling cases), --setup (the cold path in parts).
+
 --impl reference times only that CPU implementation (rank 0; other ranks exit).
 Multi-GPU: the path is not sharded here (one GPU per box); N ranks run N replicas.
 """
@@ -277,6 +280,92 @@ def run_amg(args):
                                "setup_ms": setup * 1e3, "sample": "one complete FP64 AMG-PCG solve on the oracle"}
     out["value"] = out["mixed"]["ms"]
     print(json.dumps(out), flush=True)
+
+
+def run_transfers(args):
+    """The transfers between the fine level and the next (trilinear P and R = P^T of the size^3 grid),
+    BF16 values with FP32 vectors and FP64: restriction R x and prolongation y = P x + v, each timed
+    by CUDA events around single launches with L2 flushed before each.  One JSON line."""
+    import torch
+    import utopia_gb300 as U
+    from utopia_gb300 import problems as P
+
+    ctx = U.Context(0)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    Pm = U.SparseMatrix(ctx, P.interpolation_3d(args.size))
+    Rm = Pm.transpose()
+    P16, R16 = Pm.cast(U.BF16), Rm.cast(U.BF16)
+    nf, nc = Pm.nrows, Pm.ncols
+    rng = np.random.default_rng(0)
+    rf32, xc32 = U.Vector(ctx, rng.standard_normal(nf), dtype=U.F32), U.Vector(ctx, rng.standard_normal(nc), dtype=U.F32)
+    yc32, yf32 = U.Vector(ctx, n=nc, dtype=U.F32), U.Vector(ctx, n=nf, dtype=U.F32)
+    rf64, yc64 = U.Vector(ctx, rng.standard_normal(nf)), U.Vector(ctx, n=nc)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    def t(fn, reps=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        tot = 0.0
+        for _ in range(reps):
+            flush.zero_()
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            tot += s.elapsed_time(e)
+        return tot / reps * 1e3
+
+    out = {"metric": f"transfer times {args.size}^3 <-> {args.size // 2}^3", "unit": "us",
+           "restrict_bf16_us": t(lambda: R16.apply(rf32, yc32)),
+           "prolong_add_bf16_us": t(lambda: P16.apply_add(xc32, rf32, yf32)),
+           "restrict_f64_us": t(lambda: Rm.apply(rf64, yc64)),
+           "R_sell": R16.sell_info(), "P_sell": P16.sell_info(), "l2": "flushed (256 MB write) before each launch"}
+    print(json.dumps(out), flush=True)
+
+
+def run_setup(args):
+    """The cold path of the headline solve in parts: operator upload (CSR from host arrays, validation,
+    sliced-ELL layout), transfer uploads, transfer set-up (transposes), hierarchy set-up (Galerkin
+    products, storage casts and layouts, coarse factorisation), the first solve (graph capture) and a
+    second one.  Host-timed with a synchronisation around each part, three repetitions.  One JSON line."""
+    import utopia_gb300 as U
+
+    A, Ps, b = make_problem(args.size)
+    ctx = U.Context(0)
+    nb = float(np.linalg.norm(b))
+    reps = []
+    for _ in range(3):
+        log = {}
+
+        def part(tag, fn):
+            ctx.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            ctx.synchronize()
+            log[tag] = (time.perf_counter() - t0) * 1e3
+            return r
+
+        A_d = part("operator_upload_ms", lambda: U.SparseMatrix(ctx, A))
+        P_d = part("transfer_upload_ms", lambda: [U.SparseMatrix(ctx, p) for p in Ps])
+        b_d = part("rhs_upload_ms", lambda: U.Vector(ctx, b))
+        mg = U.Multigrid(ctx, smoother="jacobi", omega=0.8, pre_smoothing_steps=2, post_smoothing_steps=2,
+                         precision=U.BF16)
+        part("transfer_setup_ms", lambda: mg.set_transfer_operators(P_d))
+        cg = U.ConjugateGradient(ctx, atol=RTOL * nb, flexible=1)
+        cg.set_preconditioner(mg)
+        x_d = U.Vector(ctx, n=A.nrows)
+        part("hierarchy_setup_ms", lambda: cg.update(A_d))
+        part("first_solve_ms", lambda: cg.apply(b_d, x_d))
+        x_d.set(0.0)
+        part("second_solve_ms", lambda: cg.apply(b_d, x_d))
+        part("download_ms", lambda: x_d.numpy())
+        reps.append(log)
+        del cg, mg, A_d, P_d, b_d, x_d
+    print(json.dumps({"metric": f"cold path in parts, {args.size}^3 mixed MG-PCG", "unit": "ms",
+                      "repetitions": reps}), flush=True)
 
 
 def qp_measure(ctx, N, scale, steps, eager=False, max_it=400000, pgs=True, pgs_max_it=None):
@@ -559,7 +648,19 @@ def main():
     ap.add_argument("--spmv-only", action="store_true",
                     help="profiling case: FP64 and FP32 products and a BF16 Jacobi sweep of the fine operator, "
                          "two launches each, nothing else")
+    ap.add_argument("--transfers", action="store_true",
+                    help="profiling case: the BF16 and FP64 restriction and the BF16 prolongation (add form) of "
+                         "the fine level to the next, L2 flushed between launches; one JSON line")
+    ap.add_argument("--setup", action="store_true",
+                    help="the cold path in parts (operator and transfer uploads, hierarchy set-up, first and "
+                         "second solve), three repetitions; one JSON line")
     args = ap.parse_args()
+    if args.transfers:
+        run_transfers(args)
+        return
+    if args.setup:
+        run_setup(args)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
