@@ -380,6 +380,47 @@ def test_spgemm_wide_rows_use_the_window_path(ctx, oracle):
     np.testing.assert_array_equal(C1.csr()[2], Ag.matmul(Bg).csr()[2])
 
 
+def test_spgemm_mid_tier_and_its_overflow(ctx, oracle):
+    """Rows of 129..1024 products go to the mid tier sized by distinct columns: rows whose
+    products land on a few dozen columns stay there, rows with more than 128 distinct columns
+    overflow to the full-size warp tier.  Both kinds in one product: the oracle's structure and
+    values, the same bits on a second run, and the same bits from a numeric-only recomputation
+    through a kept Galerkin plan."""
+    import scipy.sparse as sp
+
+    rng = np.random.default_rng(31)
+    n, m = 2000, 3000
+    rows, cols = [], []
+    for i in range(n):
+        k = 24 if i % 3 else 6  # 24 entries: ~24 x 20 products; 6: tier 1
+        rows += [i] * k
+        if i % 3 == 1:  # only B's concentrated rows: the products land on at most 40 columns
+            cols += list(2 * rng.choice(m // 2, k, replace=False))
+        else:
+            cols += list(rng.choice(m, k, replace=False))
+    A = sp.csr_matrix((rng.standard_normal(len(rows)), (rows, cols)), shape=(n, m))
+    # B: half the rows concentrated on 40 columns (few distinct products), half spread (many)
+    brows, bcols = [], []
+    for j in range(m):
+        pool = 40 if j % 2 == 0 else 2500
+        c = rng.choice(pool, 20, replace=False) + (0 if j % 2 == 0 else 40)
+        brows += [j] * 20
+        bcols += list(c)
+    B = sp.csr_matrix((rng.standard_normal(len(brows)), (brows, bcols)), shape=(m, 2540))
+    A.sort_indices()
+    B.sort_indices()
+    C = (A @ B).tocsr()
+    per_row = np.diff(C.indptr)
+    ub = A.astype(bool).astype(int) @ np.diff(B.indptr)
+    mid = (ub > 128) & (ub <= 1024)
+    assert (mid & (per_row <= 128)).any() and (mid & (per_row > 128)).any()
+    Ac, Bc = P.CSR.from_scipy(A), P.CSR.from_scipy(B)
+    Ag, Bg = U.SparseMatrix(ctx, Ac), U.SparseMatrix(ctx, Bc)
+    C1 = Ag.matmul(Bg)
+    _same_csr(C1, oracle.Matrix(Ac).matmul(oracle.Matrix(Bc)), "close")
+    np.testing.assert_array_equal(C1.csr()[2], Ag.matmul(Bg).csr()[2])
+
+
 def test_ptap_structure_bit_exact_fixture(ctx, oracle, laplace_hierarchy):
     A, Is, _ = laplace_hierarchy
     _same_csr(U.SparseMatrix(ctx, A).ptap(U.SparseMatrix(ctx, Is[2])), oracle.Matrix(A).ptap(oracle.Matrix(Is[2])),
