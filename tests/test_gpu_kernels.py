@@ -383,9 +383,8 @@ def test_spgemm_wide_rows_use_the_window_path(ctx, oracle):
 def test_spgemm_mid_tier_and_its_overflow(ctx, oracle):
     """Rows of 129..1024 products go to the mid tier sized by distinct columns: rows whose
     products land on a few dozen columns stay there, rows with more than 128 distinct columns
-    overflow to the full-size warp tier.  Both kinds in one product: the oracle's structure and
-    values, the same bits on a second run, and the same bits from a numeric-only recomputation
-    through a kept Galerkin plan."""
+    overflow to the full-size warp tier.  Both kinds in one product (666 and 667 rows): the
+    oracle's structure and values, and the same bits on a second run."""
     import scipy.sparse as sp
 
     rng = np.random.default_rng(31)
