@@ -103,17 +103,18 @@ __global__ void k_copy_block(const double *src, int64_t lds, double *dst, int64_
 
 // C[M x N] (ldc) += alpha * op(A) op(B); TA/TB: operand stored transposed.
 // lower_only: skip tiles strictly above the diagonal (SYRK-style update).
-template <bool TA, bool TB>
-__global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha, const double *A, int64_t lda,
-                                               const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
-                                               bool lower_only) {
-    constexpr int TM = 64, TN = 64, TK = 16;
+// T x T tiles (64 or 32), 256 threads as 16 x 16, each thread T/16 x T/16 outputs.
+template <bool TA, bool TB, int T>
+__global__ void __launch_bounds__(256) k_dgemm_t(int M, int N, int K, double alpha, const double *A, int64_t lda,
+                                                 const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                                                 bool lower_only) {
+    constexpr int TM = T, TN = T, TK = 16, PT = T / 16;
     __shared__ double As[TK][TM + 1];
     __shared__ double Bs[TK][TN + 1];
     const int bm = blockIdx.y * TM, bn = blockIdx.x * TN;
     if (lower_only && bn > bm + TM - 1) return;
     const int tx = threadIdx.x % 16, ty = threadIdx.x / 16;
-    double acc[4][4] = {};
+    double acc[PT][PT] = {};
     for (int k0 = 0; k0 < K; k0 += TK) {
         for (int e = threadIdx.x; e < TM * TK; e += 256) {
             int mm = e / TK, kk = e % TK;
@@ -132,29 +133,46 @@ __global__ void __launch_bounds__(256) k_dgemm(int M, int N, int K, double alpha
         __syncthreads();
 #pragma unroll
         for (int kk = 0; kk < TK; ++kk) {
-            double a[4], b[4];
+            double a[PT], b[PT];
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
+            for (int q = 0; q < PT; ++q) {
                 a[q] = As[kk][ty + 16 * q];
                 b[q] = Bs[kk][tx + 16 * q];
             }
 #pragma unroll
-            for (int p = 0; p < 4; ++p)
+            for (int p = 0; p < PT; ++p)
 #pragma unroll
-                for (int q = 0; q < 4; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
+                for (int q = 0; q < PT; ++q) acc[p][q] = fma(a[p], b[q], acc[p][q]);
         }
         __syncthreads();
     }
 #pragma unroll
-    for (int p = 0; p < 4; ++p)
+    for (int p = 0; p < PT; ++p)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
+        for (int q = 0; q < PT; ++q) {
             int gm = bm + ty + 16 * p, gn = bn + tx + 16 * q;
             if (gm < M && gn < N) {
                 double *c = C + int64_t(gm) * ldc + gn;
                 *c = (beta == 0.0 ? 0.0 : beta * *c) + alpha * acc[p][q];
             }
         }
+}
+
+// the GEMM with the tile that keeps the grid at least two CTAs per SM: 64 x 64 tiles where
+// there are that many, else 32 x 32 (a few hundred 64-tiles on 152 SMs leave SMs with one CTA
+// beside SMs with two, each pacing its FP64 pipe)
+template <bool TA, bool TB>
+void dgemm(Context &c, int M, int N, int K, double alpha, const double *A, int64_t lda, const double *B, int64_t ldb,
+           double beta, double *C, int64_t ldc, bool lower_only) {
+    const int64_t tiles64 = int64_t((M + 63) / 64) * ((N + 63) / 64);
+    if (tiles64 >= 2 * int64_t(c.sms)) {
+        dim3 grid(unsigned((N + 63) / 64), unsigned((M + 63) / 64));
+        k_dgemm_t<TA, TB, 64><<<grid, 256, 0, c.stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    } else {
+        dim3 grid(unsigned((N + 31) / 32), unsigned((M + 31) / 32));
+        k_dgemm_t<TA, TB, 32><<<grid, 256, 0, c.stream>>>(M, N, K, alpha, A, lda, B, ldb, beta, C, ldc, lower_only);
+    }
+    c.launches++;
 }
 
 // A[i][j] = A[j][i] for j > i (the strictly upper triangle from the lower one)
@@ -266,12 +284,9 @@ bool DenseCholesky::factor(const Mat &A) {
         if (rest > 0) {
             double *A21 = Lp + (k0 + kb) * n + k0;
             copy_block(A21, n, Tp, kb, int(rest), kb);
-            dim3 gp(unsigned((kb + 63) / 64), unsigned((rest + 63) / 64));
-            k_dgemm<false, true><<<gp, 256, 0, c.stream>>>(int(rest), kb, kb, 1.0, Tp, kb, Lb, NB, 0.0, A21, n, false);
-            dim3 grid(unsigned((rest + 63) / 64), unsigned((rest + 63) / 64));
-            k_dgemm<false, true><<<grid, 256, 0, c.stream>>>(int(rest), int(rest), kb, -1.0, A21, n, A21, n, 1.0,
-                                                             Lp + (k0 + kb) * n + k0 + kb, n, true);
-            c.launches += 2;
+            dgemm<false, true>(c, int(rest), kb, kb, 1.0, Tp, kb, Lb, NB, 0.0, A21, n, false);
+            dgemm<false, true>(c, int(rest), int(rest), kb, -1.0, A21, n, A21, n, 1.0, Lp + (k0 + kb) * n + k0 + kb,
+                               n, true);
         }
         UGPU_LAUNCH_CHECK();
     }
@@ -297,14 +312,12 @@ bool DenseCholesky::factor(const Mat &A) {
         tri_inv(r0, h);
         tri_inv(r0 + h, m - h);
         const int64_t m2 = m - h;
-        dim3 grid(unsigned((h + 63) / 64), unsigned((m2 + 63) / 64));
         // W = L21 Y11  (m2 x h, leading dimension h)
-        k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(int(m2), int(h), int(h), 1.0, Lp + (r0 + h) * n + r0, n,
-                                                          Y + r0 * n + r0, n, 0.0, Wp, h, false);
+        dgemm<false, false>(c, int(m2), int(h), int(h), 1.0, Lp + (r0 + h) * n + r0, n, Y + r0 * n + r0, n, 0.0, Wp,
+                            h, false);
         // Y21 = -Y22 W
-        k_dgemm<false, false><<<grid, 256, 0, c.stream>>>(int(m2), int(h), int(m2), -1.0, Y + (r0 + h) * n + r0 + h,
-                                                          n, Wp, h, 0.0, Y + (r0 + h) * n + r0, n, false);
-        c.launches += 2;
+        dgemm<false, false>(c, int(m2), int(h), int(m2), -1.0, Y + (r0 + h) * n + r0 + h, n, Wp, h, 0.0,
+                            Y + (r0 + h) * n + r0, n, false);
         UGPU_LAUNCH_CHECK();
     };
     tri_inv(0, n);
@@ -320,10 +333,9 @@ bool DenseCholesky::factor(const Mat &A) {
     // Ainv = Y^T Y (stored in L's buffer, then swapped): the lower triangle's tiles, then mirrored
     // (the product is symmetric bit for bit: (i, j) and (j, i) sum the same products in one order)
     {
-        dim3 grid(unsigned((n + 63) / 64), unsigned((n + 63) / 64));
-        k_dgemm<true, false><<<grid, 256, 0, c.stream>>>(int(n), int(n), int(n), 1.0, Y, n, Y, n, 0.0, Lp, n, true);
+        dgemm<true, false>(c, int(n), int(n), int(n), 1.0, Y, n, Y, n, 0.0, Lp, n, true);
         k_mirror_lower<<<stream_grid(c, n * n), kBlock, 0, c.stream>>>(Lp, n);
-        c.launches += 2;
+        c.launches++;
         UGPU_LAUNCH_CHECK();
     }
     std::swap(L, Ainv);  // Ainv now holds the inverse; L holds L^-1 (kept for diagnostics)
