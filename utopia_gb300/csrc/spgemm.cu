@@ -199,10 +199,11 @@ __device__ __forceinline__ int hash_insert(int32_t *keys, int mask, int32_t c, i
     }
 }
 
+// the group's barrier: the CTA, or the lanes of gmask within a warp (a whole warp or a sub-warp group)
 template <bool CTA>
-__device__ __forceinline__ void group_sync() {
+__device__ __forceinline__ void group_sync(unsigned gmask) {
     if constexpr (CTA) __syncthreads();
-    else __syncwarp();
+    else __syncwarp(gmask);
 }
 
 // table size for a row: power of two >= 2 * upper bound (load factor <= 1/2)
@@ -218,14 +219,14 @@ template <class V, bool NUMERIC, bool CTA>
 __device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, double *vals, int32_t *lkeys,
                             double *lvals, int *s_count, const int32_t *arp, const int32_t *aci, const V *acv,
                             const int32_t *brp, const int32_t *bci, const V *bcv, int64_t *cnt_out,
-                            const int32_t *crp, int32_t *cci, V *ccv) {
+                            const int32_t *crp, int32_t *cci, V *ccv, unsigned gmask = 0xffffffffu) {
     const int mask = TS - 1;
     for (int s = tid; s < TS; s += G) {
         keys[s] = -1;
         if (NUMERIC) vals[s] = 0.0;
     }
     if (tid == 0) *s_count = 0;
-    group_sync<CTA>();
+    group_sync<CTA>(gmask);
     for (int32_t ka = arp[i]; ka < arp[i + 1]; ++ka) {
         const int32_t j = aci[ka];
         const double a = NUMERIC ? cvt<double>(acv[ka]) : 0.0;
@@ -234,11 +235,11 @@ __device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, do
             const int slot = hash_insert(keys, mask, bci[kb], NUMERIC ? nullptr : s_count);
             if (NUMERIC) vals[slot] = fma(a, cvt<double>(bcv[kb]), vals[slot]);
         }
-        group_sync<CTA>();  // every product of this j lands before the next j
+        group_sync<CTA>(gmask);  // every product of this j lands before the next j
     }
     if (!NUMERIC) {
         if (tid == 0) cnt_out[i] = *s_count;
-        group_sync<CTA>();
+        group_sync<CTA>(gmask);
         return;
     }
     // compact the occupied slots, then place each entry at its rank (sorted by column)
@@ -250,7 +251,7 @@ __device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, do
             lvals[p] = vals[s];
         }
     }
-    group_sync<CTA>();
+    group_sync<CTA>(gmask);
     const int u = *s_count;
     const int32_t base = crp[i];
     for (int e = tid; e < u; e += G) {
@@ -260,7 +261,7 @@ __device__ void row_product(int64_t i, int tid, int G, int TS, int32_t *keys, do
         cci[base + rank] = k;
         ccv[base + rank] = cvt<V>(lvals[e]);
     }
-    group_sync<CTA>();
+    group_sync<CTA>(gmask);
 }
 
 constexpr size_t kWarpSmem = (sizeof(int32_t) + sizeof(double)) * (kWarpTable + kWarpRowsUb) * kWarpsPerCta;
@@ -302,6 +303,39 @@ __global__ void __launch_bounds__(WARPS * 32) k_spgemm_warp(int64_t m, int64_t l
         }
         row_product<V, NUMERIC, false>(i, lane, 32, table_size(u, TABLE), keys, vals, lkeys, lvals, &s_count[w],
                                        arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
+    }
+}
+
+// Tier 0 with sub-warp groups: rows of at most kTier0Ub products (the A P rows of a Galerkin product
+// have a few to a few dozen) take a group of kSubLanes lanes each, kSubGroups groups per warp, each
+// with its own table; a whole warp per such row left most of its lanes idle.  The same per-column
+// accumulation order as the warp form (products land in A-row order), so the same bits.
+constexpr int kSubLanes = 8, kSubGroups = 32 / kSubLanes, kSubWarps = 8;
+constexpr size_t kSubSmem = (sizeof(int32_t) + sizeof(double)) * size_t(kTier0Table + kTier0Ub) * kSubWarps * kSubGroups;
+
+template <class V, bool NUMERIC>
+__global__ void __launch_bounds__(kSubWarps * 32) k_spgemm_sub(int64_t m, const int64_t *ub, const int32_t *arp,
+                                                             const int32_t *aci, const V *acv, const int32_t *brp,
+                                                             const int32_t *bci, const V *bcv, int64_t *cnt,
+                                                             const int32_t *crp, int32_t *cci, V *ccv) {
+    extern __shared__ unsigned char smem[];
+    constexpr int NG = kSubWarps * kSubGroups;  // groups per CTA
+    const int lane = threadIdx.x & 31;
+    const int g = threadIdx.x / kSubLanes;  // group within the CTA
+    const int tid = lane % kSubLanes;
+    const unsigned gmask = ((1u << kSubLanes) - 1u) << (lane & ~(kSubLanes - 1));
+    double *vals = reinterpret_cast<double *>(smem) + size_t(g) * kTier0Table;
+    double *lvals = reinterpret_cast<double *>(smem) + size_t(NG) * kTier0Table + size_t(g) * kTier0Ub;
+    int32_t *ibase = reinterpret_cast<int32_t *>(smem + sizeof(double) * (kTier0Table + kTier0Ub) * NG);
+    int32_t *keys = ibase + size_t(g) * kTier0Table;
+    int32_t *lkeys = ibase + size_t(NG) * kTier0Table + size_t(g) * kTier0Ub;
+    __shared__ int s_count[NG];
+    const int64_t ng = int64_t(gridDim.x) * NG;
+    for (int64_t i = int64_t(blockIdx.x) * NG + g; i < m; i += ng) {
+        const int64_t u = ub[i];
+        if (u > kTier0Ub) continue;  // the group's lanes agree: one row per group
+        row_product<V, NUMERIC, false>(i, tid, kSubLanes, table_size(u, kTier0Table), keys, vals, lkeys, lvals,
+                                       &s_count[g], arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, gmask);
     }
 }
 
@@ -678,9 +712,8 @@ void launch_warp_tiers(Context &ctx, const Mat &A, const Mat &B, unsigned long l
     auto grid = [&](int warps, int per_sm) {
         return int(std::max<int64_t>(1, std::min<int64_t>((m + warps - 1) / warps, int64_t(ctx.sms) * per_sm)));
     };
-    k_spgemm_warp<double, N, kTier0Table, kTier0Ub, kTier0Warps, false>
-        <<<grid(kTier0Warps, 8), kTier0Warps * 32, tier_smem<kTier0Table, kTier0Ub, kTier0Warps>(), ctx.stream>>>(
-            m, -1, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv, nullptr, nullptr);
+    k_spgemm_sub<double, N><<<grid(kSubWarps * kSubGroups, 8), kSubWarps * 32, kSubSmem, ctx.stream>>>(
+        m, ub, arp, aci, acv, brp, bci, bcv, cnt, crp, cci, ccv);
     ctx.launches++;
     if (max_ub > (unsigned long long)kTier0Ub) {
         k_spgemm_warp<double, N, kTier1Table, kTier1Ub, kTier1Warps, false>
