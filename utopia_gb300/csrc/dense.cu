@@ -391,7 +391,7 @@ __global__ void __launch_bounds__(256) k_gemv64_warp(const double *M, int64_t n,
 }
 
 // The same product for coarse levels whose right-hand side fits shared memory: r is converted to
-// FP64 once per CTA into shared memory, and each row is split over four warps (two rows per CTA),
+// FP64 once per CTA into shared memory, and each row is split over two warps (four rows per CTA),
 // so every lane has only a few independent 16-byte row loads and the grid keeps enough of them
 // in flight to stream the inverse at HBM rate.
 constexpr int kGemvSmemMax = 96 * 1024;  // bytes of r staged per CTA
@@ -404,14 +404,14 @@ __global__ void __launch_bounds__(256) k_gemv64_split(const double *M, int64_t n
     for (int64_t j = threadIdx.x; j < n; j += blockDim.x) sr[j] = cvt<double>(r[j]);
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rl = warp >> 2, q = warp & 3;  // row of the pair, quarter of the row
-    for (int64_t i0 = 2 * int64_t(blockIdx.x); i0 < n; i0 += 2 * int64_t(gridDim.x)) {
+    const int rl = warp >> 1, q = warp & 1;  // row of the four, half of the row
+    for (int64_t i0 = 4 * int64_t(blockIdx.x); i0 < n; i0 += 4 * int64_t(gridDim.x)) {
         const int64_t i = i0 + rl;
         double s0 = 0.0, s1 = 0.0;
         if (i < n) {
             const double *row = M + i * n;
             if (vec) {  // n even, rows 16-byte aligned: pairs [q n2 / 4, (q + 1) n2 / 4)
-                const int64_t n2 = n >> 1, c0 = q * n2 / 4, c1 = (q + 1) * n2 / 4;
+                const int64_t n2 = n >> 1, c0 = q * n2 / 2, c1 = (q + 1) * n2 / 2;
                 const double2 *rv = reinterpret_cast<const double2 *>(row);
                 const double2 *xv = reinterpret_cast<const double2 *>(sr);
 #pragma unroll 4
@@ -421,16 +421,16 @@ __global__ void __launch_bounds__(256) k_gemv64_split(const double *M, int64_t n
                     s1 = fma(a.y, b.y, s1);
                 }
             } else {
-                const int64_t c0 = q * n / 4, c1 = (q + 1) * n / 4;
+                const int64_t c0 = q * n / 2, c1 = (q + 1) * n / 2;
                 for (int64_t c = c0 + lane; c < c1; c += 32) s0 = fma(__ldg(row + c), sr[c], s0);
             }
         }
         const double s = warp_sum(s0 + s1);
         if (lane == 0) part[warp] = s;
         __syncthreads();
-        if (threadIdx.x < 2 && i0 + threadIdx.x < n) {
-            const double *pp = part + 4 * threadIdx.x;
-            x[i0 + threadIdx.x] = cvt<VT>((pp[0] + pp[1]) + (pp[2] + pp[3]));
+        if (threadIdx.x < 4 && i0 + threadIdx.x < n) {
+            const double *pp = part + 2 * threadIdx.x;
+            x[i0 + threadIdx.x] = cvt<VT>(pp[0] + pp[1]);
         }
         __syncthreads();
     }
@@ -491,7 +491,7 @@ void DenseCholesky::solve(const void *rhs, int rdt, void *x, int xdt, const int 
     const bool split = (rdt == xdt) && (rdt == UGPU_F64 || (rdt == UGPU_F32 && !Ainv32.ptr)) &&
                        size_t(n) * sizeof(double) <= size_t(kGemvSmemMax);
     if (split) {
-        const int gs = int(std::min<int64_t>((n + 1) / 2, int64_t(c.sms) * 8));  // two rows per CTA
+        const int gs = int(std::min<int64_t>((n + 3) / 4, int64_t(c.sms) * 8));  // four rows per CTA
         const size_t smem = size_t(n) * sizeof(double);
         const int vec = (n % 2 == 0) && al(Ainv.ptr);
         if (rdt == UGPU_F64) {
