@@ -79,22 +79,14 @@ __global__ void __launch_bounds__(NB) k_trinv_diag(const double *L, int64_t n, i
     for (int i = 0; i < kb; ++i)
         if (c < kb) l[i][c] = Lb[int64_t(i) * n + c];
     __syncthreads();
-    // column c of the inverse, written straight to Li and read back by the same thread; each
-    // row's sum in four independent partial sums, so the loads and FMAs of consecutive terms overlap
+    // column c of the inverse, written straight to Li and read back by the same thread
     double *xc = Li + c;
     for (int i = 0; i < NB; ++i) {
         double v = 0.0;
         if (c < kb && i >= c && i < kb) {
-            double s0 = (i == c) ? 1.0 : 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
-            int q = c;
-            for (; q + 3 < i; q += 4) {
-                s0 -= l[i][q] * xc[q * NB];
-                s1 -= l[i][q + 1] * xc[(q + 1) * NB];
-                s2 -= l[i][q + 2] * xc[(q + 2) * NB];
-                s3 -= l[i][q + 3] * xc[(q + 3) * NB];
-            }
-            for (; q < i; ++q) s0 -= l[i][q] * xc[q * NB];
-            v = ((s0 + s1) + (s2 + s3)) / l[i][i];
+            double s = (i == c) ? 1.0 : 0.0;
+            for (int q = c; q < i; ++q) s -= l[i][q] * xc[q * NB];
+            v = s / l[i][i];
         }
         xc[i * NB] = v;
     }
